@@ -1,0 +1,449 @@
+// bulk.cu -- plans, tables and launch sequences of the bulk propagator.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+#include "bulk_reg.cuh"
+
+namespace {
+
+int pow2_floor(int v) {
+  int p = 1;
+  while (p * 2 <= v) p *= 2;
+  return p;
+}
+
+bool make_plan(int n, Plan1D& P) {
+  std::memset(&P, 0, sizeof(P));
+  P.n = n;
+  int m = n;
+  while (m % 8 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 8; m /= 8; }
+  while (m % 4 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 4; m /= 4; }
+  while (m % 2 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 2; m /= 2; }
+  while (m % 3 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 3; m /= 3; }
+  while (m % 5 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 5; m /= 5; }
+  if (m != 1) return false;
+  int tpl = pow2_floor(n / 8 > 0 ? n / 8 : 1);
+  if (tpl > 64) tpl = 64;
+  P.tpl = tpl;
+  P.lpc = BULK_THREADS / tpl;
+  P.ld = n + 1;
+  return true;
+}
+
+// signed wave number of index i (mod_fourier.f90:178-186)
+double wavenum(int i, int n, double L) {
+  double m = (i > n / 2) ? double(i - n) : double(i);
+  return 2.0 * M_PI * m / L;
+}
+
+template <typename T>
+size_t plan_smem(const Plan1D& P) {
+  size_t twn = (P.n + 1) & ~1;
+  return (twn + 2 * (size_t)P.lpc * P.ld) * sizeof(cplx<T>);
+}
+
+template <typename T>
+BulkDev<T>& hb(adscf_ctx* c);
+template <>
+BulkDev<float>& hb<float>(adscf_ctx* c) { return c->hb32; }
+template <>
+BulkDev<double>& hb<double>(adscf_ctx* c) { return c->hb64; }
+
+bool is_pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+int reg_size(int n) { return (n == 32 || n == 64 || n == 128 || n == 256) ? n : 0; }
+
+template <typename T>
+size_t reg_smem(int n) {
+  switch (n) {
+    case 32: return regk::Layout<T, 32>::bytes;
+    case 64: return regk::Layout<T, 64>::bytes;
+    case 128: return regk::Layout<T, 128>::bytes;
+    case 256: return regk::Layout<T, 256>::bytes;
+  }
+  return 0;
+}
+int reg_lpc(int n) {
+  switch (n) {
+    case 32: return BULK_THREADS / regk::Cfg<32>::TPL;
+    case 64: return BULK_THREADS / regk::Cfg<64>::TPL;
+    case 128: return BULK_THREADS / regk::Cfg<128>::TPL;
+    case 256: return BULK_THREADS / regk::Cfg<256>::TPL;
+  }
+  return 0;
+}
+
+template <typename T>
+int set_reg_attrs(adscf_ctx* ctx) {
+#define ADSCF_ATTR(NN)                                                                        \
+  CK(cudaFuncSetAttribute(k_rx<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,          \
+                          (int)regk::Layout<T, NN>::bytes));                                  \
+  CK(cudaFuncSetAttribute(k_rs<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,          \
+                          (int)regk::Layout<T, NN>::bytes));
+  ADSCF_ATTR(32) ADSCF_ATTR(64) ADSCF_ATTR(128) ADSCF_ATTR(256)
+#undef ADSCF_ATTR
+  return ADSCF_OK;
+}
+
+// X pass launch: register kernel for 32..256-point rows, generic otherwise
+template <typename T>
+void launch_x(adscf_ctx* ctx, int t, int mode, XAux aux) {
+  const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
+  const cplx<T>* tw = static_cast<const cplx<T>*>(ctx->d_tw);
+  cudaStream_t s = ctx->stream;
+  const dim3 g(ctx->n_work_x), b(BULK_THREADS);
+  switch (ctx->regx) {
+    case 32: k_rx<T, 32><<<g, b, ctx->smem_x, s>>>(d, ctx->d_work_x, tw, t, mode, aux); break;
+    case 64: k_rx<T, 64><<<g, b, ctx->smem_x, s>>>(d, ctx->d_work_x, tw, t, mode, aux); break;
+    case 128: k_rx<T, 128><<<g, b, ctx->smem_x, s>>>(d, ctx->d_work_x, tw, t, mode, aux); break;
+    case 256: k_rx<T, 256><<<g, b, ctx->smem_x, s>>>(d, ctx->d_work_x, tw, t, mode, aux); break;
+    default: k_bulk_xpass<T><<<g, b, ctx->smem_x, s>>>(d, ctx->d_work_x, tw, t, mode, aux);
+  }
+}
+
+// Y (kind 0/1) and Z (kind 2/3/4) pass launch
+template <typename T>
+void launch_s(adscf_ctx* ctx, int t, int kind) {
+  const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
+  const cplx<T>* tw = static_cast<const cplx<T>*>(ctx->d_tw);
+  const T* fk = static_cast<const T*>(ctx->d_fk);
+  const double2* tw64 = static_cast<const double2*>(ctx->d_tw64);
+  const double* g64 = ctx->d_g64;
+  cudaStream_t s = ctx->stream;
+  const bool z = kind >= 2;
+  const int n = z ? ctx->regz : ctx->regy;
+  const int2* work = z ? ctx->d_work_z : ctx->d_work_y;
+  const dim3 g(z ? ctx->n_work_z : ctx->n_work_y), b(BULK_THREADS);
+  const size_t sm = z ? ctx->smem_z : ctx->smem_y;
+  switch (n) {
+    case 32: k_rs<T, 32><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind); break;
+    case 64: k_rs<T, 64><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind); break;
+    case 128: k_rs<T, 128><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind); break;
+    case 256: k_rs<T, 256><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind); break;
+    default: k_bulk_strided<T><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind);
+  }
+}
+
+template <typename T>
+int create_t(adscf_ctx* ctx) {
+  BulkDev<T> I{};
+  I.gx = ctx->gx; I.gy = ctx->gy; I.gz = ctx->gz;
+  I.npts = ctx->npts;
+  I.ns = ctx->ns; I.na = ctx->na; I.nb = ctx->nb;
+  if (!make_plan(ctx->gx, I.px) || !make_plan(ctx->gy, I.py) || !make_plan(ctx->gz, I.pz))
+    return set_err(ctx, ADSCF_E_ARG, "grid sizes must be products of 2, 3 and 5");
+  // twiddle tables W_n^m = exp(-2 pi i m / n), computed in FP64
+  std::vector<int> ns = {ctx->gx, ctx->gy, ctx->gz};
+  std::vector<cplx<T>> tw;
+  int offs[3];
+  for (int d = 0; d < 3; ++d) {
+    int found = -1;
+    for (int e = 0; e < d; ++e)
+      if (ns[e] == ns[d]) found = offs[e];
+    if (found >= 0) { offs[d] = found; continue; }
+    offs[d] = (int)tw.size();
+    for (int m = 0; m < ns[d]; ++m) {
+      const double a = -2.0 * M_PI * (double)m / (double)ns[d];
+      tw.push_back(mk<T>((T)std::cos(a), (T)std::sin(a)));
+    }
+  }
+  I.px.tw_off = offs[0]; I.py.tw_off = offs[1]; I.pz.tw_off = offs[2];
+  // diffusion factors exp(-ds k^2) (mod_fourier.f90:188): g_xy[y][x] and
+  // g_z[z]/N, each as T plus its rounding residue (hi, lo)
+  const double ds = ctx->p.ds;
+  const double invn = 1.0 / ((double)ctx->gx * ctx->gy * ctx->gz);
+  const int nxy = ctx->gx * ctx->gy;
+  std::vector<T> fk(2 * (size_t)nxy + 2 * (size_t)ctx->gz);
+  I.gxy_off = 0;
+  I.gz_off = 2 * nxy;
+  for (int y = 0; y < ctx->gy; ++y) {
+    const double ky = wavenum(y, ctx->gy, ctx->p.sizey);
+    for (int x = 0; x < ctx->gx; ++x) {
+      const double kx = wavenum(x, ctx->gx, ctx->p.sizex);
+      const double g = std::exp(-ds * kx * kx) * std::exp(-ds * ky * ky);
+      const T h = (T)g;
+      fk[(size_t)y * ctx->gx + x] = h;
+      fk[(size_t)nxy + y * ctx->gx + x] = (T)(g - (double)h);
+    }
+  }
+  std::vector<double> g64(ctx->gz);
+  std::vector<double2> tw64(ctx->gz);
+  for (int z = 0; z < ctx->gz; ++z) {
+    const double kz = wavenum(z, ctx->gz, ctx->p.sizez);
+    const double g = std::exp(-ds * kz * kz) * invn;
+    const T h = (T)g;
+    fk[I.gz_off + z] = h;
+    fk[I.gz_off + ctx->gz + z] = (T)(g - (double)h);
+    g64[z] = g;
+    const double a = -2.0 * M_PI * (double)z / (double)ctx->gz;
+    tw64[z] = make_double2(std::cos(a), std::sin(a));
+  }
+  I.tw64_off = 0;
+  I.g64_off = 0;
+  CK(cudaMalloc(&ctx->d_tw64, tw64.size() * sizeof(double2)));
+  CK(cudaMemcpy(ctx->d_tw64, tw64.data(), tw64.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&ctx->d_g64, g64.size() * sizeof(double)));
+  CK(cudaMemcpy(ctx->d_g64, g64.data(), g64.size() * sizeof(double), cudaMemcpyHostToDevice));
+
+  CK(cudaMalloc(&ctx->d_tw, tw.size() * sizeof(cplx<T>)));
+  CK(cudaMemcpy(ctx->d_tw, tw.data(), tw.size() * sizeof(cplx<T>), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&ctx->d_fk, fk.size() * sizeof(T)));
+  CK(cudaMemcpy(ctx->d_fk, fk.data(), fk.size() * sizeof(T), cudaMemcpyHostToDevice));
+
+  const size_t np = (size_t)ctx->npts;
+  cplx<T>* spec = nullptr;
+  cplx<T>* slices = nullptr;
+  T* E = nullptr;
+  const size_t ne = sizeof(T) == 4 ? 4 * np : 2 * np;   // FP32 keeps the residue
+  if (cudaMalloc(&spec, np * sizeof(cplx<T>)) != cudaSuccess ||
+      cudaMalloc(&slices, (size_t)(ctx->ns + 1) * np * sizeof(cplx<T>)) != cudaSuccess ||
+      cudaMalloc(&E, ne * sizeof(T)) != cudaSuccess) {
+    cudaFree(spec); cudaFree(slices); cudaFree(E);
+    cudaGetLastError();
+    return set_err(ctx, ADSCF_E_OOM, "device allocation of propagator slices failed");
+  }
+  I.spec = spec; I.slices = slices; I.E = E;
+  I.Elo = sizeof(T) == 4 ? E + 2 * np : nullptr;
+  I.dist = ctx->d_dist;
+  ctx->contour_blocks = (int)std::min<size_t>((np + BULK_THREADS - 1) / BULK_THREADS, 152 * 4);
+  CK(cudaMalloc(&ctx->d_qpart, ctx->contour_blocks * sizeof(double)));
+  I.qpart = ctx->d_qpart;
+
+  // work lists (single instance)
+  auto mkwork = [&](int ntiles, int2*& d, int& n) -> int {
+    std::vector<int2> w(ntiles);
+    for (int i = 0; i < ntiles; ++i) w[i] = make_int2(0, i);
+    n = ntiles;
+    CK(cudaMalloc(&d, ntiles * sizeof(int2)));
+    CK(cudaMemcpy(d, w.data(), ntiles * sizeof(int2), cudaMemcpyHostToDevice));
+    return ADSCF_OK;
+  };
+  int rc;
+  // per-axis kernel choice: register FFT for 32..256-point lines (the strided
+  // passes also need a power-of-two gx for their line indexing)
+  ctx->regx = ctx->use_generic ? 0 : reg_size(ctx->gx);
+  ctx->regy = (ctx->use_generic || !is_pow2(ctx->gx)) ? 0 : reg_size(ctx->gy);
+  ctx->regz = (ctx->use_generic || !is_pow2(ctx->gx)) ? 0 : reg_size(ctx->gz);
+  const int lx = ctx->regx ? reg_lpc(ctx->regx) : I.px.lpc;
+  const int ly = ctx->regy ? reg_lpc(ctx->regy) : I.py.lpc;
+  const int lz = ctx->regz ? reg_lpc(ctx->regz) : I.pz.lpc;
+  if ((rc = mkwork((ctx->gy * ctx->gz + lx - 1) / lx, ctx->d_work_x, ctx->n_work_x))) return rc;
+  if ((rc = mkwork((ctx->gx * ctx->gz + ly - 1) / ly, ctx->d_work_y, ctx->n_work_y))) return rc;
+  if ((rc = mkwork((ctx->gx * ctx->gy + lz - 1) / lz, ctx->d_work_z, ctx->n_work_z))) return rc;
+  ctx->smem_x = ctx->regx ? reg_smem<T>(ctx->regx) : plan_smem<T>(I.px);
+  ctx->smem_y = ctx->regy ? reg_smem<T>(ctx->regy) : plan_smem<T>(I.py);
+  ctx->smem_z = ctx->regz ? reg_smem<T>(ctx->regz)
+                          : plan_smem<T>(I.pz) + 16 + (((I.pz.n + 1) & ~1) + 2 * (size_t)I.pz.ld) * sizeof(double2);
+  size_t mx = std::max(ctx->smem_x, std::max(ctx->smem_y, ctx->smem_z));
+  if (mx > 227 * 1024) return set_err(ctx, ADSCF_E_ARG, "grid line too long for shared memory");
+  CK(cudaFuncSetAttribute(k_bulk_xpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+  CK(cudaFuncSetAttribute(k_bulk_strided<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+  if ((rc = set_reg_attrs<T>(ctx))) return rc;
+
+  CK(cudaMalloc(&ctx->d_inst, sizeof(BulkDev<T>)));
+  CK(cudaMemcpy(ctx->d_inst, &I, sizeof(I), cudaMemcpyHostToDevice));
+  hb<T>(ctx) = I;
+  return ADSCF_OK;
+}
+
+template <typename T>
+int chains_t(adscf_ctx* ctx) {
+  const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
+  const cplx<T>* tw = static_cast<const cplx<T>*>(ctx->d_tw);
+  const T* fk = static_cast<const T*>(ctx->d_fk);
+  const double2* tw64 = static_cast<const double2*>(ctx->d_tw64);
+  const double* g64 = ctx->d_g64;
+  cudaStream_t s = ctx->stream;
+  XAux none{nullptr, nullptr, nullptr};
+  launch_x<T>(ctx, 0, XM_INIT, none);
+  for (int t = 1; t <= ctx->ns; ++t) {
+    launch_s<T>(ctx, t, 0);
+    launch_s<T>(ctx, t, 2);
+    launch_s<T>(ctx, t, 1);
+    launch_x<T>(ctx, t, XM_STEP, none);
+  }
+  CK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+template <typename T>
+int contour_t(adscf_ctx* ctx) {
+  const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
+  k_bulk_contour<T><<<dim3(ctx->contour_blocks, 1), BULK_THREADS, 0, ctx->stream>>>(d, ctx->p.ds);
+  CK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+template <typename T>
+int propagate_t(adscf_ctx* ctx) {
+  int rc = chains_t<T>(ctx);
+  return rc ? rc : contour_t<T>(ctx);
+}
+
+template <typename T>
+int expfield_t(adscf_ctx* ctx, const double* d_w) {
+  T* E = hb<T>(ctx).E;
+  const size_t n = 2 * (size_t)ctx->npts;
+  k_expfield<T><<<std::min<size_t>((n + 255) / 256, 152 * 8), 256, 0, ctx->stream>>>(d_w, E, hb<T>(ctx).Elo, n, ctx->p.ds);
+  CK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+// one Propagate_Step on a single real field: prop <- E IFFT(G FFT(E prop))
+template <typename T>
+int step_single_t(adscf_ctx* ctx, double* d_prop, const double* d_e) {
+  BulkDev<T>& I = hb<T>(ctx);
+  const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
+  const cplx<T>* tw = static_cast<const cplx<T>*>(ctx->d_tw);
+  const T* fk = static_cast<const T*>(ctx->d_fk);
+  const double2* tw64 = static_cast<const double2*>(ctx->d_tw64);
+  const double* g64 = ctx->d_g64;
+  cudaStream_t s = ctx->stream;
+  const size_t n = (size_t)ctx->npts;
+  // T staging inside the slice buffer: [prop | E]
+  T* tp = reinterpret_cast<T*>(I.slices);
+  T* te = tp + n;
+  const int gb = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+  k_convert<T, double><<<gb, 256, 0, s>>>(d_prop, tp, n);
+  k_convert<T, double><<<gb, 256, 0, s>>>(d_e, te, n);
+  XAux a{tp, nullptr, te};
+  launch_x<T>(ctx, 0, XM_R2S, a);
+  launch_s<T>(ctx, 0, 0);
+  launch_s<T>(ctx, 0, 2);
+  launch_s<T>(ctx, 0, 1);
+  XAux b{nullptr, tp, te};
+  launch_x<T>(ctx, 0, XM_S2R, b);
+  k_convert<double, T><<<gb, 256, 0, s>>>(tp, d_prop, n);
+  CK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+// forward 3D transform of a real field (Real2Fourier: scaled 1/N), returns the
+// r2c half spectrum [gz][gy][gx/2+1] interleaved on the host
+template <typename T>
+int r2c_t(adscf_ctx* ctx, const double* d_prop, double* h_half) {
+  BulkDev<T>& I = hb<T>(ctx);
+  const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
+  const cplx<T>* tw = static_cast<const cplx<T>*>(ctx->d_tw);
+  const T* fk = static_cast<const T*>(ctx->d_fk);
+  const double2* tw64 = static_cast<const double2*>(ctx->d_tw64);
+  const double* g64 = ctx->d_g64;
+  cudaStream_t s = ctx->stream;
+  const size_t n = (size_t)ctx->npts;
+  T* tp = reinterpret_cast<T*>(I.slices);
+  const int gb = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+  k_convert<T, double><<<gb, 256, 0, s>>>(d_prop, tp, n);
+  XAux a{tp, nullptr, nullptr};
+  launch_x<T>(ctx, 0, XM_R2S, a);
+  launch_s<T>(ctx, 0, 0);
+  launch_s<T>(ctx, 0, 3);
+  double2* full = reinterpret_cast<double2*>(ctx->d_tmp);  // needs 2*npts doubles
+  k_spec_to_f64<T><<<gb, 256, 0, s>>>(I.spec, full, n, 1.0 / (double)n);
+  CK(cudaGetLastError());
+  std::vector<double2> h(n);
+  CK(cudaMemcpyAsync(h.data(), full, n * sizeof(double2), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const int hx = ctx->gx / 2 + 1;
+  for (int z = 0; z < ctx->gz; ++z)
+    for (int y = 0; y < ctx->gy; ++y)
+      for (int x = 0; x < hx; ++x) {
+        const double2 v = h[((size_t)z * ctx->gy + y) * ctx->gx + x];
+        const size_t o = ((size_t)z * ctx->gy + y) * hx + x;
+        h_half[2 * o] = v.x;
+        h_half[2 * o + 1] = v.y;
+      }
+  return ADSCF_OK;
+}
+
+// Fourier2Real: unnormalised inverse of a Hermitian half spectrum
+template <typename T>
+int c2r_t(adscf_ctx* ctx, const double* h_half, double* d_prop) {
+  BulkDev<T>& I = hb<T>(ctx);
+  const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
+  const cplx<T>* tw = static_cast<const cplx<T>*>(ctx->d_tw);
+  const T* fk = static_cast<const T*>(ctx->d_fk);
+  const double2* tw64 = static_cast<const double2*>(ctx->d_tw64);
+  const double* g64 = ctx->d_g64;
+  cudaStream_t s = ctx->stream;
+  const size_t n = (size_t)ctx->npts;
+  const int gx = ctx->gx, gy = ctx->gy, gz = ctx->gz, hx = gx / 2 + 1;
+  std::vector<double2> h(n);
+  for (int z = 0; z < gz; ++z)
+    for (int y = 0; y < gy; ++y)
+      for (int x = 0; x < gx; ++x) {
+        double2 v;
+        if (x < hx) {
+          const size_t o = ((size_t)z * gy + y) * hx + x;
+          v = make_double2(h_half[2 * o], h_half[2 * o + 1]);
+        } else {  // Hermitian completion X(-k) = conj X(k)
+          const int xs = gx - x, ys = (gy - y) % gy, zs = (gz - z) % gz;
+          const size_t o = ((size_t)zs * gy + ys) * hx + xs;
+          v = make_double2(h_half[2 * o], -h_half[2 * o + 1]);
+        }
+        h[((size_t)z * gy + y) * gx + x] = v;
+      }
+  double2* full = reinterpret_cast<double2*>(ctx->d_tmp);
+  CK(cudaMemcpyAsync(full, h.data(), n * sizeof(double2), cudaMemcpyHostToDevice, s));
+  const int gb = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+  k_f64_to_spec<T><<<gb, 256, 0, s>>>(full, I.spec, n);
+  launch_s<T>(ctx, 0, 4);
+  launch_s<T>(ctx, 0, 1);
+  T* tp = reinterpret_cast<T*>(I.slices);
+  XAux b{nullptr, tp, nullptr};
+  launch_x<T>(ctx, 0, XM_S2R, b);
+  k_convert<double, T><<<gb, 256, 0, s>>>(tp, d_prop, n);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  return ADSCF_OK;
+}
+
+template <typename T>
+int mix_e_t(adscf_ctx* ctx) {
+  k_mix<T><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, hb<T>(ctx).E, hb<T>(ctx).Elo, ctx->p.ds);
+  CK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+}  // namespace
+
+int bulk_create(adscf_ctx* ctx) {
+  return ctx->prec == ADSCF_SPLIT ? create_t<float>(ctx) : create_t<double>(ctx);
+}
+
+void bulk_destroy(adscf_ctx* ctx) {
+  if (ctx->prec == ADSCF_SPLIT) {
+    cudaFree(ctx->hb32.spec); cudaFree(ctx->hb32.slices); cudaFree(ctx->hb32.E);
+  } else {
+    cudaFree(ctx->hb64.spec); cudaFree(ctx->hb64.slices); cudaFree(ctx->hb64.E);
+  }
+  cudaFree(ctx->d_inst); cudaFree(ctx->d_tw); cudaFree(ctx->d_fk);
+  cudaFree(ctx->d_tw64); cudaFree(ctx->d_g64);
+  cudaFree(ctx->d_work_x); cudaFree(ctx->d_work_y); cudaFree(ctx->d_work_z);
+  cudaFree(ctx->d_qpart);
+}
+
+int bulk_enqueue_propagate(adscf_ctx* ctx) {
+  return ctx->prec == ADSCF_SPLIT ? propagate_t<float>(ctx) : propagate_t<double>(ctx);
+}
+int bulk_enqueue_chains(adscf_ctx* ctx) {
+  return ctx->prec == ADSCF_SPLIT ? chains_t<float>(ctx) : chains_t<double>(ctx);
+}
+int bulk_enqueue_contour(adscf_ctx* ctx) {
+  return ctx->prec == ADSCF_SPLIT ? contour_t<float>(ctx) : contour_t<double>(ctx);
+}
+int bulk_enqueue_expfield(adscf_ctx* ctx, const double* d_w) {
+  return ctx->prec == ADSCF_SPLIT ? expfield_t<float>(ctx, d_w) : expfield_t<double>(ctx, d_w);
+}
+int bulk_step_single(adscf_ctx* ctx, double* d_prop, const double* d_e) {
+  return ctx->prec == ADSCF_SPLIT ? step_single_t<float>(ctx, d_prop, d_e) : step_single_t<double>(ctx, d_prop, d_e);
+}
+int bulk_r2c(adscf_ctx* ctx, const double* d_prop, double* h_half) {
+  return ctx->prec == ADSCF_SPLIT ? r2c_t<float>(ctx, d_prop, h_half) : r2c_t<double>(ctx, d_prop, h_half);
+}
+int bulk_c2r(adscf_ctx* ctx, const double* h_half, double* d_prop) {
+  return ctx->prec == ADSCF_SPLIT ? c2r_t<float>(ctx, h_half, d_prop) : c2r_t<double>(ctx, h_half, d_prop);
+}
+int bulk_mix_e(adscf_ctx* ctx) {
+  return ctx->prec == ADSCF_SPLIT ? mix_e_t<float>(ctx) : mix_e_t<double>(ctx);
+}

@@ -1,0 +1,429 @@
+// bulk_kernels.cuh -- pseudo-spectral diblock propagator on sm_103a.
+//
+// Reference: Propagate_Step (Bulk_3D_FFT/General_Routines/mod_propagate.f90:
+// 40-68), Real2Fourier/Fourier2Real (Bulk_3D_FFT/Geometry_Modules/Bulk/
+// mod_fourier.f90:75-105), Calculate_Laplace (:165-198) and the chain loops
+// and contour integral of Propagate_Diblock (Bulk_3D_FFT/Polymer_Modules/
+// mod_diblock.f90:116-154).
+//
+// Design.  The forward propagator q and the backward propagator q-dagger
+// are real, and the diffusion factor exp(-k^2 ds) is real and even in k, so
+// one complex 3D FFT of z = E_f q + i E_b q-dagger advances both chains by
+// one contour step: IFFT(G FFT(z)) = IFFT(G FFT(E_f q)) + i IFFT(G FFT(E_b
+// q-dagger)) exactly.  A "double step" t therefore produces contour node t of
+// both chains, stored as one complex slice (q_t, q-dagger_t).  The 3D FFT
+// is three line passes over an L2-resident spectrum buffer:
+//   X(t)  : inverse x-FFT -> q_t = E(t) * z -> store slice t ->
+//           z = E(t+1) * q_t -> forward x-FFT            (fused real space)
+//   Yf(t) : forward y-FFT
+//   Z(t)  : forward z-FFT -> * exp(-ds k^2)/N -> inverse z-FFT
+//   Yi(t) : inverse y-FFT
+// so the real-space Boltzmann factors, the slice store and the k-space
+// factor never take an extra pass over memory.
+#pragma once
+#include "fft.cuh"
+
+#define BULK_THREADS 256
+
+template <typename T>
+struct BulkDev {
+  int gx, gy, gz;
+  int npts;
+  int ns, na, nb;            // contour steps, A-block steps (fwd), B-block steps (bwd)
+  Plan1D px, py, pz;
+  // exp(-ds k^2) tables in `fk`: g_xy[gy*gx] (hi then lo), g_z[gz]/N (hi then
+  // lo); lo parts are the FP32 rounding residues (zero in FP64)
+  int gxy_off, gz_off;
+  int tw64_off, g64_off;     // FP64 twiddles / factors of the (0,0) z pencil
+  cplx<T>* spec;             // [npts] complex spectrum / work buffer
+  cplx<T>* slices;           // [(ns+1)][npts] (q_t, qdag_t)
+  T* E;                      // [2][npts] exp(-ds w/2), species A, B
+  T* Elo;                    // [2][npts] FP32 residue of E (null in FP64)
+  double* dist;              // [2][npts] contour integrals (block A, block B)
+  double* qpart;             // [gridDim] partial sums of q_N
+};
+
+// X-pass modes
+enum { XM_INIT = 0, XM_STEP = 1, XM_R2S = 2, XM_S2R = 3 };
+
+struct XAux {
+  const void* in;   // XM_R2S: real input [npts] (T)
+  void* out;        // XM_S2R: real output [npts] (T)
+  const void* e;    // XM_R2S / XM_S2R: real factor [npts] (T) or null
+};
+
+// z * (hi + lo) with one rounding: the FP32 residue of E keeps the Boltzmann
+// factor exact to ~1e-14 so its rounding cannot bias every step the same way
+__device__ __forceinline__ float emul(float z, float hi, float lo) { return fmaf(z, hi, z * lo); }
+__device__ __forceinline__ double emul(double z, double hi, double) { return z * hi; }
+
+template <typename T>
+__device__ __forceinline__ int chain_type_fwd(const BulkDev<T>& I, int t) { return t <= I.na ? 0 : 1; }
+template <typename T>
+__device__ __forceinline__ int chain_type_bwd(const BulkDev<T>& I, int t) { return t <= I.nb ? 1 : 0; }
+
+// shared-memory carve-up for one pass: twiddles (N) + two line buffers
+template <typename T>
+__device__ __forceinline__ void carve(unsigned char* raw, const Plan1D& P, cplx<T>*& tw,
+                                      cplx<T>*& b0, cplx<T>*& b1) {
+  tw = reinterpret_cast<cplx<T>*>(raw);
+  int twn = (P.n + 1) & ~1;
+  b0 = tw + twn;
+  b1 = b0 + P.lpc * P.ld;
+}
+
+template <typename T>
+__device__ __forceinline__ void load_twiddles(cplx<T>* tw, const cplx<T>* gtw, const Plan1D& P) {
+  for (int i = threadIdx.x; i < P.n; i += blockDim.x) tw[i] = gtw[P.tw_off + i];
+}
+
+// ---------------------------------------------------------------------------
+// X pass: lines along x (contiguous rows).  work.y = row tile.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(BULK_THREADS)
+k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
+             const cplx<T>* __restrict__ gtw, int t, int mode, XAux aux) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int2 w = work[blockIdx.x];
+  const BulkDev<T> I = insts[w.x];
+  if (mode == XM_STEP && t > I.ns) return;
+  const Plan1D P = I.px;
+  cplx<T> *tw, *b0, *b1;
+  carve<T>(smraw, P, tw, b0, b1);
+  load_twiddles<T>(tw, gtw, P);
+  const int N = P.n, LPC = P.lpc;
+  const int nrows = I.gy * I.gz;
+  const int row0 = w.y * LPC;
+  const int nl = min(LPC, nrows - row0);
+  const size_t base = (size_t)row0 * N;
+  const int tot = nl * N;
+  const int line = threadIdx.x / P.tpl, lt = threadIdx.x % P.tpl;
+  const bool active = line < nl;
+
+  const T* EA = I.E;
+  const T* EB = I.E + I.npts;
+  const T* LA = I.Elo ? I.Elo : I.E;             // residues (unused in FP64)
+  const T* LB = I.Elo ? I.Elo + I.npts : I.E + I.npts;
+  if (mode == XM_INIT) {
+    // slice 0 = (1, 1); z = (E_f(1), E_b(1)) -> forward
+    const bool fa = chain_type_fwd(I, 1) == 0, fb = chain_type_bwd(I, 1) == 0;
+    const T* ef = fa ? EA : EB;
+    const T* eb = fb ? EA : EB;
+    cplx<T>* s0 = I.slices;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const size_t g = base + e;
+      s0[g] = mk<T>((T)1, (T)1);
+      b0[(e / N) * P.ld + (e % N)] = mk<T>(ef[g], eb[g]);
+    }
+    __syncthreads();
+    cplx<T>* r = fft_lines<T>(b0, b1, tw, P, line, lt, active, +1);
+    for (int e = threadIdx.x; e < tot; e += blockDim.x)
+      I.spec[base + e] = r[(e / N) * P.ld + (e % N)];
+    return;
+  }
+  if (mode == XM_R2S) {
+    const T* in = static_cast<const T*>(aux.in);
+    const T* ee = static_cast<const T*>(aux.e);
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const size_t g = base + e;
+      T v = in[g];
+      if (ee) v *= ee[g];
+      b0[(e / N) * P.ld + (e % N)] = mk<T>(v, (T)0);
+    }
+    __syncthreads();
+    cplx<T>* r = fft_lines<T>(b0, b1, tw, P, line, lt, active, +1);
+    for (int e = threadIdx.x; e < tot; e += blockDim.x)
+      I.spec[base + e] = r[(e / N) * P.ld + (e % N)];
+    return;
+  }
+  // XM_STEP / XM_S2R: inverse x-FFT of the spectrum rows first
+  for (int e = threadIdx.x; e < tot; e += blockDim.x)
+    b0[(e / N) * P.ld + (e % N)] = I.spec[base + e];
+  __syncthreads();
+  cplx<T>* r = fft_lines<T>(b0, b1, tw, P, line, lt, active, -1);
+  cplx<T>* o = (r == b0) ? b1 : b0;
+  if (mode == XM_S2R) {
+    T* out = static_cast<T*>(aux.out);
+    const T* ee = static_cast<const T*>(aux.e);
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const size_t g = base + e;
+      T v = r[(e / N) * P.ld + (e % N)].x;
+      if (ee) v *= ee[g];
+      out[g] = v;
+    }
+    return;
+  }
+  // contour node t of both chains
+  const bool ta = chain_type_fwd(I, t) == 0, tb = chain_type_bwd(I, t) == 0;
+  const T* ef = ta ? EA : EB;
+  const T* eb = tb ? EA : EB;
+  const T* lf = ta ? LA : LB;
+  const T* lb = tb ? LA : LB;
+  const bool more = t < I.ns;
+  const bool ta2 = chain_type_fwd(I, t + 1) == 0, tb2 = chain_type_bwd(I, t + 1) == 0;
+  const T* ef2 = ta2 ? EA : EB;
+  const T* eb2 = tb2 ? EA : EB;
+  const T* lf2 = ta2 ? LA : LB;
+  const T* lb2 = tb2 ? LA : LB;
+  cplx<T>* sl = I.slices + (size_t)t * I.npts;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    const size_t g = base + e;
+    const int si = (e / N) * P.ld + (e % N);
+    const cplx<T> z = r[si];
+    const T fa = ef[g], fb = eb[g];
+    const T la = lf[g], lbv = lb[g];
+    const cplx<T> q = mk<T>(emul(z.x, fa, la), emul(z.y, fb, lbv));
+    sl[g] = q;
+    if (more) {
+      const T ga = (ef2 == ef) ? fa : ef2[g];
+      const T gb = (eb2 == eb) ? fb : eb2[g];
+      const T ha = (ef2 == ef) ? la : lf2[g];
+      const T hb = (eb2 == eb) ? lbv : lb2[g];
+      o[si] = mk<T>(emul(q.x, ga, ha), emul(q.y, gb, hb));
+    }
+  }
+  if (!more) return;
+  __syncthreads();
+  cplx<T>* r2 = fft_lines<T>(o, r, tw, P, line, lt, active, +1);
+  for (int e = threadIdx.x; e < tot; e += blockDim.x)
+    I.spec[base + e] = r2[(e / N) * P.ld + (e % N)];
+}
+
+// ---------------------------------------------------------------------------
+// Y / Z passes: lines along a strided axis.  Lines are flattened as
+// L = o*gx + x (o = z for Y passes, y for Z passes); a tile is LPC
+// consecutive lines, so consecutive threads read consecutive x.
+//   kind 0: forward y, 1: inverse y, 2: z (forward, exp(-ds k^2)/N, inverse),
+//   3: forward z only, 4: inverse z only
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(BULK_THREADS)
+k_bulk_strided(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
+               const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
+               const double2* __restrict__ gtw64, const double* __restrict__ g64,
+               int t, int kind) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int2 w = work[blockIdx.x];
+  const BulkDev<T> I = insts[w.x];
+  if (t > I.ns) return;
+  const bool zdir = kind >= 2;
+  const Plan1D P = zdir ? I.pz : I.py;
+  cplx<T> *tw, *b0, *b1;
+  carve<T>(smraw, P, tw, b0, b1);
+  load_twiddles<T>(tw, gtw, P);
+  const int N = P.n, LPC = P.lpc;
+  const int nlines = I.gx * (zdir ? I.gy : I.gz);
+  const int L0 = w.y * LPC;
+  const int nl = min(LPC, nlines - L0);
+  const size_t es = zdir ? (size_t)I.gx * I.gy : (size_t)I.gx;
+  const size_t ostride = zdir ? (size_t)I.gx : (size_t)I.gx * I.gy;
+  const int tot = nl * N;
+  const int line = threadIdx.x / P.tpl, lt = threadIdx.x % P.tpl;
+  const bool active = line < nl;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    const int j = e / nl, l = e % nl;
+    const int L = L0 + l;
+    const size_t b = (size_t)(L / I.gx) * ostride + (L % I.gx);
+    b0[l * P.ld + j] = I.spec[b + (size_t)j * es];
+  }
+  __syncthreads();
+  cplx<T>* r;
+  if (kind == 2) {
+    // The (kx, ky) = (0, 0) pencil carries the mean of the propagator; in FP32
+    // its rounding would be coherent over the whole box and accumulate over the
+    // contour, so it is transformed in FP64 (one line, negligible cost).
+    constexpr bool dc64 = sizeof(T) == 4;
+    double2* a64 = nullptr;
+    double2* b64 = nullptr;
+    double2* tw64 = nullptr;
+    Plan1D P64 = P;
+    if (dc64 && L0 == 0) {
+      unsigned char* tail = reinterpret_cast<unsigned char*>(b1 + P.lpc * P.ld);
+      tail = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tail) + 15) & ~uintptr_t(15));
+      tw64 = reinterpret_cast<double2*>(tail);
+      a64 = tw64 + ((N + 1) & ~1);
+      b64 = a64 + P.ld;
+      P64.tw_off = 0;
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        tw64[i] = gtw64[I.tw64_off + i];
+        a64[i] = make_double2((double)b0[i].x, (double)b0[i].y);
+      }
+      __syncthreads();
+    }
+    r = fft_lines<T>(b0, b1, tw, P, line, lt, active, +1);
+    // exp(-ds (kx^2 + ky^2 + kz^2)) / N from the separable tables, applied with
+    // one rounding (compensated product of the hi/lo parts)
+    const T* gxy = fk + I.gxy_off;
+    const T* gzt = fk + I.gz_off;
+    const int nxy = I.gx * I.gy;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const int l = e / N, j = e % N;
+      const int L = L0 + l;
+      cplx<T>& v = r[l * P.ld + j];
+      if constexpr (sizeof(T) == 4) {
+        const float ah = gxy[L], al = gxy[nxy + L], bh = gzt[j], bl = gzt[N + j];
+        const float gh = ah * bh;
+        const float gl = fmaf(ah, bh, -gh) + fmaf(ah, bl, al * bh);
+        v = mk<T>(fmaf(v.x, gh, v.x * gl), fmaf(v.y, gh, v.y * gl));
+      } else {
+        const T f = gxy[L] * gzt[j];
+        v = mk<T>(v.x * f, v.y * f);
+      }
+    }
+    __syncthreads();
+    cplx<T>* o = (r == b0) ? b1 : b0;
+    r = fft_lines<T>(r, o, tw, P, line, lt, active, -1);
+    if (dc64 && L0 == 0) {
+      const bool act = threadIdx.x < P64.tpl;
+      double2* rr = fft_lines<double>(a64, b64, tw64, P64, 0, threadIdx.x, act, +1);
+      for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const double f = g64[I.g64_off + j];
+        rr[j] = make_double2(rr[j].x * f, rr[j].y * f);
+      }
+      __syncthreads();
+      double2* oo = (rr == a64) ? b64 : a64;
+      rr = fft_lines<double>(rr, oo, tw64, P64, 0, threadIdx.x, act, -1);
+      for (int j = threadIdx.x; j < N; j += blockDim.x)
+        r[j] = mk<T>((T)rr[j].x, (T)rr[j].y);
+      __syncthreads();
+    }
+  } else {
+    const int sg = (kind == 0 || kind == 3) ? +1 : -1;
+    r = fft_lines<T>(b0, b1, tw, P, line, lt, active, sg);
+  }
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    const int j = e / nl, l = e % nl;
+    const int L = L0 + l;
+    const size_t b = (size_t)(L / I.gx) * ostride + (L % I.gx);
+    I.spec[b + (size_t)j * es] = r[l * P.ld + j];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Contour integral (mod_diblock.f90:143-154) and sum of q_N (:141).
+// Nodes s and N-s are read together: slice s = (q_s, qdag_s) and slice N-s
+// = (q_{N-s}, qdag_{N-s}) give the products q_s qdag_{N-s} (node s) and
+// q_{N-s} qdag_s (node N-s).  Trapezoid weights per block: 1/2 at the block
+// ends, 1 inside (times ds, applied at the end).
+//   FP32 slices: each product is split exactly (TwoProd via FMA) and summed
+//   with a compensated (Kahan/TwoSum) float pair, flushed every CHUNK pairs
+//   into FP64 accumulators.
+//   FP64 slices: plain FP64 accumulation, as the reference.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float wA_of(int s, int na) {
+  return (s == 0 ? 0.5f : 0.f) + (s == na ? 0.5f : 0.f) + ((s > 0 && s < na) ? 1.f : 0.f);
+}
+__device__ __forceinline__ float wB_of(int s, int na, int n) {
+  return (s == na ? 0.5f : 0.f) + (s == n ? 0.5f : 0.f) + ((s > na && s < n) ? 1.f : 0.f);
+}
+
+struct FF {  // compensated float accumulator
+  float hi, lo;
+};
+__device__ __forceinline__ void ff_add_prod(FF& a, float x, float y, float wgt) {
+  const float p = x * y;
+  const float e = fmaf(x, y, -p);          // exact: x*y = p + e
+  const float pw = p * wgt, ew = e * wgt;  // wgt in {1/2, 1}: exact
+  const float s = a.hi + pw;
+  const float bp = s - a.hi;
+  const float err = (a.hi - (s - bp)) + (pw - bp);
+  a.lo += err + ew;
+  a.hi = s;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BULK_THREADS)
+k_bulk_contour(const BulkDev<T>* __restrict__ insts, double ds) {
+  __shared__ double red[32];
+  const BulkDev<T> I = insts[blockIdx.y];
+  const int N = I.ns, NA = I.na;
+  const cplx<T>* sl = I.slices;
+  const size_t np = I.npts;
+  double qsum = 0.0;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < I.npts; p += gridDim.x * blockDim.x) {
+    double accA = 0.0, accB = 0.0;
+    if constexpr (sizeof(T) == 4) {
+      FF fa = {0.f, 0.f}, fb = {0.f, 0.f};
+      int cnt = 0;
+      for (int s = 0; 2 * s <= N; ++s) {
+        const int u = N - s;
+        const cplx<T> a = sl[(size_t)s * np + p];
+        const cplx<T> b = sl[(size_t)u * np + p];
+        if (s == 0) qsum += (double)b.x;
+        // node s: q_s * qdag_{N-s}
+        const float x1 = (float)a.x, y1 = (float)b.y;
+        float wa = wA_of(s, NA), wb = wB_of(s, NA, N);
+        if (wa != 0.f) ff_add_prod(fa, x1, y1, wa);
+        if (wb != 0.f) ff_add_prod(fb, x1, y1, wb);
+        if (u != s) {  // node N-s: q_{N-s} * qdag_s
+          const float x2 = (float)b.x, y2 = (float)a.y;
+          wa = wA_of(u, NA); wb = wB_of(u, NA, N);
+          if (wa != 0.f) ff_add_prod(fa, x2, y2, wa);
+          if (wb != 0.f) ff_add_prod(fb, x2, y2, wb);
+        }
+        if (++cnt == 16) {
+          accA += (double)fa.hi + (double)fa.lo; fa.hi = fa.lo = 0.f;
+          accB += (double)fb.hi + (double)fb.lo; fb.hi = fb.lo = 0.f;
+          cnt = 0;
+        }
+      }
+      accA += (double)fa.hi + (double)fa.lo;
+      accB += (double)fb.hi + (double)fb.lo;
+    } else {
+      for (int s = 0; 2 * s <= N; ++s) {
+        const int u = N - s;
+        const cplx<T> a = sl[(size_t)s * np + p];
+        const cplx<T> b = sl[(size_t)u * np + p];
+        if (s == 0) qsum += (double)b.x;
+        double pr = (double)a.x * (double)b.y;
+        accA += (double)wA_of(s, NA) * pr;
+        accB += (double)wB_of(s, NA, N) * pr;
+        if (u != s) {
+          pr = (double)b.x * (double)a.y;
+          accA += (double)wA_of(u, NA) * pr;
+          accB += (double)wB_of(u, NA, N) * pr;
+        }
+      }
+    }
+    I.dist[p] = ds * accA;
+    I.dist[np + p] = ds * accB;
+  }
+  const double tot = block_reduce_1(qsum, red);
+  if (threadIdx.x == 0) I.qpart[blockIdx.x] = tot;
+}
+
+// E = exp(-0.5 ds w) for both species (Calculate_Expfield, mod_propagate.f90:28)
+// (Elo: FP32 residue E - (float)E, or null)
+template <typename T>
+__global__ void k_expfield(const double* __restrict__ w, T* __restrict__ E, T* __restrict__ Elo,
+                           size_t n, double ds) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double e = exp(-0.5 * ds * w[i]);
+    const T h = (T)e;
+    E[i] = h;
+    if (Elo) Elo[i] = (T)(e - (double)h);
+  }
+}
+
+template <typename TO, typename TI>
+__global__ void k_convert(const TI* __restrict__ in, TO* __restrict__ out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (TO)in[i];
+}
+
+// spectrum (full complex, T) -> FP64 copy scaled by s
+template <typename T>
+__global__ void k_spec_to_f64(const cplx<T>* __restrict__ in, double2* __restrict__ out, size_t n, double s) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    cplx<T> v = in[i];
+    out[i] = make_double2((double)v.x * s, (double)v.y * s);
+  }
+}
+template <typename T>
+__global__ void k_f64_to_spec(const double2* __restrict__ in, cplx<T>* __restrict__ out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double2 v = in[i];
+    out[i] = mk<T>((T)v.x, (T)v.y);
+  }
+}

@@ -1,0 +1,272 @@
+// bulk_reg.cuh -- register-FFT passes of the bulk propagator (power-of-two axes).
+//
+// Same pipeline and arithmetic as bulk_kernels.cuh (X, Yf, Z, Yi passes per
+// double step), with every line transform held in registers (RegFFT): one
+// in-warp exchange per 1D transform, power-of-two index arithmetic, and
+// global loads/stores issued straight from the register distributions.
+#pragma once
+#include "bulk_kernels.cuh"
+#include "fft_reg.cuh"
+
+namespace regk {
+
+template <int N>
+struct Cfg;
+template <> struct Cfg<32> { static constexpr int R1 = 8, TPL = 4; };
+template <> struct Cfg<64> { static constexpr int R1 = 8, TPL = 8; };
+template <> struct Cfg<128> { static constexpr int R1 = 16, TPL = 8; };
+template <> struct Cfg<256> { static constexpr int R1 = 16, TPL = 16; };
+
+template <typename T, int N>
+struct Layout {
+  using F = RegFFT<T, Cfg<N>::R1, Cfg<N>::TPL>;
+  static constexpr int LPC = BULK_THREADS / F::TPL;
+  // shared memory: twiddles [N] | z factors hi,lo [2N] (T) | scratch [LPC*LS] | dc [N] double2
+  static constexpr size_t tw_bytes = N * sizeof(cplx<T>);
+  static constexpr size_t gz_bytes = 2 * N * sizeof(T);
+  static constexpr size_t sc_off = ((tw_bytes + gz_bytes + 15) / 16) * 16;
+  static constexpr size_t sc_bytes = (size_t)LPC * F::LS * sizeof(cplx<T>);
+  static constexpr size_t dc_off = ((sc_off + sc_bytes + 15) / 16) * 16;
+  static constexpr size_t bytes = dc_off + N * sizeof(double2);
+};
+
+__device__ __forceinline__ int ilog2(int v) { return __ffs(v) - 1; }
+
+}  // namespace regk
+
+// ---------------------------------------------------------------------------
+// X pass (rows along x).  Modes as k_bulk_xpass.
+// ---------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void __launch_bounds__(BULK_THREADS)
+k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
+     const cplx<T>* __restrict__ gtw, int t, int mode, XAux aux) {
+  using LY = regk::Layout<T, N>;
+  using F = typename LY::F;
+  constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smraw);
+  cplx<T>* scr = reinterpret_cast<cplx<T>*>(smraw + LY::sc_off);
+  const int2 w = work[blockIdx.x];
+  const BulkDev<T>& I = insts[w.x];
+  const int ns = I.ns;
+  if (mode == XM_STEP && t > ns) return;
+  const int npts = I.npts;
+  const int nrows = I.gy * I.gz;
+  const int tw_off = I.px.tw_off;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
+  __syncthreads();
+  const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
+  const int row0 = w.y * LPC + line;
+  const bool valid = row0 < nrows;
+  const int row = valid ? row0 : nrows - 1;
+  cplx<T>* sc = scr + line * F::LS;
+  const size_t base = (size_t)row * N;
+  cplx<T>* spec = I.spec;
+  const T* EA = I.E;
+  const T* EB = I.E + npts;
+  const T* LA = I.Elo ? I.Elo : I.E;
+  const T* LB = I.Elo ? I.Elo + npts : I.E + npts;
+  cplx<T> v[R1];
+
+  if (mode == XM_INIT || mode == XM_R2S) {
+    if (mode == XM_INIT) {
+      const T* ef = (1 <= I.na) ? EA : EB;
+      const T* eb = (1 <= I.nb) ? EB : EA;
+      cplx<T>* s0 = I.slices;
+#pragma unroll
+      for (int m = 0; m < R1; ++m) {
+        const size_t g = base + F::in_index(lt, m);
+        v[m] = mk<T>(ef[g], eb[g]);
+        if (valid) s0[g] = mk<T>((T)1, (T)1);
+      }
+    } else {
+      const T* in = static_cast<const T*>(aux.in);
+      const T* ee = static_cast<const T*>(aux.e);
+#pragma unroll
+      for (int m = 0; m < R1; ++m) {
+        const size_t g = base + F::in_index(lt, m);
+        T x = in[g];
+        if (ee) x *= ee[g];
+        v[m] = mk<T>(x, (T)0);
+      }
+    }
+    F::forward(v, sc, tw, lt);
+    if (valid) {
+#pragma unroll
+      for (int r = 0; r < R1; ++r) spec[base + F::out_index(lt, r)] = v[r];
+    }
+    return;
+  }
+  // XM_STEP / XM_S2R: inverse x of the spectrum row
+#pragma unroll
+  for (int r = 0; r < R1; ++r) v[r] = spec[base + F::out_index(lt, r)];
+  F::inverse(v, sc, tw, lt);
+  if (mode == XM_S2R) {
+    T* out = static_cast<T*>(aux.out);
+    const T* ee = static_cast<const T*>(aux.e);
+    if (valid) {
+#pragma unroll
+      for (int m = 0; m < R1; ++m) {
+        const size_t g = base + F::in_index(lt, m);
+        T x = v[m].x;
+        if (ee) x *= ee[g];
+        out[g] = x;
+      }
+    }
+    return;
+  }
+  const bool ta = t <= I.na, tb = t <= I.nb;
+  const T* ef = ta ? EA : EB;
+  const T* eb = tb ? EB : EA;
+  const T* lf = ta ? LA : LB;
+  const T* lb = tb ? LB : LA;
+  const bool more = t < ns;
+  const bool ta2 = (t + 1) <= I.na, tb2 = (t + 1) <= I.nb;
+  const T* ef2 = ta2 ? EA : EB;
+  const T* eb2 = tb2 ? EB : EA;
+  const T* lf2 = ta2 ? LA : LB;
+  const T* lb2 = tb2 ? LB : LA;
+  cplx<T>* sl = I.slices + (size_t)t * npts;
+#pragma unroll
+  for (int m = 0; m < R1; ++m) {
+    const size_t g = base + F::in_index(lt, m);
+    const T fa = ef[g], fb = eb[g], la = lf[g], lbv = lb[g];
+    const cplx<T> q = mk<T>(emul(v[m].x, fa, la), emul(v[m].y, fb, lbv));
+    if (valid) sl[g] = q;
+    if (more) {
+      const T ga = (ef2 == ef) ? fa : ef2[g];
+      const T gb = (eb2 == eb) ? fb : eb2[g];
+      const T ha = (ef2 == ef) ? la : lf2[g];
+      const T hb = (eb2 == eb) ? lbv : lb2[g];
+      v[m] = mk<T>(emul(q.x, ga, ha), emul(q.y, gb, hb));
+    }
+  }
+  if (!more) return;
+  F::forward(v, sc, tw, lt);
+  if (valid) {
+#pragma unroll
+    for (int r = 0; r < R1; ++r) spec[base + F::out_index(lt, r)] = v[r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Strided passes (Y: kind 0 fwd / 1 inv; Z: kind 2 fwd*G*inv, 3 fwd, 4 inv).
+// Flattened lines L = o*gx + x; LPC consecutive lines per CTA.
+// ---------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void __launch_bounds__(BULK_THREADS)
+k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
+     const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
+     const double2* __restrict__ gtw64, const double* __restrict__ g64, int t, int kind) {
+  using LY = regk::Layout<T, N>;
+  using F = typename LY::F;
+  constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smraw);
+  T* gzs = reinterpret_cast<T*>(smraw + LY::tw_bytes);
+  cplx<T>* scr = reinterpret_cast<cplx<T>*>(smraw + LY::sc_off);
+  double2* dcb = reinterpret_cast<double2*>(smraw + LY::dc_off);
+  const int2 w = work[blockIdx.x];
+  const BulkDev<T>& I = insts[w.x];
+  if (t > I.ns) return;
+  const bool zdir = kind >= 2;
+  const int gx = I.gx, gy = I.gy;
+  const int lgx = regk::ilog2(gx);
+  const int tw_off = zdir ? I.pz.tw_off : I.py.tw_off;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
+  if (kind == 2) {
+    const T* gzt = fk + I.gz_off;
+    for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) gzs[i] = gzt[i];
+  }
+  __syncthreads();
+  const int nlines = gx * (zdir ? gy : I.gz);
+  const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
+  const int L0 = w.y * LPC;
+  const int Lr = L0 + line;
+  const bool valid = Lr < nlines;
+  const int L = valid ? Lr : nlines - 1;
+  const size_t es = zdir ? (size_t)gx * gy : (size_t)gx;
+  const size_t ostride = zdir ? (size_t)gx : (size_t)gx * gy;
+  const size_t base = (size_t)(L >> lgx) * ostride + (L & (gx - 1));
+  cplx<T>* sc = scr + line * F::LS;
+  cplx<T>* spec = I.spec;
+  cplx<T> v[R1];
+  const bool in_dout = (kind == 1 || kind == 4);  // inverse-only passes start in D_out
+  if (in_dout) {
+#pragma unroll
+    for (int r = 0; r < R1; ++r) v[r] = spec[base + (size_t)F::out_index(lt, r) * es];
+    F::inverse(v, sc, tw, lt);
+#pragma unroll
+    for (int m = 0; m < R1; ++m)
+      if (valid) spec[base + (size_t)F::in_index(lt, m) * es] = v[m];
+    return;
+  }
+#pragma unroll
+  for (int m = 0; m < R1; ++m) v[m] = spec[base + (size_t)F::in_index(lt, m) * es];
+  constexpr bool dc64 = sizeof(T) == 4;
+  const bool dcline = dc64 && kind == 2 && L0 == 0;  // CTA holding the (0,0) pencil
+  if (dcline && line == 0) {
+#pragma unroll
+    for (int m = 0; m < R1; ++m)
+      dcb[F::in_index(lt, m)] = make_double2((double)v[m].x, (double)v[m].y);
+  }
+  F::forward(v, sc, tw, lt);
+  if (kind == 0 || kind == 3) {
+    if (valid) {
+#pragma unroll
+      for (int r = 0; r < R1; ++r) spec[base + (size_t)F::out_index(lt, r) * es] = v[r];
+    }
+    return;
+  }
+  // exp(-ds k^2)/N, one rounding (compensated hi/lo product in FP32)
+  {
+    const T* gxy = fk + I.gxy_off;
+    const int nxy = gx * gy;
+    const T ah = gxy[L];
+    const T al = gxy[nxy + L];
+#pragma unroll
+    for (int r = 0; r < R1; ++r) {
+      const int kz = F::out_index(lt, r);
+      if constexpr (sizeof(T) == 4) {
+        const float bh = gzs[kz], bl = gzs[N + kz];
+        const float gh = ah * bh;
+        const float gl = fmaf(ah, bh, -gh) + fmaf(ah, bl, al * bh);
+        v[r] = mk<T>(fmaf(v[r].x, gh, v[r].x * gl), fmaf(v[r].y, gh, v[r].y * gl));
+      } else {
+        const T f = ah * gzs[kz];
+        v[r] = mk<T>(v[r].x * f, v[r].y * f);
+      }
+    }
+  }
+  F::inverse(v, sc, tw, lt);
+  if (valid) {
+#pragma unroll
+    for (int m = 0; m < R1; ++m) spec[base + (size_t)F::in_index(lt, m) * es] = v[m];
+  }
+  if (!dcline) return;
+  // (kx, ky) = (0, 0) pencil again in FP64: it carries the mean of both
+  // propagators, whose FP32 rounding would be coherent over the whole box
+  __syncthreads();
+  if (threadIdx.x >= 32) return;
+  using F64 = RegFFT<double, F::R1, F::TPL>;
+  double2* sc64 = reinterpret_cast<double2*>(smraw + LY::sc_off) + line * F64::LS;
+  double2* tw64 = reinterpret_cast<double2*>(smraw + LY::sc_off) + (32 / TPL) * F64::LS;
+  for (int i = threadIdx.x; i < N; i += 32) tw64[i] = gtw64[I.tw64_off + i];
+  __syncwarp();
+  double2 u[R1];
+#pragma unroll
+  for (int m = 0; m < R1; ++m) u[m] = dcb[F::in_index(lt, m)];
+  F64::forward(u, sc64, tw64, lt);
+#pragma unroll
+  for (int r = 0; r < R1; ++r) {
+    const double f = g64[I.g64_off + F::out_index(lt, r)];
+    u[r] = make_double2(u[r].x * f, u[r].y * f);
+  }
+  F64::inverse(u, sc64, tw64, lt);
+  if (line == 0) {
+#pragma unroll
+    for (int m = 0; m < R1; ++m)
+      spec[(size_t)F::in_index(lt, m) * es] = mk<T>((T)u[m].x, (T)u[m].y);
+  }
+}

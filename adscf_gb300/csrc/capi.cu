@@ -1,0 +1,619 @@
+// capi.cu -- the C ABI (include/adscf.h): context, host copies, SCF driver.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "internal.h"
+
+int set_err(adscf_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+namespace {
+
+// nint: round half away from zero (Fortran NINT)
+int nint(double x) { return x >= 0 ? (int)std::floor(x + 0.5) : -(int)std::floor(-x + 0.5); }
+
+int grid_blocks(size_t n, int per, int cap) {
+  size_t b = (n + per - 1) / per;
+  if (b < 1) b = 1;
+  return (int)std::min<size_t>(b, (size_t)cap);
+}
+
+int ensure_pinned(adscf_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->pinned_bytes) return ADSCF_OK;
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  ctx->h_pinned = nullptr;
+  ctx->pinned_bytes = 0;
+  CK(cudaMallocHost(&ctx->h_pinned, bytes));
+  ctx->pinned_bytes = bytes;
+  return ADSCF_OK;
+}
+
+// host -> device through pinned staging (one cudaMemcpyAsync per copy)
+int h2d(adscf_ctx* ctx, double* d, const double* h, size_t n) {
+  int rc = ensure_pinned(ctx, n * sizeof(double));
+  if (rc) return rc;
+  std::memcpy(ctx->h_pinned, h, n * sizeof(double));
+  CK(cudaMemcpyAsync(d, ctx->h_pinned, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return ADSCF_OK;
+}
+int d2h(adscf_ctx* ctx, double* h, const double* d, size_t n) {
+  int rc = ensure_pinned(ctx, n * sizeof(double));
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(ctx->h_pinned, d, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(h, ctx->h_pinned, n * sizeof(double));
+  return ADSCF_OK;
+}
+
+size_t nvar(const adscf_ctx* c) { return (size_t)c->ntypes * c->npts; }
+double* hx_slot(adscf_ctx* c, int s) { return c->d_hx + (size_t)s * nvar(c); }
+double* hr_slot(adscf_ctx* c, int s) { return c->d_hr + (size_t)s * nvar(c); }
+
+int read_result(adscf_ctx* ctx, adscf_iter_result* out, adscf_chain_result* ch) {
+  double r[R_COUNT];
+  CK(cudaMemcpyAsync(r, ctx->d_res, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (out) {
+    out->accuracy = r[R_ACC];
+    out->free_energy = r[R_F];
+    out->Qsum = r[R_Q];
+    out->logQ = r[R_LOGQ];
+    out->mu = r[R_MU];
+    out->rho = r[R_RHO];
+    out->lambda = r[R_LAMBDA];
+    out->iter = (int)r[R_ITER];
+    out->status = (int)r[R_STATUS];
+  }
+  if (ch) {
+    ch->Qsum = r[R_Q];
+    ch->logQ = r[R_LOGQ];
+    ch->mu = r[R_MU];
+    ch->rho = r[R_RHO];
+    ch->energy = r[R_ENERGY];
+  }
+  if (r[R_STATUS] != 0.0) return set_err(ctx, ADSCF_E_NONFINITE, "non-finite or non-positive Q / accuracy");
+  return ADSCF_OK;
+}
+
+// propagate from the current device field/E into dist + qpart
+int enqueue_propagate(adscf_ctx* ctx, const double* d_w) {
+  if (ctx->geometry == ADSCF_BULK) return bulk_enqueue_propagate(ctx);
+  return film_enqueue_propagate(ctx, d_w);
+}
+
+// whole iteration: propagate(x_k) -> closure -> solve -> mix (x_{k+1}, E)
+int enqueue_iteration(adscf_ctx* ctx) {
+  int rc;
+  // films read the field from the current history slot: the closure kernel
+  // and the film sweep both locate it through the device counter
+  if ((rc = enqueue_propagate(ctx, nullptr))) return rc;
+  k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, CL_MEANFIELD | CL_MIXDOTS);
+  k_solve<<<1, 64, 0, ctx->stream>>>(ctx->S, 1, 1);
+  CK(cudaGetLastError());
+  if (ctx->geometry == ADSCF_BULK) return bulk_mix_e(ctx);
+  k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, nullptr, nullptr, 0.0);
+  CK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+int build_iteration_graph(adscf_ctx* ctx) {
+  if (ctx->g_iter) return ADSCF_OK;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_iteration(ctx);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_err(ctx, ADSCF_E_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&ctx->g_iter, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_err(ctx, ADSCF_E_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+  return ADSCF_OK;
+}
+
+int build_prop_graph(adscf_ctx* ctx) {
+  if (ctx->g_prop) return ADSCF_OK;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_propagate(ctx, ctx->d_tmp);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_err(ctx, ADSCF_E_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&ctx->g_prop, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_err(ctx, ADSCF_E_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+  return ADSCF_OK;
+}
+
+int validate(const adscf_params* p, std::string& why) {
+  if (!p) { why = "null params"; return ADSCF_E_ARG; }
+  if (p->geometry < ADSCF_BULK || p->geometry > ADSCF_BRUSH) { why = "geometry"; return ADSCF_E_ARG; }
+  if (p->gx < 1 || p->gy < 1 || p->gz < 1) { why = "grid"; return ADSCF_E_ARG; }
+  if ((long long)p->gx * p->gy * (p->gz + 1) > (1LL << 30)) { why = "grid too large"; return ADSCF_E_ARG; }
+  if (p->precision != ADSCF_FP64 && p->precision != ADSCF_SPLIT) { why = "precision"; return ADSCF_E_ARG; }
+  if (p->mixing_type < 1 || p->mixing_type > 3) { why = "mixing_type"; return ADSCF_E_ARG; }
+  if (p->mixing_type == 3 && (p->mixing_dim < 1 || p->mixing_dim > SCF_MAX_HIST)) {
+    why = "mixing_dim must be 1..16"; return ADSCF_E_ARG;
+  }
+  if (p->ensemble != 1 && p->ensemble != 2) { why = "ensemble"; return ADSCF_E_ARG; }
+  if (!(p->sizex > 0 && p->sizey > 0 && p->sizez > 0)) { why = "box size"; return ADSCF_E_ARG; }
+  if (p->geometry != ADSCF_BULK && !p->dz) { why = "films need dz"; return ADSCF_E_ARG; }
+  if (!p->dss && !(p->ds > 0)) { why = "ds"; return ADSCF_E_ARG; }
+  return ADSCF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int adscf_abi_version(void) { return ADSCF_ABI_VERSION; }
+
+const char* adscf_status_string(int s) {
+  switch (s) {
+    case ADSCF_OK: return "ok";
+    case ADSCF_E_ARG: return "invalid argument";
+    case ADSCF_E_CUDA: return "CUDA error";
+    case ADSCF_E_PIVOT: return "zero tridiagonal pivot";
+    case ADSCF_E_NONFINITE: return "non-finite result";
+    case ADSCF_E_TIMEOUT: return "device wait timed out";
+    case ADSCF_E_OOM: return "device out of memory";
+    case ADSCF_E_STATE: return "invalid state";
+    default: return "unknown status";
+  }
+}
+
+const char* adscf_last_error(const adscf_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+long long adscf_field_points(const adscf_ctx* ctx) { return ctx ? (long long)ctx->npts : -1; }
+
+int adscf_contour_info(const adscf_ctx* ctx, int* ns, int* n_a) {
+  if (!ctx) return ADSCF_E_ARG;
+  if (ns) *ns = ctx->ns;
+  if (n_a) *n_a = ctx->na;
+  return ADSCF_OK;
+}
+
+int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
+  if (!out) return ADSCF_E_ARG;
+  *out = nullptr;
+  std::string why;
+  int rc = validate(p, why);
+  if (rc) return rc;
+  adscf_ctx* ctx = new (std::nothrow) adscf_ctx();
+  if (!ctx) return ADSCF_E_OOM;
+  ctx->p = *p;
+  ctx->p.dss = nullptr; ctx->p.dz = nullptr; ctx->p.ext_potential = nullptr; ctx->p.graft = nullptr;
+  ctx->geometry = p->geometry;
+  ctx->prec = p->precision;
+  ctx->gx = p->gx; ctx->gy = p->gy; ctx->gz = p->gz;
+  ctx->nplanes = p->geometry == ADSCF_BULK ? p->gz : p->gz + 1;
+  ctx->npts = p->gx * p->gy * ctx->nplanes;
+  ctx->ntypes = p->geometry == ADSCF_BRUSH ? 1 : 2;
+  // contour discretisation (Initialize_Diblock, mod_diblock.f90:74-75)
+  if (p->dss) {
+    ctx->ns = p->ns;
+    ctx->na = p->geometry == ADSCF_BRUSH ? p->ns : p->n_a;
+  } else {
+    const int sa = nint(p->block_length[0] / p->ds);
+    const int sb = p->geometry == ADSCF_BRUSH ? 0 : nint(p->block_length[1] / p->ds);
+    ctx->ns = sa + sb;
+    ctx->na = sa;
+  }
+  ctx->nb = ctx->ns - ctx->na;
+  if (ctx->ns < 1 || ctx->na < 0 || ctx->nb < 0) { delete ctx; return ADSCF_E_ARG; }
+  ctx->volume = p->sizex * p->sizey * p->sizez;
+  ctx->dvol = ctx->volume / ((double)p->gx * p->gy * p->gz);
+
+  auto fail = [&](int code) { adscf_ctx_destroy(ctx); return code; };
+  if (cudaGetDevice(&ctx->dev) != cudaSuccess) { delete ctx; return ADSCF_E_CUDA; }
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return ADSCF_E_CUDA;
+  }
+  ctx->stream = ctx->own_stream;
+  const size_t nv = nvar(ctx);
+  ctx->hist_slots = p->mixing_type == 3 ? p->mixing_dim + 1 : 2;
+  if (cudaMalloc(&ctx->d_dist, nv * sizeof(double)) ||
+      cudaMalloc(&ctx->d_dens, nv * sizeof(double)) ||
+      cudaMalloc(&ctx->d_tmp, std::max<size_t>(2 * nv, 2 * (size_t)ctx->npts) * sizeof(double)) ||
+      cudaMalloc(&ctx->d_hx, ctx->hist_slots * nv * sizeof(double)) ||
+      cudaMalloc(&ctx->d_hr, ctx->hist_slots * nv * sizeof(double)) ||
+      cudaMalloc(&ctx->d_gram, SCF_MAX_SLOTS * SCF_MAX_SLOTS * sizeof(double)) ||
+      cudaMalloc(&ctx->d_coef, 2 * SCF_MAX_SLOTS * sizeof(double)) ||
+      cudaMalloc(&ctx->d_res, R_COUNT * sizeof(double)) ||
+      cudaMalloc(&ctx->d_iter, sizeof(int))) {
+    cudaGetLastError();
+    ctx->err = "device allocation failed";
+    return fail(ADSCF_E_OOM);
+  }
+  cudaMemsetAsync(ctx->d_dens, 0, nv * sizeof(double), ctx->stream);
+  cudaMemsetAsync(ctx->d_hx, 0, ctx->hist_slots * nv * sizeof(double), ctx->stream);
+  cudaMemsetAsync(ctx->d_hr, 0, ctx->hist_slots * nv * sizeof(double), ctx->stream);
+  cudaMemsetAsync(ctx->d_gram, 0, SCF_MAX_SLOTS * SCF_MAX_SLOTS * sizeof(double), ctx->stream);
+  cudaMemsetAsync(ctx->d_res, 0, R_COUNT * sizeof(double), ctx->stream);
+  const int one = 1;
+  cudaMemcpyAsync(ctx->d_iter, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+  ctx->closure_blocks = grid_blocks(ctx->npts, SCF_THREADS, 152 * 4);
+  ctx->mix_blocks = grid_blocks(nv, SCF_THREADS, 152 * 8);
+  if (cudaMalloc(&ctx->d_part, (size_t)std::max(ctx->closure_blocks, 152 * 4) * NPART * sizeof(double))) {
+    cudaGetLastError();
+    return fail(ADSCF_E_OOM);
+  }
+
+  if (ctx->geometry == ADSCF_BULK) {
+    rc = bulk_create(ctx);
+  } else {
+    // per-plane integration weights and wall potential (films / brush)
+    rc = film_create(ctx);
+  }
+  if (rc) return fail(rc);
+
+  ScfDev& S = ctx->S;
+  S.npts = ctx->npts;
+  S.ntypes = ctx->ntypes;
+  S.plane = ctx->gx * ctx->gy;
+  S.nplanes = ctx->nplanes;
+  S.wall_mask = ctx->geometry != ADSCF_BULK;
+  S.dvol = ctx->dvol;
+  S.wz = ctx->d_wz;
+  S.ext = ctx->d_ext;
+  S.kappa = p->kappa; S.chi = p->chi;
+  S.v0 = p->monomer_volume[0] != 0 ? p->monomer_volume[0] : 1.0;
+  S.v1 = p->monomer_volume[1] != 0 ? p->monomer_volume[1] : 1.0;
+  S.ww = p->ww;
+  S.homopolymer = ctx->geometry == ADSCF_BRUSH;
+  S.ensemble = p->ensemble;
+  S.rho = p->rho; S.mu = p->mu; S.volume = ctx->volume;
+  S.chain_len = p->ds * ctx->ns;
+  S.dist = ctx->d_dist;
+  S.dens = ctx->d_dens;
+  S.hx = ctx->d_hx; S.hr = ctx->d_hr;
+  S.slots = ctx->hist_slots;
+  S.mixing_type = p->mixing_type;
+  S.warm = p->warm_iters > p->mixing_dim ? p->warm_iters : p->mixing_dim;
+  S.lambda = p->lambda;
+  S.lam_warm = p->lam_warm > 0 ? p->lam_warm : 1.0e-3;
+  S.qpart = ctx->d_qpart;
+  S.nqpart = ctx->contour_blocks;
+  S.qscale = ctx->geometry == ADSCF_BULK ? ctx->dvol : 1.0;
+  S.part = ctx->d_part;
+  S.npart_blocks = ctx->closure_blocks;
+  S.gram = ctx->d_gram;
+  S.coef = ctx->d_coef;
+  S.iter = ctx->d_iter;
+  S.res = ctx->d_res;
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(ADSCF_E_CUDA);
+  *out = ctx;
+  return ADSCF_OK;
+}
+
+int adscf_ctx_destroy(adscf_ctx* ctx) {
+  if (!ctx) return ADSCF_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->g_iter) cudaGraphExecDestroy(ctx->g_iter);
+  if (ctx->g_prop) cudaGraphExecDestroy(ctx->g_prop);
+  if (ctx->geometry == ADSCF_BULK) bulk_destroy(ctx);
+  else film_destroy(ctx);
+  cudaFree(ctx->d_dist); cudaFree(ctx->d_dens); cudaFree(ctx->d_tmp);
+  cudaFree(ctx->d_hx); cudaFree(ctx->d_hr); cudaFree(ctx->d_gram);
+  cudaFree(ctx->d_coef); cudaFree(ctx->d_res); cudaFree(ctx->d_iter);
+  cudaFree(ctx->d_part); cudaFree(ctx->d_wz); cudaFree(ctx->d_ext);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return ADSCF_OK;
+}
+
+// ---- propagator ----------------------------------------------------------
+int adscf_propagate_diblock_dev(adscf_ctx* ctx, const double* d_field, double* d_density,
+                                adscf_chain_result* out) {
+  if (!ctx || !d_field || !d_density) return ADSCF_E_ARG;
+  if (ctx->geometry == ADSCF_BRUSH) return set_err(ctx, ADSCF_E_STATE, "brush context: use adscf_propagate_homopolymer");
+  int rc;
+  if (ctx->geometry == ADSCF_BULK) {
+    if ((rc = bulk_enqueue_expfield(ctx, d_field))) return rc;
+    if ((rc = bulk_enqueue_propagate(ctx))) return rc;
+  } else {
+    if ((rc = film_enqueue_propagate(ctx, d_field))) return rc;
+  }
+  ScfDev S2 = ctx->S;
+  S2.dens = d_density;
+  k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, 0);
+  k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
+  CK(cudaGetLastError());
+  return read_result(ctx, nullptr, out);
+}
+
+int adscf_propagate_diblock(adscf_ctx* ctx, const double* field, double* density,
+                            adscf_chain_result* out) {
+  if (!ctx || !field || !density) return ADSCF_E_ARG;
+  const size_t nv = nvar(ctx);
+  double* d_w = ctx->d_tmp;
+  double* d_out = ctx->d_tmp + nv;
+  int rc = h2d(ctx, d_w, field, nv);
+  if (rc) return rc;
+  rc = adscf_propagate_diblock_dev(ctx, d_w, d_out, out);
+  if (rc) return rc;
+  return d2h(ctx, density, d_out, nv);
+}
+
+int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* density,
+                                adscf_chain_result* out) {
+  if (!ctx || !field || !density) return ADSCF_E_ARG;
+  if (ctx->geometry != ADSCF_BRUSH) return set_err(ctx, ADSCF_E_STATE, "not a brush context");
+  const size_t nv = nvar(ctx);
+  double* d_w = ctx->d_tmp;
+  double* d_out = ctx->d_tmp + nv;
+  int rc = h2d(ctx, d_w, field, nv);
+  if (rc) return rc;
+  if ((rc = film_enqueue_propagate(ctx, d_w))) return rc;
+  ScfDev S2 = ctx->S;
+  S2.dens = d_out;
+  k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, 0);
+  k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
+  CK(cudaGetLastError());
+  if ((rc = read_result(ctx, nullptr, out))) return rc;
+  return d2h(ctx, density, d_out, nv);
+}
+
+int adscf_propagate_step(adscf_ctx* ctx, double* prop, const double* aux, double ds) {
+  if (!ctx || !prop || !aux) return ADSCF_E_ARG;
+  const size_t n = ctx->npts;
+  double* d_p = ctx->d_tmp;
+  double* d_a = ctx->d_tmp + n;
+  int rc;
+  if ((rc = h2d(ctx, d_p, prop, n))) return rc;
+  if ((rc = h2d(ctx, d_a, aux, n))) return rc;
+  if (ctx->geometry == ADSCF_BULK) rc = bulk_step_single(ctx, d_p, d_a);
+  else rc = film_step_single(ctx, d_p, d_a, ds > 0 ? ds : ctx->p.ds);
+  if (rc) return rc;
+  return d2h(ctx, prop, d_p, n);
+}
+
+int adscf_real2fourier(adscf_ctx* ctx, const double* prop, double* spectrum) {
+  if (!ctx || !prop || !spectrum) return ADSCF_E_ARG;
+  if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "bulk only");
+  // the spectrum staging uses d_tmp (2*npts doubles); stage the input in d_dist
+  int rc = h2d(ctx, ctx->d_dist, prop, ctx->npts);
+  if (rc) return rc;
+  return bulk_r2c(ctx, ctx->d_dist, spectrum);
+}
+
+int adscf_fourier2real(adscf_ctx* ctx, const double* spectrum, double* prop) {
+  if (!ctx || !prop || !spectrum) return ADSCF_E_ARG;
+  if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "bulk only");
+  int rc = bulk_c2r(ctx, spectrum, ctx->d_dist);
+  if (rc) return rc;
+  return d2h(ctx, prop, ctx->d_dist, ctx->npts);
+}
+
+// ---- interactions -------------------------------------------------------
+int adscf_mean_fields(adscf_ctx* ctx, const double* density, double* field) {
+  if (!ctx || !density || !field) return ADSCF_E_ARG;
+  const size_t nv = nvar(ctx);
+  int rc = h2d(ctx, ctx->d_tmp, density, nv);
+  if (rc) return rc;
+  k_meanfield_only<<<grid_blocks(ctx->npts, 256, 152 * 8), 256, 0, ctx->stream>>>(ctx->S, ctx->d_tmp, ctx->d_tmp + nv);
+  CK(cudaGetLastError());
+  return d2h(ctx, field, ctx->d_tmp + nv, nv);
+}
+
+int adscf_interaction_energy(adscf_ctx* ctx, const double* density, double* energy) {
+  if (!ctx || !density || !energy) return ADSCF_E_ARG;
+  // closure with dist := density and scale 1: use a zero field slot so only
+  // the interaction partials matter
+  const size_t nv = nvar(ctx);
+  int rc = h2d(ctx, ctx->d_tmp, density, nv);
+  if (rc) return rc;
+  ScfDev S2 = ctx->S;
+  S2.dist = ctx->d_tmp;
+  S2.dens = ctx->d_tmp + nv;
+  S2.ensemble = 2;
+  S2.mu = 0.0;  // scale = exp(0) = 1
+  S2.hx = ctx->d_tmp + nv;  // x_k irrelevant for the interaction sum
+  S2.hr = ctx->d_tmp + nv;
+  S2.slots = 1;
+  S2.mixing_type = 1;
+  // the closure reads *iter to locate slots; slot 0 of S2 is d_tmp+nv
+  k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, CL_MEANFIELD | CL_KEEP_OLD);
+  k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
+  CK(cudaGetLastError());
+  double r[R_COUNT];
+  CK(cudaMemcpyAsync(r, ctx->d_res, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *energy = r[R_EINT];
+  return ADSCF_OK;
+}
+
+int adscf_integrator(adscf_ctx* ctx, const double* integrand, double* integral) {
+  if (!ctx || !integrand || !integral) return ADSCF_E_ARG;
+  std::vector<double> wz(ctx->nplanes, ctx->dvol);
+  if (ctx->d_wz) CK(cudaMemcpy(wz.data(), ctx->d_wz, ctx->nplanes * sizeof(double), cudaMemcpyDeviceToHost));
+  const int plane = ctx->gx * ctx->gy;
+  double s = 0.0;
+  for (int z = 0; z < ctx->nplanes; ++z) {
+    double t = 0.0;
+    for (int i = 0; i < plane; ++i) t += integrand[(size_t)z * plane + i];
+    s += wz[z] * t;
+  }
+  *integral = s;
+  return ADSCF_OK;
+}
+
+// ---- mixing ---------------------------------------------------------------
+int adscf_mix_dev(adscf_ctx* ctx, double* d_field, const double* d_dfield, int iter) {
+  if (!ctx || !d_field || !d_dfield || iter < 1) return ADSCF_E_ARG;
+  const size_t nv = nvar(ctx);
+  const int cur = iter % ctx->hist_slots;
+  CK(cudaMemcpyAsync(hx_slot(ctx, cur), d_field, nv * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(hr_slot(ctx, cur), d_dfield, nv * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_iter, &iter, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  ScfDev S2 = ctx->S;
+  S2.wall_mask = 0;  // the caller packs what is mixed (Mix_Fields)
+  k_mixdots<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2);
+  k_solve<<<1, 64, 0, ctx->stream>>>(S2, 0, 1);
+  k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, nullptr, nullptr, 0.0);
+  CK(cudaGetLastError());
+  const int nxt = (iter + 1) % ctx->hist_slots;
+  CK(cudaMemcpyAsync(d_field, hx_slot(ctx, nxt), nv * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return ADSCF_OK;
+}
+
+int adscf_mix(adscf_ctx* ctx, double* field, const double* dfield, int iter) {
+  if (!ctx || !field || !dfield) return ADSCF_E_ARG;
+  const size_t nv = nvar(ctx);
+  int rc;
+  if ((rc = h2d(ctx, ctx->d_tmp, field, nv))) return rc;
+  if ((rc = h2d(ctx, ctx->d_tmp + nv, dfield, nv))) return rc;
+  if ((rc = adscf_mix_dev(ctx, ctx->d_tmp, ctx->d_tmp + nv, iter))) return rc;
+  return d2h(ctx, field, ctx->d_tmp, nv);
+}
+
+int adscf_mix_reset(adscf_ctx* ctx) {
+  if (!ctx) return ADSCF_E_ARG;
+  const size_t nv = nvar(ctx);
+  CK(cudaMemsetAsync(ctx->d_hx, 0, ctx->hist_slots * nv * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_hr, 0, ctx->hist_slots * nv * sizeof(double), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_gram, 0, SCF_MAX_SLOTS * SCF_MAX_SLOTS * sizeof(double), ctx->stream));
+  const int one = 1;
+  CK(cudaMemcpyAsync(ctx->d_iter, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return ADSCF_OK;
+}
+
+// ---- device SCF loop --------------------------------------------------------
+int adscf_set_field(adscf_ctx* ctx, const double* field) {
+  if (!ctx || !field) return ADSCF_E_ARG;
+  int rc = adscf_mix_reset(ctx);
+  if (rc) return rc;
+  double* x1 = hx_slot(ctx, 1 % ctx->hist_slots);
+  if ((rc = h2d(ctx, x1, field, nvar(ctx)))) return rc;
+  if (ctx->geometry == ADSCF_BULK) {
+    if ((rc = bulk_enqueue_expfield(ctx, x1))) return rc;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return ADSCF_OK;
+}
+
+int adscf_set_density(adscf_ctx* ctx, const double* density) {
+  if (!ctx || !density) return ADSCF_E_ARG;
+  return h2d(ctx, ctx->d_dens, density, nvar(ctx));
+}
+
+int adscf_get_field(adscf_ctx* ctx, double* field) {
+  if (!ctx || !field) return ADSCF_E_ARG;
+  int k = 1;
+  CK(cudaMemcpyAsync(&k, ctx->d_iter, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return d2h(ctx, field, hx_slot(ctx, k % ctx->hist_slots), nvar(ctx));
+}
+
+int adscf_get_density(adscf_ctx* ctx, double* density) {
+  if (!ctx || !density) return ADSCF_E_ARG;
+  return d2h(ctx, density, ctx->d_dens, nvar(ctx));
+}
+
+int adscf_scf_run(adscf_ctx* ctx, int n_iter, double tol, adscf_iter_result* out) {
+  if (!ctx || n_iter < 0) return ADSCF_E_ARG;
+  int rc = build_iteration_graph(ctx);
+  if (rc) return rc;
+  for (int i = 0; i < n_iter; ++i) {
+    CK(cudaGraphLaunch(ctx->g_iter, ctx->stream));
+    if (tol >= 0.0) {
+      adscf_iter_result r{};
+      if ((rc = read_result(ctx, &r, nullptr))) return rc;
+      if (out) *out = r;
+      if (!(r.accuracy > tol)) return ADSCF_OK;  // NaN-safe as the reference
+    }
+  }
+  adscf_iter_result r{};
+  rc = read_result(ctx, &r, nullptr);  // synchronises the stream
+  if (out) *out = r;
+  return rc;
+}
+
+int adscf_scf_iteration(adscf_ctx* ctx, double* field, double* density, adscf_iter_result* out) {
+  if (!ctx || !field || !density) return ADSCF_E_ARG;
+  int rc = build_iteration_graph(ctx);
+  if (rc) return rc;
+  int k = 1;
+  CK(cudaMemcpyAsync(&k, ctx->d_iter, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t nv = nvar(ctx);
+  double* xk = hx_slot(ctx, k % ctx->hist_slots);
+  if ((rc = ensure_pinned(ctx, 2 * nv * sizeof(double)))) return rc;
+  std::memcpy(ctx->h_pinned, field, nv * sizeof(double));
+  CK(cudaMemcpyAsync(xk, ctx->h_pinned, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->geometry == ADSCF_BULK && (rc = bulk_enqueue_expfield(ctx, xk))) return rc;
+  CK(cudaGraphLaunch(ctx->g_iter, ctx->stream));
+  double* xn = hx_slot(ctx, (k + 1) % ctx->hist_slots);
+  CK(cudaMemcpyAsync(ctx->h_pinned, xn, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->h_pinned + nv, ctx->d_dens, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  adscf_iter_result r{};
+  rc = read_result(ctx, &r, nullptr);  // synchronises the stream
+  std::memcpy(field, ctx->h_pinned, nv * sizeof(double));
+  std::memcpy(density, ctx->h_pinned + nv, nv * sizeof(double));
+  if (out) *out = r;
+  return rc;
+}
+
+int adscf_set_stream(adscf_ctx* ctx, void* stream) {
+  if (!ctx) return ADSCF_E_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return ADSCF_OK;
+}
+
+int adscf_stage_launches(const adscf_ctx* ctx, int stage) {
+  if (!ctx) return -1;
+  int prop, contour = 1, update = 3;
+  if (ctx->geometry == ADSCF_BULK) prop = 1 + 4 * ctx->ns;
+  else prop = ctx->film_launches;
+  if (ctx->geometry != ADSCF_BULK) contour = ctx->film_contour_launches;
+  switch (stage) {
+    case ADSCF_STAGE_ITERATION: return prop + contour + update;
+    case ADSCF_STAGE_PROPAGATE: return prop;
+    case ADSCF_STAGE_CONTOUR: return contour;
+    case ADSCF_STAGE_UPDATE: return update;
+    default: return -1;
+  }
+}
+
+int adscf_enqueue(adscf_ctx* ctx, int stage, int repeats) {
+  if (!ctx || repeats < 0) return ADSCF_E_ARG;
+  int rc;
+  if (stage == ADSCF_STAGE_ITERATION) {
+    if ((rc = build_iteration_graph(ctx))) return rc;
+    for (int i = 0; i < repeats; ++i) CK(cudaGraphLaunch(ctx->g_iter, ctx->stream));
+    return ADSCF_OK;
+  }
+  for (int i = 0; i < repeats; ++i) {
+    if (stage == ADSCF_STAGE_PROPAGATE) {
+      if (ctx->geometry == ADSCF_BULK) rc = bulk_enqueue_chains(ctx);
+      else rc = film_enqueue_chains(ctx, nullptr);
+    } else if (stage == ADSCF_STAGE_CONTOUR) {
+      if (ctx->geometry == ADSCF_BULK) rc = bulk_enqueue_contour(ctx);
+      else rc = film_enqueue_contour(ctx);
+    } else if (stage == ADSCF_STAGE_UPDATE) {
+      k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, CL_MEANFIELD | CL_MIXDOTS);
+      k_solve<<<1, 64, 0, ctx->stream>>>(ctx->S, 1, 1);
+      CK(cudaGetLastError());
+      rc = ctx->geometry == ADSCF_BULK ? bulk_mix_e(ctx)
+           : (k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, nullptr, nullptr, 0.0),
+              cudaGetLastError() == cudaSuccess ? ADSCF_OK : ADSCF_E_CUDA);
+    } else {
+      return set_err(ctx, ADSCF_E_ARG, "unknown stage");
+    }
+    if (rc) return rc;
+  }
+  return ADSCF_OK;
+}
+
+}  // extern "C"

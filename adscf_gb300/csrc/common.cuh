@@ -1,0 +1,54 @@
+// common.cuh -- device helpers shared by the SCF kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+template <typename T> struct Cplx;
+template <> struct Cplx<float> { using type = float2; };
+template <> struct Cplx<double> { using type = double2; };
+template <typename T> using cplx = typename Cplx<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T x, T y) {
+  cplx<T> r; r.x = x; r.y = y; return r;
+}
+template <typename T> __device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ cplx<T> csub(cplx<T> a, cplx<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename T> __device__ __forceinline__ cplx<T> cmulc(cplx<T> a, cplx<T> b) {
+  return mk<T>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename T> __device__ __forceinline__ cplx<T> cscale(cplx<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+// multiply by -i*sg  (sg = +1 forward, -1 inverse)
+template <typename T> __device__ __forceinline__ cplx<T> mul_mi(cplx<T> a, int sg) {
+  return sg > 0 ? mk<T>(a.y, -a.x) : mk<T>(-a.y, a.x);
+}
+
+// ---- deterministic block reductions -----------------------------------
+// Sum K doubles across a block of `blockDim.x` threads (multiple of 32).
+// Result valid in threads 0..K-1 (value for index = threadIdx.x).
+template <int K>
+__device__ __forceinline__ double block_reduce_k(double (&v)[K], double* sm /* >= K*32 */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sm[k * 32 + warp] = x;
+  }
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < K) {
+    for (int w = 0; w < nw; ++w) r += sm[threadIdx.x * 32 + w];
+  }
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_reduce_1(double v, double* sm) {
+  double a[1] = {v};
+  return block_reduce_k<1>(a, sm);
+}

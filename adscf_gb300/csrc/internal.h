@@ -1,0 +1,99 @@
+// internal.h -- host-side context of the SCF library (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "../../include/adscf.h"
+#include "bulk_kernels.cuh"
+#include "scf_kernels.cuh"
+
+struct FilmState;  // film / brush device state (film.cu)
+
+struct adscf_ctx {
+  adscf_params p{};
+  std::string err;
+  int geometry = 0;
+  int prec = 0;                 // ADSCF_FP64 / ADSCF_SPLIT
+  int gx = 0, gy = 0, gz = 0;   // bulk grid; films: gz intervals
+  int nplanes = 0;              // bulk gz, films gz+1
+  int npts = 0;                 // points per species
+  int ntypes = 2;
+  int ns = 0, na = 0, nb = 0;   // contour steps
+  double volume = 0, dvol = 0;
+  cudaStream_t stream = nullptr;      // stream all work goes to
+  cudaStream_t own_stream = nullptr;  // the context's own stream
+  int dev = 0;
+  int film_launches = 0, film_contour_launches = 0;
+
+  // ---- bulk propagator (one of the two precisions is populated)
+  void* d_inst = nullptr;       // BulkDev<T> on device
+  BulkDev<float> hb32{};
+  BulkDev<double> hb64{};
+  void* d_tw = nullptr;         // twiddles (cplx<T>)
+  void* d_fk = nullptr;         // diffusion factors (T)
+  void* d_tw64 = nullptr;       // FP64 twiddles of the (0,0) z pencil
+  double* d_g64 = nullptr;      // FP64 diffusion factors of that pencil
+  int2* d_work_x = nullptr; int n_work_x = 0;
+  int2* d_work_y = nullptr; int n_work_y = 0;
+  int2* d_work_z = nullptr; int n_work_z = 0;
+  size_t smem_x = 0, smem_y = 0, smem_z = 0;
+  int regx = 0, regy = 0, regz = 0;   // register-FFT line length per pass (0: generic)
+  int use_generic = 0;                // force the generic mixed-radix kernels
+  int contour_blocks = 0;
+
+  // ---- SCF state (FP64)
+  ScfDev S{};
+  double* d_dist = nullptr;     // [ntypes][npts]
+  double* d_dens = nullptr;
+  double* d_hx = nullptr;
+  double* d_hr = nullptr;
+  double* d_qpart = nullptr;
+  double* d_part = nullptr;
+  double* d_gram = nullptr;
+  double* d_coef = nullptr;
+  double* d_res = nullptr;
+  int* d_iter = nullptr;
+  double* d_wz = nullptr;
+  double* d_ext = nullptr;
+  double* d_tmp = nullptr;      // [ntypes][npts] FP64 staging
+  double* h_pinned = nullptr;   // pinned staging for host copies
+  size_t pinned_bytes = 0;
+  int closure_blocks = 0;
+  int mix_blocks = 0;
+  int hist_slots = 2;
+
+  // graph of one whole SCF iteration (bulk) and of one propagation
+  cudaGraphExec_t g_iter = nullptr;
+  cudaGraphExec_t g_prop = nullptr;
+
+  FilmState* film = nullptr;
+};
+
+// errors
+int set_err(adscf_ctx* c, int code, const std::string& msg);
+#define CK(call)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      return set_err(ctx, ADSCF_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// bulk (bulk.cu)
+int bulk_create(adscf_ctx* ctx);
+void bulk_destroy(adscf_ctx* ctx);
+int bulk_enqueue_propagate(adscf_ctx* ctx);     // from E to dist + qpart
+int bulk_enqueue_chains(adscf_ctx* ctx);        // both chains, all steps
+int bulk_enqueue_contour(adscf_ctx* ctx);       // contour integral + Q
+int bulk_enqueue_expfield(adscf_ctx* ctx, const double* d_w);
+int bulk_step_single(adscf_ctx* ctx, double* d_prop, const double* d_e);
+int bulk_r2c(adscf_ctx* ctx, const double* d_prop, double* h_half);
+int bulk_c2r(adscf_ctx* ctx, const double* h_half, double* d_prop);
+int bulk_mix_e(adscf_ctx* ctx);                 // k_mix with E update
+// films (film.cu)
+int film_create(adscf_ctx* ctx);
+void film_destroy(adscf_ctx* ctx);
+int film_enqueue_propagate(adscf_ctx* ctx, const double* d_w);
+int film_enqueue_chains(adscf_ctx* ctx, const double* d_w);
+int film_enqueue_contour(adscf_ctx* ctx);
+int film_step_single(adscf_ctx* ctx, double* d_prop, const double* d_w, double ds);

@@ -1,0 +1,204 @@
+"""Host-side mirror of the ADSCF module procedures over the C ABI.
+
+Each method keeps the reference routine's name and argument meaning, so a
+test reads like a call into the Fortran modules:
+
+* ``propagate_diblock``  -- Propagate_Diblock (Bulk_3D_FFT/Polymer_Modules/
+  mod_diblock.f90:100-173) with Calculate_Expfield (mod_propagate.f90:22-32)
+* ``propagate_step``     -- Propagate_Step (mod_propagate.f90:40-68; films
+  Film_CK_AD/Film_1D/Geometry_Modules/mod_realspace.f90:24-79)
+* ``real2fourier`` / ``fourier2real`` -- mod_fourier.f90:75-105
+* ``mean_fields`` / ``interaction_energy`` -- mod_FloryHuggins.f90:74-129
+* ``mix``                -- Mix_Fields (main_diblock.f90:315-372)
+* ``scf_run``            -- the Calculate_Saddle_Point loop
+  (main_diblock.f90:398-451), device resident.
+
+Errors raise ``AdscfError`` carrying the C status code (the reference stops
+the program instead).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _f64(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+class Context:
+    """One SCF context (geometry, grid, chain, interactions, mixing)."""
+
+    def __init__(self, geometry=L.BULK, grid=(32, 32, 32), size=(4.0, 4.0, 4.0),
+                 ds=0.01, block_length=(0.5, 0.5), ensemble=1, rho=1.0, mu=0.0,
+                 kappa=25.0, chi=20.0, monomer_volume=(1.0, 1.0),
+                 precision=L.FP64, mixing_type=L.MIX_LAMBDA, mixing_dim=2,
+                 lam=0.1, lam_warm=1.0e-3, warm_iters=0, dss=None, n_a=0,
+                 dz=None, int_scheme=1, int_span=0, ext_potential=None,
+                 ww=1.0, graft=None, lib=None):
+        self.lib = lib or L.load()
+        p = L.Params()
+        p.geometry = geometry
+        p.gx, p.gy, p.gz = grid
+        p.sizex, p.sizey, p.sizez = size
+        p.ds = ds
+        self._keep = []
+        if dss is not None:
+            dss = _f64(dss)
+            self._keep.append(dss)
+            p.dss = L.dptr(dss)
+            p.ns = dss.size - 1
+            p.n_a = n_a
+        p.block_length[0], p.block_length[1] = block_length
+        p.ensemble = ensemble
+        p.rho, p.mu = rho, mu
+        p.kappa, p.chi = kappa, chi
+        p.monomer_volume[0], p.monomer_volume[1] = monomer_volume
+        p.precision = precision
+        p.mixing_type = mixing_type
+        p.mixing_dim = mixing_dim
+        p.lam = lam
+        p.lam_warm = lam_warm
+        p.warm_iters = warm_iters
+        for name, arr in (("dz", dz), ("ext_potential", ext_potential), ("graft", graft)):
+            if arr is not None:
+                arr = _f64(arr)
+                self._keep.append(arr)
+                setattr(p, name, L.dptr(arr))
+        p.int_scheme = int_scheme
+        p.int_span = int_span
+        p.ww = ww
+        self.params = p
+        h = C.c_void_p()
+        rc = self.lib.adscf_ctx_create(C.byref(p), C.byref(h))
+        if rc != L.ADSCF_OK:
+            raise L.AdscfError(rc, self.lib.adscf_status_string(rc).decode())
+        self.h = h
+        self.npts = int(self.lib.adscf_field_points(h))
+        ns, na = C.c_int(), C.c_int()
+        self.lib.adscf_contour_info(h, C.byref(ns), C.byref(na))
+        self.ns, self.n_a = ns.value, na.value
+        self.ntypes = 1 if geometry == L.BRUSH else 2
+        self.geometry = geometry
+
+    # -- lifetime --------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.adscf_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        L.check(self.lib, self.h, rc)
+
+    # -- propagators -----------------------------------------------------
+    def propagate_diblock(self, field):
+        """field [2][npts] -> (density [2][npts], ChainResult)."""
+        w = _f64(field, 2 * self.npts)
+        out = np.empty(2 * self.npts)
+        res = L.ChainResult()
+        self._ck(self.lib.adscf_propagate_diblock(self.h, L.dptr(w), L.dptr(out), C.byref(res)))
+        return out.reshape(np.shape(field)), res
+
+    def propagate_homopolymer(self, field):
+        w = _f64(field, self.npts)
+        out = np.empty(self.npts)
+        res = L.ChainResult()
+        self._ck(self.lib.adscf_propagate_homopolymer(self.h, L.dptr(w), L.dptr(out), C.byref(res)))
+        return out.reshape(np.shape(field)), res
+
+    def propagate_step(self, prop, aux, ds=0.0):
+        """One step in place on a copy; aux = expfield (bulk) or field (films)."""
+        q = _f64(prop, self.npts).copy()
+        a = _f64(aux, self.npts)
+        self._ck(self.lib.adscf_propagate_step(self.h, L.dptr(q), L.dptr(a), ds))
+        return q.reshape(np.shape(prop))
+
+    def real2fourier(self, prop):
+        gx, gy, gz = self.params.gx, self.params.gy, self.params.gz
+        q = _f64(prop, self.npts)
+        out = np.empty((gz, gy, gx // 2 + 1, 2))
+        self._ck(self.lib.adscf_real2fourier(self.h, L.dptr(q), L.dptr(out)))
+        return out[..., 0] + 1j * out[..., 1]
+
+    def fourier2real(self, spec):
+        gx, gy, gz = self.params.gx, self.params.gy, self.params.gz
+        s = np.ascontiguousarray(np.stack([spec.real, spec.imag], axis=-1), dtype=np.float64)
+        out = np.empty((gz, gy, gx))
+        self._ck(self.lib.adscf_fourier2real(self.h, L.dptr(s), L.dptr(out)))
+        return out
+
+    def integrator(self, integrand):
+        f = _f64(integrand, self.npts)
+        out = C.c_double()
+        self._ck(self.lib.adscf_integrator(self.h, L.dptr(f), C.byref(out)))
+        return out.value
+
+    # -- interactions ----------------------------------------------------
+    def mean_fields(self, density):
+        d = _f64(density, self.ntypes * self.npts)
+        out = np.empty_like(d)
+        self._ck(self.lib.adscf_mean_fields(self.h, L.dptr(d), L.dptr(out)))
+        return out.reshape(np.shape(density))
+
+    def interaction_energy(self, density):
+        d = _f64(density, self.ntypes * self.npts)
+        out = C.c_double()
+        self._ck(self.lib.adscf_interaction_energy(self.h, L.dptr(d), C.byref(out)))
+        return out.value
+
+    # -- mixing -----------------------------------------------------------
+    def mix(self, field, dfield, it):
+        x = _f64(field).copy()
+        r = _f64(dfield, x.size)
+        self._ck(self.lib.adscf_mix(self.h, L.dptr(x), L.dptr(r), int(it)))
+        return x.reshape(np.shape(field))
+
+    def mix_reset(self):
+        self._ck(self.lib.adscf_mix_reset(self.h))
+
+    # -- device SCF loop ---------------------------------------------------
+    def set_field(self, field):
+        self._ck(self.lib.adscf_set_field(self.h, L.dptr(_f64(field, self.ntypes * self.npts))))
+
+    def set_density(self, density):
+        self._ck(self.lib.adscf_set_density(self.h, L.dptr(_f64(density, self.ntypes * self.npts))))
+
+    def get_field(self):
+        out = np.empty(self.ntypes * self.npts)
+        self._ck(self.lib.adscf_get_field(self.h, L.dptr(out)))
+        return out
+
+    def get_density(self):
+        out = np.empty(self.ntypes * self.npts)
+        self._ck(self.lib.adscf_get_density(self.h, L.dptr(out)))
+        return out
+
+    def scf_run(self, n_iter, tol=-1.0):
+        res = L.IterResult()
+        self._ck(self.lib.adscf_scf_run(self.h, int(n_iter), float(tol), C.byref(res)))
+        return res
+
+    def scf_iteration(self, field, density_out=None):
+        x = _f64(field).copy()
+        d = np.empty_like(x) if density_out is None else density_out
+        res = L.IterResult()
+        self._ck(self.lib.adscf_scf_iteration(self.h, L.dptr(x), L.dptr(d), C.byref(res)))
+        return x, d, res

@@ -1,0 +1,402 @@
+#!/usr/bin/env python
+"""SCF iterations/s of the bulk AB-diblock SCF loop on one GB300.
+
+Workload: 128^3 grid, Ns = 200 (ds = 0.005, N_A = 80, N_B = 120), f_A = 0.40,
+chi N = 20, kappa = 25, cubic box L = 3.8 R_g, canonical ensemble, Anderson
+mixing with history m = 10 (lambda = 0.1).  Fields: the single-harmonic sum
+of the 24 {211} plane waves with amplitude 0.5 plus seeded N(0, 0.05^2)
+noise (synthetic, numpy default_rng).  A step is one whole SCF iteration
+(both chains over all contour steps, contour integral, Q, mean fields,
+residual, Anderson solve and mix), replayed from a CUDA graph.  The working
+set (3.2 GB of FP32 propagator slices) is far larger than L2.
+
+``python bench.py [--gpus N --steps K --warmup W]`` prints one JSON line.
+``--impl reference`` times the CPU restatement of the reference instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = ("SCF iter/s @128^3,Ns=200: FP32/FP64-split vs FP64 GPU at "
+          "|ΔF|≤1e-7; %HBM peak")
+GRID = 128
+L = 3.8
+DS = 0.005
+F_A = 0.40
+CHI = 20.0
+KAPPA = 25.0
+M_HIST = 10
+LAM = 0.1
+SEED = 3
+
+
+def c3_fields(n=GRID, length=L, seed=SEED):
+    """w_A = 0.5 S + noise, w_B = -0.5 S + noise; S = mean over the 12 +-pairs
+    of {211} of cos(2 pi G.r / L); noise N(0, 0.05^2) per point and species."""
+    rng = np.random.default_rng(seed)
+    r = np.arange(n) * length / n
+    z, y, x = np.meshgrid(r, r, r, indexing="ij")
+    gs = set()
+    import itertools
+    for perm in set(itertools.permutations((2, 1, 1))):
+        for sg in itertools.product((1, -1), repeat=3):
+            g = tuple(p * s for p, s in zip(perm, sg))
+            if tuple(-c for c in g) not in gs:
+                gs.add(g)
+    assert len(gs) == 12
+    S = np.zeros((n, n, n))
+    for gx, gy, gz in sorted(gs):
+        S += np.cos(2 * np.pi * (gx * x + gy * y + gz * z) / length)
+    S /= 12.0
+    w = np.empty((2, n, n, n))
+    w[0] = 0.5 * S + rng.normal(0.0, 0.05, S.shape)
+    w[1] = -0.5 * S + rng.normal(0.0, 0.05, S.shape)
+    return w
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_ctx(A, prec, stream=None):
+    c = A.Context(A.BULK, grid=(GRID, GRID, GRID), size=(L, L, L), ds=DS,
+                  block_length=(F_A, 1.0 - F_A), ensemble=1, rho=1.0, kappa=KAPPA,
+                  chi=CHI, precision=prec, mixing_type=A.MIX_ANDERSON,
+                  mixing_dim=M_HIST, lam=LAM, lam_warm=LAM, warm_iters=M_HIST)
+    if stream is not None:
+        A._lib.check(c.lib, c.h, c.lib.adscf_set_stream(c.h, stream.cuda_stream))
+    return c
+
+
+def time_stage(torch, ctx, stream, stage, reps):
+    lib = ctx.lib
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ctx._ck(lib.adscf_enqueue(ctx.h, stage, reps))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+# --------------------------------------------------------------------------
+# CPU legs (oracle restatement of the reference, bounded samples)
+# --------------------------------------------------------------------------
+def cpu_sample(nsteps, workers):
+    """Time `nsteps` Propagate_Step calls, `nsteps` contour-slice products and
+    one closure + Anderson mix at 128^3 on the host; return seconds per whole
+    iteration (2 Ns steps, Ns+1 slices) extrapolated from the sample."""
+    from oracle import bulk as ob, interactions as oi, iterate as oit
+    grid = (GRID, GRID, GRID)
+    w = c3_fields()
+    e = ob.calculate_expfield(w, DS)
+    lap = ob.calculate_laplace(grid, (L, L, L), DS)
+    if workers and workers > 1:
+        import scipy.fft as sf
+        fwd = lambda a: sf.rfftn(a, workers=workers) / a.size
+        inv = lambda f, s: sf.irfftn(f, s=s, workers=workers) * float(np.prod(s))
+    else:
+        fwd = ob.real2fourier
+        inv = ob.fourier2real
+    q = np.ones(grid)
+    t0 = time.perf_counter()
+    for s in range(nsteps):
+        t = 0 if s % 2 == 0 else 1
+        q = e[t] * q
+        q = inv(lap * fwd(q), q.shape)
+        q = e[t] * q
+    t1 = time.perf_counter()
+    acc = np.zeros(grid)
+    for s in range(nsteps):
+        acc += DS * q * q
+    t2 = time.perf_counter()
+    dens = np.stack([acc, acc])
+    nf = oi.mean_fields(dens, KAPPA, CHI)
+    hist = np.zeros((M_HIST + 1, dens.size))
+    dh = np.zeros_like(hist)
+    hist[:] = w.reshape(1, -1)
+    dh[:] = (nf - w).reshape(1, -1) * (1 + 0.01 * np.arange(M_HIST + 1))[:, None]
+    oit.mixing_anderson(hist, dh, LAM, it=M_HIST + 1)
+    t3 = time.perf_counter()
+    ns = int(round(F_A / DS)) + int(round((1 - F_A) / DS))
+    per_step = (t1 - t0) / nsteps
+    per_slice = (t2 - t1) / nsteps
+    return 2 * ns * per_step + (ns + 1) * per_slice + (t3 - t2), t3 - t0
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    per_iter = []
+    for _ in range(args.warmup):
+        cpu_sample(4, cores)
+    wall = 0.0
+    for _ in range(args.steps):
+        t_iter, t_wall = cpu_sample(8, cores)
+        per_iter.append(t_iter)
+        wall += t_wall
+    v = 1.0 / statistics.mean(per_iter)
+    sample = (f"each step: 8 Propagate_Step (r2c/c2r via scipy.fft, {cores} workers) + 8 contour "
+              f"slice products + one closure/Anderson mix at 128^3, extrapolated to 400 steps and "
+              f"201 slices; FP64 restatement of the reference (gfortran absent)")
+    out = {
+        "metric": METRIC, "value": v, "unit": "iter/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "bulk diblock 128^3 Ns=200 f_A=0.40 chiN=20 L=3.8 Anderson m=10",
+                   "grid": [GRID, GRID, GRID], "ns": 200, "l2": "n/a (host)"},
+        "cpu_baseline": {"value": v, "unit": "iter/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def run_profile():
+    """One SCF iteration's stages at 128^3, ds = 0.05 (20 contour steps, 340 MB
+    of slices) on the split path: the kernels of the bench, few launches."""
+    import adscf_gb300 as A
+    from adscf_gb300 import _lib as L_
+    w = c3_fields()
+    c = A.Context(A.BULK, grid=(GRID, GRID, GRID), size=(L, L, L), ds=0.05,
+                  block_length=(F_A, 1.0 - F_A), kappa=KAPPA, chi=CHI, precision=A.SPLIT,
+                  mixing_type=A.MIX_ANDERSON, mixing_dim=M_HIST, lam=LAM, lam_warm=LAM,
+                  warm_iters=M_HIST)
+    c.set_field(w)
+    for st in (L_.STAGE_PROPAGATE, L_.STAGE_CONTOUR, L_.STAGE_UPDATE):
+        c._ck(c.lib.adscf_enqueue(c.h, st, 1))
+    c.get_field()
+    c.close()
+    print("profile run done")
+    return 0
+
+
+# --------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--profile", action="store_true",
+                    help="small run for ncu: one propagation, contour and update of the "
+                         "split path at 128^3 with 20 contour steps")
+    args = ap.parse_args()
+    if args.profile:
+        return run_profile()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import adscf_gb300 as A
+    from adscf_gb300 import _lib as L_
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    w = c3_fields()
+    nv = w.size
+    npts = GRID ** 3
+
+    # ---- parity at the same field: split vs FP64 (untimed) -------------
+    res = {}
+    for prec in (A.FP64, A.SPLIT):
+        with make_ctx(A, prec, stream) as c:
+            c.set_field(w)
+            x1, d1, r1 = c.scf_iteration(w.reshape(-1))
+            res[prec] = (r1, d1)
+    dF = abs(res[A.SPLIT][0].free_energy - res[A.FP64][0].free_energy)
+    dphi = float(np.max(np.abs(res[A.SPLIT][1] - res[A.FP64][1])))
+    dlogQ = abs(res[A.SPLIT][0].logQ - res[A.FP64][0].logQ)
+
+    # ---- FP64 GPU path timing ---------------------------------------------
+    with make_ctx(A, A.FP64, stream) as c64:
+        c64.set_field(w)
+        c64.scf_run(M_HIST + 1)                     # past the warm-up mixing
+        time_stage(torch, c64, stream, L_.STAGE_ITERATION, 1)
+        t64 = time_stage(torch, c64, stream, L_.STAGE_ITERATION, args.fp64_steps)
+    fp64_iter_s = 1000.0 / t64
+
+    # ---- split path: the timed region ------------------------------------
+    ctx = make_ctx(A, A.SPLIT, stream)
+    ctx.set_field(w)
+    ctx.scf_run(M_HIST + 1)                         # Anderson active from here
+    lib = ctx.lib
+    ctx._ck(lib.adscf_enqueue(ctx.h, L_.STAGE_ITERATION, args.warmup))
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    ctx._ck(lib.adscf_enqueue(ctx.h, L_.STAGE_ITERATION, args.steps))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    launches_per_step = lib.adscf_stage_launches(ctx.h, L_.STAGE_ITERATION)
+
+    # ---- stage breakdown (CUDA events on the launching stream) ------------
+    ns = ctx.ns
+    t_prop = time_stage(torch, ctx, stream, L_.STAGE_PROPAGATE, 3)
+    t_cont = time_stage(torch, ctx, stream, L_.STAGE_CONTOUR, 3)
+    t_upd = time_stage(torch, ctx, stream, L_.STAGE_UPDATE, 3)
+    t_dstep = t_prop / ns                            # one double step (q and q-dagger)
+    alg_dstep = 2 * 12 * npts                        # 12 N B per propagator step, two chains
+    hbm, peak_kind = peaks()
+    achieved = alg_dstep / (t_dstep * 1e-3) / 1e9
+    alg_contour = 8 * (ns + 1) * npts + 16 * npts   # read all FP32 slices, write FP64 phi
+
+    # ---- end to end through the C ABI with host buffers ---------------------
+    xh = w.reshape(-1).copy()
+    dh = np.empty(nv)
+    for _ in range(2):
+        xh, dh, _r = ctx.scf_iteration(xh, dh)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ke2e = max(3, args.steps // 2)
+    for _ in range(ke2e):
+        xh, dh, _r = ctx.scf_iteration(xh, dh)
+    e2e_s = (time.perf_counter() - t0) / ke2e
+    ctx.close()
+
+    value = world * 1000.0 / ms_step
+    out = {
+        "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32/f64-split", "data": "synthetic",
+        "config": {"workload": "bulk diblock 128^3 Ns=200 f_A=0.40 chiN=20 kappa=25 L=3.8 "
+                               "canonical, Anderson m=10, {211} fields + noise",
+                   "grid": [GRID, GRID, GRID], "ns": ns, "parallelism": f"replicas{world}",
+                   "l2": "working set 3.4 GB > L2 (no flush needed)"},
+        "fp64_gpu_iter_s": world * fp64_iter_s,
+        "split_over_fp64": fp64_iter_s and (1000.0 / ms_step) / fp64_iter_s,
+        "contour_steps_per_s": world * 2 * ns * 1000.0 / ms_step,
+        "parity": {"dF_per_chain": dF, "max_dphi": dphi, "dlogQ": dlogQ,
+                   "vs": "FP64 GPU path, same field, one iteration"},
+        "stages_ms": {"propagate": t_prop, "contour": t_cont, "update": t_upd,
+                      "double_step": t_dstep},
+        "roofline": {"bound": "hbm", "kernel": "propagator double step (Yf, Z, Yi, X passes)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_kind": peak_kind,
+                     "algorithmic_bytes": alg_dstep, "traffic": None,
+                     "contour_GBs": alg_contour / (t_cont * 1e-3) / 1e9},
+        "clocks": clk,
+        "gpu_launches": launches_per_step * args.steps,
+        "e2e": {"value": world / e2e_s, "unit": "iter/s", "h2d_bytes_per_step": nv * 8,
+                "d2h_bytes_per_step": 2 * nv * 8 + 13 * 8,
+                "api": "adscf_scf_iteration (host field in/out, host density out)"},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        t_iter, t_wall = cpu_sample(24, 1)
+        out["cpu_baseline"] = {
+            "value": 1.0 / t_iter, "unit": "iter/s", "cores": 1, "kind": "port",
+            "sample": f"24 Propagate_Step + 24 contour slice products + one closure/Anderson mix "
+                      f"at 128^3 (numpy FP64 oracle, {t_wall:.1f} s), extrapolated to 400 steps "
+                      f"and 201 slices"}
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

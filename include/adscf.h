@@ -1,0 +1,219 @@
+/*
+ * adscf.h -- C ABI of the GB300 (sm_103a) SCF inner-loop library.
+ *
+ * The library replaces the compute core of ADSCF's Fortran 90 module
+ * procedures.  Every entry point below names the reference routine it
+ * stands in for (file:line within the ADSCF tree).  The Fortran drivers
+ * keep their input decks, SCF loop and output; they bind these functions
+ * through iso_c_binding.
+ *
+ * Conventions
+ *  - Plain C: opaque handles, plain pointers and sizes, int status returns.
+ *    Nothing here prints, exits or throws.
+ *  - Field arrays are [species][z][y][x] FP64, the same linear order as the
+ *    reference's Fortran (x,y,z,species).  Films and brushes include both
+ *    wall planes, z = 0..gz.
+ *  - Host pointers are caller-owned; functions without the _dev suffix copy
+ *    host data in and out.  *_dev variants take device pointers.
+ *  - A context owns its device buffers and its CUDA stream.  One context per
+ *    host thread; a context is not safe for concurrent use.
+ */
+#ifndef ADSCF_H
+#define ADSCF_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ADSCF_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define ADSCF_API __attribute__((visibility("default")))
+#else
+#define ADSCF_API
+#endif
+
+/* status codes (the reference has none: it prints and stops) */
+enum {
+  ADSCF_OK = 0,
+  ADSCF_E_ARG = 1,        /* invalid argument / unsupported shape          */
+  ADSCF_E_CUDA = 2,       /* CUDA runtime error                            */
+  ADSCF_E_PIVOT = 3,      /* zero tridiagonal pivot ("TriDiag Error",
+                             Film_3D/.../mod_realspace.f90:194-207)         */
+  ADSCF_E_NONFINITE = 4,  /* non-finite Q, density or field                */
+  ADSCF_E_TIMEOUT = 5,    /* bounded device wait expired                   */
+  ADSCF_E_OOM = 6,        /* device allocation failed                      */
+  ADSCF_E_STATE = 7       /* call not valid for this context / state       */
+};
+
+enum { ADSCF_BULK = 0, ADSCF_FILM_1D = 1, ADSCF_FILM_3D = 2, ADSCF_BRUSH = 3 };
+/* precision policy: FP64 everywhere, or FP32 propagators/FFTs/line sweeps
+ * with FP64 Q, free energy, compensated density accumulation and mixing   */
+enum { ADSCF_FP64 = 0, ADSCF_SPLIT = 1 };
+/* mixing_type as in main_diblock.f90:44 */
+enum { ADSCF_MIX_SIMPLE = 1, ADSCF_MIX_LAMBDA = 2, ADSCF_MIX_ANDERSON = 3 };
+
+typedef struct adscf_params {
+  int geometry;             /* ADSCF_BULK, ADSCF_FILM_1D, ADSCF_FILM_3D, ADSCF_BRUSH */
+  int gx, gy, gz;           /* bulk: grid points; films/brush: gz intervals, planes 0..gz */
+  double sizex, sizey, sizez;
+  double ds;                /* uniform contour step (input_general)          */
+  const double *dss;        /* optional [ns+1] contour steps, dss[0] = 0
+                               (Brush mod_homopolymer.f90:98-115); NULL = ds */
+  int ns;                   /* contour steps when dss != NULL                */
+  int n_a;                  /* contour node of the A-B junction (dss != NULL) */
+  double block_length[2];   /* f_A, f_B; segments = nint(f/ds)
+                               (mod_diblock.f90:74)                           */
+  int ensemble;             /* 1 canonical, 2 grand canonical                */
+  double rho, mu;           /* C and mu_scf of input_general                 */
+  double kappa, chi;        /* input_interactions                            */
+  double monomer_volume[2];
+  int precision;            /* ADSCF_FP64 or ADSCF_SPLIT                      */
+  int mixing_type;          /* ADSCF_MIX_*                                    */
+  int mixing_dim;           /* Anderson history m (reference: 2)             */
+  double lambda;            /* lambda / lam_mix / lammax                     */
+  double lam_warm;          /* Anderson warm-up step (reference lam00 1e-3)  */
+  int warm_iters;           /* Anderson for iter > warm_iters (>= mixing_dim) */
+  const double *dz;         /* films/brush: [gz+1] mesh steps, dz[0] = 0     */
+  int int_scheme;           /* films/brush: 0 rectangle, 1 trapezoid         */
+  int int_span;             /* 0: Film_3D integrator (full), 1: Film_1D/Brush
+                               integrator (interior intervals only)          */
+  const double *ext_potential; /* films/brush: [types][gz+1] wall potential
+                               added inside Calculate_Mean_Ext_Fields; NULL=0 */
+  double ww;                /* brush: w = ww*phi + U (mod_virial_expansion) */
+  const double *graft;      /* brush: [gz+1] grafting distribution q-dag_0   */
+} adscf_params;
+
+typedef struct adscf_ctx adscf_ctx;
+
+/* chain quantities of Propagate_Diblock / Propagate_Homopolymer */
+typedef struct adscf_chain_result {
+  double Qsum;     /* single-chain partition function (dvol * sum q_N)   */
+  double logQ;
+  double mu;       /* chemical potential                                  */
+  double rho;      /* polymer concentration                               */
+  double energy;   /* chain energy term of the ensemble                   */
+} adscf_chain_result;
+
+/* one Calculate_Saddle_Point loop body (main_diblock.f90:410-429) */
+typedef struct adscf_iter_result {
+  double accuracy;      /* Check_Accuracy: sum (phi_old - phi_new)^2       */
+  double free_energy;   /* [chain - dvol sum(phi w) + interaction] / (rho V) */
+  double Qsum, logQ, mu, rho;
+  double lambda;        /* mixing step used                                */
+  int iter;             /* 1-based iteration index                         */
+  int status;
+} adscf_iter_result;
+
+/* ---- context ----------------------------------------------------------
+ * Initialize (Bulk_3D_FFT/General_Routines/sub_wrap.f90:8-40):
+ * Initialize_Fourier + Calculate_Laplace + Calculate_Volume_Parameters
+ * (mod_fourier.f90:49-54,152-198), Initialize_Diblock (mod_diblock.f90:46-88),
+ * Initialize_Interactions (mod_FloryHuggins.f90:37-66); films: generate_mesh
+ * (Film_3D/.../mod_realspace.f90:222-265) is done by the caller, who passes
+ * dz.  Finish (sub_wrap.f90:48-58) is adscf_ctx_destroy.                   */
+ADSCF_API int adscf_ctx_create(const adscf_params *params, adscf_ctx **ctx);
+ADSCF_API int adscf_ctx_destroy(adscf_ctx *ctx);
+ADSCF_API const char *adscf_status_string(int status);
+ADSCF_API const char *adscf_last_error(const adscf_ctx *ctx);
+ADSCF_API int adscf_abi_version(void);
+/* number of points of one species field ([z][y][x], walls included) */
+ADSCF_API long long adscf_field_points(const adscf_ctx *ctx);
+/* contour steps (segments) and A-block steps of the chain */
+ADSCF_API int adscf_contour_info(const adscf_ctx *ctx, int *ns, int *n_a);
+
+/* ---- propagator -------------------------------------------------------
+ * Calculate_Expfield (Bulk_3D_FFT/General_Routines/mod_propagate.f90:22-32)
+ * + Propagate_Diblock (Bulk_3D_FFT/Polymer_Modules/mod_diblock.f90:100-173;
+ * films Film_CK_AD/Film_1D/Polymer_Modules/mod_diblock.f90:110-195,
+ * Film_3D :105-182).  field [2][npts] in, density [2][npts] out (by
+ * monomer type, main_diblock.f90:277-283).                                 */
+ADSCF_API int adscf_propagate_diblock(adscf_ctx *ctx, const double *field,
+                            double *density, adscf_chain_result *out);
+ADSCF_API int adscf_propagate_diblock_dev(adscf_ctx *ctx, const double *d_field,
+                                double *d_density, adscf_chain_result *out);
+
+/* Propagate_Homopolymer (Brush_CK_AD/Polymer_Modules/mod_homopolymer.f90:
+ * 181-259): single-species field [npts], density [npts].                   */
+ADSCF_API int adscf_propagate_homopolymer(adscf_ctx *ctx, const double *field,
+                                double *density, adscf_chain_result *out);
+
+/* Propagate_Step: one contour step on one propagator in place.
+ *  bulk : prop <- E IFFT(exp(-k^2 ds) FFT(E prop)), E = expfield
+ *         (mod_propagate.f90:40-68; expfield from Calculate_Expfield);
+ *  films: Crank-Nicolson / Douglas ADI step with the given field and ds
+ *         (Film_1D/.../mod_realspace.f90:24-79, Film_3D :22-140,
+ *         Brush_CK_AD/Geometry_Modules/mod_realspace.f90:26-79);
+ *         `aux` is the field w, `ds` the step (<= 0: params ds).          */
+ADSCF_API int adscf_propagate_step(adscf_ctx *ctx, double *prop, const double *aux,
+                         double ds);
+
+/* Real2Fourier (scaled 1/N) and Fourier2Real (unnormalised), bulk only,
+ * mod_fourier.f90:75-105.  Spectrum is the r2c half spectrum
+ * [gz][gy][gx/2+1] of interleaved (re, im) doubles.                         */
+ADSCF_API int adscf_real2fourier(adscf_ctx *ctx, const double *prop, double *spectrum);
+ADSCF_API int adscf_fourier2real(adscf_ctx *ctx, const double *spectrum, double *prop);
+
+/* integrator (Film_3D/.../mod_realspace.f90:267-281, Brush
+ * mod_adaptive.f90:124-143); bulk: dvol * sum.                              */
+ADSCF_API int adscf_integrator(adscf_ctx *ctx, const double *integrand, double *integral);
+
+/* ---- interactions -----------------------------------------------------
+ * Calculate_Mean_Fields (mod_FloryHuggins.f90:104-129) / films
+ * Calculate_Mean_Ext_Fields (Film_1D/.../mod_FloryHuggins.f90:140-167) with
+ * params.ext_potential as the wall potential; brush w = ww phi + U
+ * (mod_virial_expansion.f90:111-137).                                       */
+ADSCF_API int adscf_mean_fields(adscf_ctx *ctx, const double *density, double *field);
+/* Interaction_Energy (mod_FloryHuggins.f90:74-96) */
+ADSCF_API int adscf_interaction_energy(adscf_ctx *ctx, const double *density,
+                             double *energy);
+
+/* ---- mixing -----------------------------------------------------------
+ * Mix_Fields (main_diblock.f90:315-372) with Mixing_Simple / Mixing_Lambda /
+ * Mixing_Anderson (mod_iterate.f90:27-150), history kept on the device
+ * across calls.  field: in x_k, out x_{k+1}; dfield: r_k.                   */
+ADSCF_API int adscf_mix(adscf_ctx *ctx, double *field, const double *dfield, int iter);
+ADSCF_API int adscf_mix_dev(adscf_ctx *ctx, double *d_field, const double *d_dfield,
+                  int iter);
+/* forget the mixing history (next call behaves as iter == 1) */
+ADSCF_API int adscf_mix_reset(adscf_ctx *ctx);
+
+/* ---- whole SCF iteration on the device --------------------------------
+ * Loop body of Calculate_Saddle_Point (main_diblock.f90:410-429): densities,
+ * Check_Accuracy, mean fields, Mix_Fields, all device resident.  The whole
+ * iteration is replayed from a CUDA graph.  adscf_set_field loads x_1 and
+ * resets the iteration counter and density history.                       */
+ADSCF_API int adscf_set_field(adscf_ctx *ctx, const double *field);
+ADSCF_API int adscf_set_density(adscf_ctx *ctx, const double *density);
+ADSCF_API int adscf_get_field(adscf_ctx *ctx, double *field);     /* current x_k   */
+ADSCF_API int adscf_get_density(adscf_ctx *ctx, double *density); /* newest phi    */
+/* n iterations; result describes the last one.  Stops early when
+ * accuracy <= tol (tol < 0: never).                                        */
+ADSCF_API int adscf_scf_run(adscf_ctx *ctx, int n_iter, double tol,
+                  adscf_iter_result *out);
+/* one iteration with host buffers: field in (x_k) -> field out (x_{k+1}),
+ * density out (phi[x_k]); the call a Fortran SCF loop makes per iteration */
+ADSCF_API int adscf_scf_iteration(adscf_ctx *ctx, double *field, double *density,
+                        adscf_iter_result *out);
+
+/* ---- streams and asynchronous stages ---------------------------------
+ * Run all further work of the context on the caller's CUDA stream
+ * (cudaStream_t passed as void*; NULL restores the context's own stream).
+ * No reference counterpart: the reference is synchronous CPU code.        */
+ADSCF_API int adscf_set_stream(adscf_ctx *ctx, void *cuda_stream);
+/* Enqueue `repeats` runs of one stage on the context stream without any
+ * host synchronisation, starting from the device-resident field:
+ *   ADSCF_STAGE_ITERATION  whole SCF iteration (graph replay)
+ *   ADSCF_STAGE_PROPAGATE  both chains, all contour steps (no contour sum)
+ *   ADSCF_STAGE_CONTOUR    contour integral of the densities and Q
+ *   ADSCF_STAGE_UPDATE     closure, mean fields, residual, mixing solve+mix */
+enum { ADSCF_STAGE_ITERATION = 0, ADSCF_STAGE_PROPAGATE = 1,
+       ADSCF_STAGE_CONTOUR = 2, ADSCF_STAGE_UPDATE = 3 };
+ADSCF_API int adscf_enqueue(adscf_ctx *ctx, int stage, int repeats);
+/* kernel launches one run of a stage makes (for launch accounting) */
+ADSCF_API int adscf_stage_launches(const adscf_ctx *ctx, int stage);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ADSCF_H */

@@ -1,0 +1,43 @@
+"""SCF loop restatement (FP64) -- test infrastructure.
+
+Calculate_Saddle_Point loop body, Bulk_3D_FFT/Main_Diblock_Melt/
+main_diblock.f90:410-429: densities of the current field, Check_Accuracy
+(:380-390), Calculate_Mean_Fields, dfield = newfield - field, Mix_Fields,
+density = newdensity.  The free energy per chain reported for iterate k is
+[chain energy - dvol sum(phi_new * w_k) + Interaction_Energy(phi_new)]/(rho V)
+(Calculate_Energy, main_diblock.f90:295-307, evaluated at the iterate).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import bulk, interactions, iterate
+
+
+def bulk_scf(field, n_iter, grid, size, ds, block_length, kappa, chi,
+             mixing_type=2, lam=0.1, m=2, lam00=1.0e-3, warm=None,
+             ensemble=1, rho=1.0, mu=0.0, density0=None, vol=(1.0, 1.0),
+             gram=False):
+    field = np.array(field, dtype=np.float64, copy=True)
+    density = np.zeros_like(field) if density0 is None else np.array(density0, dtype=np.float64)
+    mixer = iterate.Mixer(field.size, mixing_type, lam, m=m, lam00=lam00, warm=warm,
+                          gram=gram)
+    hist = []
+    for it in range(1, n_iter + 1):
+        r = bulk.propagate_diblock(field, grid, size, ds, block_length,
+                                   ensemble=ensemble, rho=rho, mu=mu)
+        newdensity = bulk.density_by_type(r["density"])
+        acc = interactions.check_accuracy(density, newdensity)
+        newfield = interactions.mean_fields(newdensity, kappa, chi, vol)
+        dvol = r["dvol"]
+        eint = interactions.interaction_energy(newdensity, kappa, chi, dvol, vol)
+        phiw = dvol * np.sum(newdensity * field)
+        volume = r["volume"]
+        rho_now = r["rho"]
+        F = (r["energy"] - phiw + eint) / (rho_now * volume)
+        hist.append(dict(iter=it, accuracy=acc, F=F, Qsum=r["Qsum"], mu=r["mu"],
+                         density=newdensity, field=field.copy()))
+        dfield = newfield - field
+        field = mixer(field, dfield, it)
+        density = newdensity
+    return field, hist
