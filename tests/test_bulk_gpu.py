@@ -145,9 +145,10 @@ def test_mixing_matches_oracle(mtype, m, warm, rng):
 
 @pytest.mark.parametrize("mtype,m,warm", [(MIX_LAMBDA, 2, None), (MIX_ANDERSON, 3, 5)])
 def test_scf_run_matches_oracle(mtype, m, warm, rng):
-    """Whole device SCF loop vs the oracle loop.  A lamellar start near the
-    saddle keeps the Anderson system well conditioned, so the comparison is
-    of arithmetic, not of chaotic amplification of rounding."""
+    """Whole device SCF loop vs the oracle loop.  The warm-up step is 0.05:
+    with the reference's 1e-3 the residuals entering the first Anderson step
+    are nearly equal, U is nearly singular and even the oracle's two algebraic
+    forms of the same system (direct and Gram) disagree at 1e-3 in F."""
     grid, size, ds = (12, 12, 12), (3.8, 3.8, 3.8), 0.02
     f = (0.4, 0.6)
     kappa, chi = 25.0, 15.0
@@ -159,11 +160,11 @@ def test_scf_run_matches_oracle(mtype, m, warm, rng):
     # oracle's Gram form is the tight reference, the reference's direct form
     # (ill-conditioned U amplifies rounding) the loose one
     xr, hist = oscf.bulk_scf(field, n, grid, size, ds, f, kappa, chi, mixing_type=mtype,
-                             lam=0.1, m=m, lam00=1e-3, warm=warm, gram=True)
+                             lam=0.1, m=m, lam00=0.05, warm=warm, gram=True)
     xd, hd = oscf.bulk_scf(field, n, grid, size, ds, f, kappa, chi, mixing_type=mtype,
-                           lam=0.1, m=m, lam00=1e-3, warm=warm, gram=False)
+                           lam=0.1, m=m, lam00=0.05, warm=warm, gram=False)
     with mkctx(grid, size, ds, FP64, f=f, kappa=kappa, chi=chi, mixing_type=mtype,
-               mixing_dim=m, lam=0.1, lam_warm=1e-3, warm_iters=warm or 0) as c:
+               mixing_dim=m, lam=0.1, lam_warm=0.05, warm_iters=warm or 0) as c:
         c.set_field(field)
         res = c.scf_run(n)
         xg = c.get_field()
@@ -173,7 +174,7 @@ def test_scf_run_matches_oracle(mtype, m, warm, rng):
     assert abs(res.accuracy - hist[-1]["accuracy"]) <= 1e-8 * hist[-1]["accuracy"] + 1e-20
     assert np.max(np.abs(dg - hist[-1]["density"].reshape(-1))) < 1e-9
     assert np.max(np.abs(xg - xr.reshape(-1))) < 1e-8 * (1 + np.max(np.abs(xr)))
-    assert abs(res.free_energy - hd[-1]["F"]) < 1e-5 * abs(hd[-1]["F"])
+    assert abs(res.free_energy - hd[-1]["F"]) < 1e-9 * abs(hd[-1]["F"])
 
 
 def test_scf_iteration_host_buffers(rng):
