@@ -20,6 +20,7 @@ ADSCF_E_NONFINITE = 4
 ADSCF_E_TIMEOUT = 5
 ADSCF_E_OOM = 6
 ADSCF_E_STATE = 7
+ADSCF_E_TOO_LARGE = 8
 
 BULK, FILM_1D, FILM_3D, BRUSH = 0, 1, 2, 3
 FP64, SPLIT = 0, 1
@@ -99,6 +100,9 @@ SIGNATURES = {
     "adscf_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "adscf_enqueue": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "adscf_stage_launches": (C.c_int, [C.c_void_p, C.c_int]),
+    "adscf_propagate_step_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                               C.c_double, C.c_double, C.c_void_p, C.c_void_p,
+                                               C.c_void_p]),
 }
 
 STAGE_ITERATION, STAGE_PROPAGATE, STAGE_CONTOUR, STAGE_UPDATE = 0, 1, 2, 3

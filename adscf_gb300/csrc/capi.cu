@@ -163,6 +163,7 @@ const char* adscf_status_string(int s) {
     case ADSCF_E_TIMEOUT: return "device wait timed out";
     case ADSCF_E_OOM: return "device out of memory";
     case ADSCF_E_STATE: return "invalid state";
+    case ADSCF_E_TOO_LARGE: return "problem larger than the fixed scratch of the allocation-free entry point";
     default: return "unknown status";
   }
 }

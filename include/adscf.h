@@ -43,7 +43,9 @@ enum {
   ADSCF_E_NONFINITE = 4,  /* non-finite Q, density or field                */
   ADSCF_E_TIMEOUT = 5,    /* bounded device wait expired                   */
   ADSCF_E_OOM = 6,        /* device allocation failed                      */
-  ADSCF_E_STATE = 7       /* call not valid for this context / state       */
+  ADSCF_E_STATE = 7,      /* call not valid for this context / state       */
+  ADSCF_E_TOO_LARGE = 8   /* problem exceeds the fixed scratch of the
+                             allocation-free entry point                  */
 };
 
 enum { ADSCF_BULK = 0, ADSCF_FILM_1D = 1, ADSCF_FILM_3D = 2, ADSCF_BRUSH = 3 };
@@ -212,6 +214,26 @@ enum { ADSCF_STAGE_ITERATION = 0, ADSCF_STAGE_PROPAGATE = 1,
 ADSCF_API int adscf_enqueue(adscf_ctx *ctx, int stage, int repeats);
 /* kernel launches one run of a stage makes (for launch accounting) */
 ADSCF_API int adscf_stage_launches(const adscf_ctx *ctx, int stage);
+
+/* ---- allocation-free propagator step ----------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (a pre-partitioned or quota-limited GPU, a driver that owns every
+ * device buffer, code paths where cudaMalloc's implicit synchronisation is
+ * not allowed): one FP64 bulk Propagate_Step, prop <- E IFFT(exp(-k^2 ds)
+ * FFT(E prop)) with E = expfield (mod_propagate.f90:40-68), on caller-owned
+ * device buffers d_prop [gz][gy][gx] (in/out) and d_expfield, enqueued on
+ * `stream` (cudaStream_t as void*).  It calls no allocator: plan, tables and
+ * spectrum live in one file-scope static device array of about 6.6 MB that
+ * every GPU loading the library holds until exit.  Limits: gx*gy*gz <=
+ * 262144, each axis <= 512 and a product of 2, 3 and 5, gx*gy <= 65536;
+ * larger problems return ADSCF_E_TOO_LARGE.  The first call on a device
+ * sets the array up (cudaGetSymbolAddress, kernel attributes): make it
+ * before any stream capture.  All calls share the array, so calls whose
+ * kernels overlap on the GPU race; order them on one stream.               */
+ADSCF_API int adscf_propagate_step_noalloc(int gx, int gy, int gz, double sizex,
+                                           double sizey, double sizez, double ds,
+                                           double *d_prop, const double *d_expfield,
+                                           void *stream);
 
 #ifdef __cplusplus
 }
