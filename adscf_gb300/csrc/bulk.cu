@@ -76,13 +76,16 @@ int reg_lpc(int n) {
 
 template <typename T>
 int set_reg_attrs(adscf_ctx* ctx) {
+#define ADSCF_ATTR1(NN, KK)                                                                   \
+  CK(cudaFuncSetAttribute(k_rs<T, NN, KK>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                          (int)regk::Layout<T, NN>::bytes));
 #define ADSCF_ATTR(NN)                                                                        \
   CK(cudaFuncSetAttribute(k_rx<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,          \
                           (int)regk::Layout<T, NN>::bytes));                                  \
-  CK(cudaFuncSetAttribute(k_rs<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize,          \
-                          (int)regk::Layout<T, NN>::bytes));
+  ADSCF_ATTR1(NN, 0) ADSCF_ATTR1(NN, 1) ADSCF_ATTR1(NN, 2) ADSCF_ATTR1(NN, 3) ADSCF_ATTR1(NN, 4)
   ADSCF_ATTR(32) ADSCF_ATTR(64) ADSCF_ATTR(128) ADSCF_ATTR(256)
 #undef ADSCF_ATTR
+#undef ADSCF_ATTR1
   return ADSCF_OK;
 }
 
@@ -116,13 +119,42 @@ void launch_s(adscf_ctx* ctx, int t, int kind) {
   const int2* work = z ? ctx->d_work_z : ctx->d_work_y;
   const dim3 g(z ? ctx->n_work_z : ctx->n_work_y), b(BULK_THREADS);
   const size_t sm = z ? ctx->smem_z : ctx->smem_y;
+#define ADSCF_KS(NN)                                                                          \
+  switch (kind) {                                                                             \
+    case 0: k_rs<T, NN, 0><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t); break;           \
+    case 1: k_rs<T, NN, 1><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t); break;           \
+    case 2: k_rs<T, NN, 2><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t); break;           \
+    case 3: k_rs<T, NN, 3><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t); break;           \
+    default: k_rs<T, NN, 4><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t); break;          \
+  }
   switch (n) {
-    case 32: k_rs<T, 32><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind); break;
-    case 64: k_rs<T, 64><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind); break;
-    case 128: k_rs<T, 128><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind); break;
-    case 256: k_rs<T, 256><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind); break;
+    case 32: ADSCF_KS(32) break;
+    case 64: ADSCF_KS(64) break;
+    case 128: ADSCF_KS(128) break;
+    case 256: ADSCF_KS(256) break;
     default: k_bulk_strided<T><<<g, b, sm, s>>>(d, work, tw, fk, tw64, g64, t, kind);
   }
+#undef ADSCF_KS
+}
+
+// persistent pipelined passes: grid = resident CTAs (occupancy x SMs)
+template <typename T, int NN>
+int setup_persistent(adscf_ctx* ctx) {
+  const int sm = (int)regk::Layout<T, NN>::bytes;
+  int nsm = 0, o0 = 0, o1 = 0, o2 = 0, ox = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
+  CK(cudaFuncSetAttribute(k_rs_p<T, NN, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  CK(cudaFuncSetAttribute(k_rs_p<T, NN, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  CK(cudaFuncSetAttribute(k_rs_p<T, NN, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  CK(cudaFuncSetAttribute(k_rx_p<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o0, k_rs_p<T, NN, 0>, BULK_THREADS, sm));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, k_rs_p<T, NN, 1>, BULK_THREADS, sm));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o2, k_rs_p<T, NN, 2>, BULK_THREADS, sm));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ox, k_rx_p<T, NN>, BULK_THREADS, sm));
+  ctx->pgrid_y = std::min(ctx->n_work_y, nsm * std::max(1, std::min(o0, o1)));
+  ctx->pgrid_z = std::min(ctx->n_work_z, nsm * std::max(1, o2));
+  ctx->pgrid_x = std::min(ctx->n_work_x, nsm * std::max(1, ox));
+  return ADSCF_OK;
 }
 
 template <typename T>
@@ -240,6 +272,16 @@ int create_t(adscf_ctx* ctx) {
   CK(cudaFuncSetAttribute(k_bulk_xpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
   CK(cudaFuncSetAttribute(k_bulk_strided<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
   if ((rc = set_reg_attrs<T>(ctx))) return rc;
+  // the persistent passes need one register length on all three axes
+  if (ctx->regx && ctx->regx == ctx->regy && ctx->regx == ctx->regz && !ctx->no_persistent) {
+    switch (ctx->regx) {
+      case 32: rc = setup_persistent<T, 32>(ctx); break;
+      case 64: rc = setup_persistent<T, 64>(ctx); break;
+      case 128: rc = setup_persistent<T, 128>(ctx); break;
+      case 256: rc = setup_persistent<T, 256>(ctx); break;
+    }
+    if (rc) return rc;
+  }
 
   CK(cudaMalloc(&ctx->d_inst, sizeof(BulkDev<T>)));
   CK(cudaMemcpy(ctx->d_inst, &I, sizeof(I), cudaMemcpyHostToDevice));
@@ -257,11 +299,31 @@ int chains_t(adscf_ctx* ctx) {
   cudaStream_t s = ctx->stream;
   XAux none{nullptr, nullptr, nullptr};
   launch_x<T>(ctx, 0, XM_INIT, none);
-  for (int t = 1; t <= ctx->ns; ++t) {
-    launch_s<T>(ctx, t, 0);
-    launch_s<T>(ctx, t, 2);
-    launch_s<T>(ctx, t, 1);
-    launch_x<T>(ctx, t, XM_STEP, none);
+  if (ctx->pgrid_x) {
+    const double2* tw64 = static_cast<const double2*>(ctx->d_tw64);
+    const double* g64 = ctx->d_g64;
+    const size_t sm = ctx->smem_x;
+#define ADSCF_PSTEP(NN)                                                                          \
+  for (int t = 1; t <= ctx->ns; ++t) {                                                           \
+    k_rs_p<T, NN, 0><<<ctx->pgrid_y, BULK_THREADS, sm, s>>>(d, ctx->n_work_y, tw, fk, tw64, g64, t); \
+    k_rs_p<T, NN, 2><<<ctx->pgrid_z, BULK_THREADS, sm, s>>>(d, ctx->n_work_z, tw, fk, tw64, g64, t); \
+    k_rs_p<T, NN, 1><<<ctx->pgrid_y, BULK_THREADS, sm, s>>>(d, ctx->n_work_y, tw, fk, tw64, g64, t); \
+    k_rx_p<T, NN><<<ctx->pgrid_x, BULK_THREADS, sm, s>>>(d, ctx->n_work_x, tw, t);              \
+  }
+    switch (ctx->regx) {
+      case 32: ADSCF_PSTEP(32) break;
+      case 64: ADSCF_PSTEP(64) break;
+      case 128: ADSCF_PSTEP(128) break;
+      case 256: ADSCF_PSTEP(256) break;
+    }
+#undef ADSCF_PSTEP
+  } else {
+    for (int t = 1; t <= ctx->ns; ++t) {
+      launch_s<T>(ctx, t, 0);
+      launch_s<T>(ctx, t, 2);
+      launch_s<T>(ctx, t, 1);
+      launch_x<T>(ctx, t, XM_STEP, none);
+    }
   }
   CK(cudaGetLastError());
   return ADSCF_OK;

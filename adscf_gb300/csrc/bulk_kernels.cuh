@@ -399,7 +399,7 @@ template <typename T>
 __global__ void k_expfield(const double* __restrict__ w, T* __restrict__ E, T* __restrict__ Elo,
                            size_t n, double ds) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double e = exp(-0.5 * ds * w[i]);
+    const double e = exp_boltzmann(-0.5 * ds * w[i]);
     const T h = (T)e;
     E[i] = h;
     if (Elo) Elo[i] = (T)(e - (double)h);

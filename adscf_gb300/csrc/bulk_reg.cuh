@@ -151,14 +151,14 @@ k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
 }
 
 // ---------------------------------------------------------------------------
-// Strided passes (Y: kind 0 fwd / 1 inv; Z: kind 2 fwd*G*inv, 3 fwd, 4 inv).
+// Strided passes (Y: KIND 0 fwd / 1 inv; Z: KIND 2 fwd*G*inv, 3 fwd, 4 inv).
 // Flattened lines L = o*gx + x; LPC consecutive lines per CTA.
 // ---------------------------------------------------------------------------
-template <typename T, int N>
-__global__ void __launch_bounds__(BULK_THREADS)
+template <typename T, int N, int KIND>
+__global__ void __launch_bounds__(BULK_THREADS, KIND == 2 ? 2 : 3)
 k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
      const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
-     const double2* __restrict__ gtw64, const double* __restrict__ g64, int t, int kind) {
+     const double2* __restrict__ gtw64, const double* __restrict__ g64, int t) {
   using LY = regk::Layout<T, N>;
   using F = typename LY::F;
   constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
@@ -170,12 +170,12 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
   const int2 w = work[blockIdx.x];
   const BulkDev<T>& I = insts[w.x];
   if (t > I.ns) return;
-  const bool zdir = kind >= 2;
+  constexpr bool zdir = KIND >= 2;
   const int gx = I.gx, gy = I.gy;
   const int lgx = regk::ilog2(gx);
   const int tw_off = zdir ? I.pz.tw_off : I.py.tw_off;
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
-  if (kind == 2) {
+  if constexpr (KIND == 2) {
     const T* gzt = fk + I.gz_off;
     for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) gzs[i] = gzt[i];
   }
@@ -192,8 +192,8 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
   cplx<T>* sc = scr + line * F::LS;
   cplx<T>* spec = I.spec;
   cplx<T> v[R1];
-  const bool in_dout = (kind == 1 || kind == 4);  // inverse-only passes start in D_out
-  if (in_dout) {
+  constexpr bool in_dout = (KIND == 1 || KIND == 4);  // inverse-only passes start in D_out
+  if constexpr (in_dout) {
 #pragma unroll
     for (int r = 0; r < R1; ++r) v[r] = spec[base + (size_t)F::out_index(lt, r) * es];
     F::inverse(v, sc, tw, lt);
@@ -204,15 +204,15 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
   }
 #pragma unroll
   for (int m = 0; m < R1; ++m) v[m] = spec[base + (size_t)F::in_index(lt, m) * es];
-  constexpr bool dc64 = sizeof(T) == 4;
-  const bool dcline = dc64 && kind == 2 && L0 == 0;  // CTA holding the (0,0) pencil
+  constexpr bool dc64 = sizeof(T) == 4 && KIND == 2;
+  const bool dcline = dc64 && L0 == 0;  // CTA holding the (0,0) pencil
   if (dcline && line == 0) {
 #pragma unroll
     for (int m = 0; m < R1; ++m)
       dcb[F::in_index(lt, m)] = make_double2((double)v[m].x, (double)v[m].y);
   }
   F::forward(v, sc, tw, lt);
-  if (kind == 0 || kind == 3) {
+  if constexpr (KIND == 0 || KIND == 3) {
     if (valid) {
 #pragma unroll
       for (int r = 0; r < R1; ++r) spec[base + (size_t)F::out_index(lt, r) * es] = v[r];
@@ -220,7 +220,7 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
     return;
   }
   // exp(-ds k^2)/N, one rounding (compensated hi/lo product in FP32)
-  {
+  if constexpr (KIND == 2) {
     const T* gxy = fk + I.gxy_off;
     const int nxy = gx * gy;
     const T ah = gxy[L];
@@ -244,6 +244,7 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
 #pragma unroll
     for (int m = 0; m < R1; ++m) spec[base + (size_t)F::in_index(lt, m) * es] = v[m];
   }
+  if constexpr (!dc64) return;
   if (!dcline) return;
   // (kx, ky) = (0, 0) pencil again in FP64: it carries the mean of both
   // propagators, whose FP32 rounding would be coherent over the whole box
@@ -268,5 +269,217 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
 #pragma unroll
     for (int m = 0; m < R1; ++m)
       spec[(size_t)F::in_index(lt, m) * es] = mk<T>((T)u[m].x, (T)u[m].y);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent, software-pipelined variants (one instance, power-of-two axes):
+// each CTA walks tiles blockIdx.x, blockIdx.x + gridDim.x, ... and loads the
+// next tile's registers before transforming the current one, so the memory
+// latency of tile i+1 overlaps the FFT of tile i.
+// ---------------------------------------------------------------------------
+template <typename T, int N, int KIND>
+__global__ void __launch_bounds__(BULK_THREADS, 2)
+k_rs_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restrict__ gtw,
+       const T* __restrict__ fk, const double2* __restrict__ gtw64,
+       const double* __restrict__ g64, int t) {
+  using LY = regk::Layout<T, N>;
+  using F = typename LY::F;
+  constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
+  constexpr bool zdir = KIND >= 2;
+  constexpr bool in_dout = (KIND == 1);
+  constexpr bool out_dout = (KIND == 0);
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smraw);
+  T* gzs = reinterpret_cast<T*>(smraw + LY::tw_bytes);
+  cplx<T>* scr = reinterpret_cast<cplx<T>*>(smraw + LY::sc_off);
+  double2* dcb = reinterpret_cast<double2*>(smraw + LY::dc_off);
+  const BulkDev<T>& I = insts[0];
+  if (t > I.ns) return;
+  const int gx = I.gx, gy = I.gy;
+  const int lgx = regk::ilog2(gx);
+  const int tw_off = zdir ? I.pz.tw_off : I.py.tw_off;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
+  if constexpr (KIND == 2) {
+    const T* gzt = fk + I.gz_off;
+    for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) gzs[i] = gzt[i];
+  }
+  __syncthreads();
+  const int nlines = gx * (zdir ? gy : I.gz);
+  const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
+  const size_t es = zdir ? (size_t)gx * gy : (size_t)gx;
+  const size_t ostride = zdir ? (size_t)gx : (size_t)gx * gy;
+  cplx<T>* sc = scr + line * F::LS;
+  cplx<T>* spec = I.spec;
+  const T* gxy = fk + I.gxy_off;
+  auto line_of = [&](int tile) { return min(tile * LPC + line, nlines - 1); };
+  auto base_of = [&](int L) { return (size_t)(L >> lgx) * ostride + (L & (gx - 1)); };
+  cplx<T> nx[R1];
+  int tile = blockIdx.x;
+  if (tile < ntiles) {
+    const size_t b = base_of(line_of(tile));
+#pragma unroll
+    for (int r = 0; r < R1; ++r)
+      nx[r] = spec[b + (size_t)(in_dout ? F::out_index(lt, r) : F::in_index(lt, r)) * es];
+  }
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int Lr = tile * LPC + line;
+    const bool valid = Lr < nlines;
+    const int L = valid ? Lr : nlines - 1;
+    const size_t base = base_of(L);
+    cplx<T> v[R1];
+#pragma unroll
+    for (int r = 0; r < R1; ++r) v[r] = nx[r];
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) {
+      const size_t b = base_of(line_of(nxt));
+#pragma unroll
+      for (int r = 0; r < R1; ++r)
+        nx[r] = spec[b + (size_t)(in_dout ? F::out_index(lt, r) : F::in_index(lt, r)) * es];
+    }
+    constexpr bool dc64 = sizeof(T) == 4 && KIND == 2;
+    const bool dcblk = dc64 && tile == 0;
+    if (dcblk && line == 0) {
+#pragma unroll
+      for (int m = 0; m < R1; ++m) dcb[F::in_index(lt, m)] = make_double2((double)v[m].x, (double)v[m].y);
+    }
+    if constexpr (KIND == 1) {
+      F::inverse(v, sc, tw, lt);
+    } else if constexpr (KIND == 0) {
+      F::forward(v, sc, tw, lt);
+    } else {
+      F::forward(v, sc, tw, lt);
+      const T ah = gxy[L];
+      const T al = gxy[gx * gy + L];
+#pragma unroll
+      for (int r = 0; r < R1; ++r) {
+        const int kz = F::out_index(lt, r);
+        if constexpr (sizeof(T) == 4) {
+          const float bh = gzs[kz], bl = gzs[N + kz];
+          const float gh = ah * bh;
+          const float gl = fmaf(ah, bh, -gh) + fmaf(ah, bl, al * bh);
+          v[r] = mk<T>(fmaf(v[r].x, gh, v[r].x * gl), fmaf(v[r].y, gh, v[r].y * gl));
+        } else {
+          const T f = ah * gzs[kz];
+          v[r] = mk<T>(v[r].x * f, v[r].y * f);
+        }
+      }
+      F::inverse(v, sc, tw, lt);
+    }
+    if (valid) {
+#pragma unroll
+      for (int r = 0; r < R1; ++r)
+        spec[base + (size_t)(out_dout ? F::out_index(lt, r) : F::in_index(lt, r)) * es] = v[r];
+    }
+    if constexpr (dc64) {
+      if (dcblk) {
+        // the (kx, ky) = (0, 0) pencil again in FP64 (see k_rs)
+        __syncthreads();
+        if (threadIdx.x < 32) {
+          // FP64 exchange scratch and twiddles reuse the FP32 exchange region
+          using F64 = RegFFT<double, F::R1, F::TPL>;
+          double2* dsc = reinterpret_cast<double2*>(smraw + LY::sc_off);
+          double2* tw64 = dsc + (32 / TPL) * F64::LS;
+          for (int i = threadIdx.x; i < N; i += 32) tw64[i] = gtw64[I.tw64_off + i];
+          __syncwarp();
+          double2 u[R1];
+#pragma unroll
+          for (int m = 0; m < R1; ++m) u[m] = dcb[F::in_index(lt, m)];
+          F64::forward(u, dsc + line * F64::LS, tw64, lt);
+#pragma unroll
+          for (int r = 0; r < R1; ++r) {
+            const double f = g64[I.g64_off + F::out_index(lt, r)];
+            u[r] = make_double2(u[r].x * f, u[r].y * f);
+          }
+          F64::inverse(u, dsc + line * F64::LS, tw64, lt);
+          if (line == 0) {
+#pragma unroll
+            for (int m = 0; m < R1; ++m)
+              spec[(size_t)F::in_index(lt, m) * es] = mk<T>((T)u[m].x, (T)u[m].y);
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+// X pass, XM_STEP only, persistent with the next spectrum row prefetched
+template <typename T, int N>
+__global__ void __launch_bounds__(BULK_THREADS, 2)
+k_rx_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restrict__ gtw, int t) {
+  using LY = regk::Layout<T, N>;
+  using F = typename LY::F;
+  constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cplx<T>* tw = reinterpret_cast<cplx<T>*>(smraw);
+  cplx<T>* scr = reinterpret_cast<cplx<T>*>(smraw + LY::sc_off);
+  const BulkDev<T>& I = insts[0];
+  const int ns = I.ns;
+  if (t > ns) return;
+  const int npts = I.npts;
+  const int nrows = I.gy * I.gz;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[I.px.tw_off + i];
+  __syncthreads();
+  const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
+  cplx<T>* sc = scr + line * F::LS;
+  cplx<T>* spec = I.spec;
+  const T* EA = I.E;
+  const T* EB = I.E + npts;
+  const T* LA = I.Elo ? I.Elo : I.E;
+  const T* LB = I.Elo ? I.Elo + npts : I.E + npts;
+  const bool ta = t <= I.na, tb = t <= I.nb;
+  const T* ef = ta ? EA : EB;
+  const T* eb = tb ? EB : EA;
+  const T* lf = ta ? LA : LB;
+  const T* lb = tb ? LB : LA;
+  const bool more = t < ns;
+  const bool ta2 = (t + 1) <= I.na, tb2 = (t + 1) <= I.nb;
+  const T* ef2 = ta2 ? EA : EB;
+  const T* eb2 = tb2 ? EB : EA;
+  const T* lf2 = ta2 ? LA : LB;
+  const T* lb2 = tb2 ? LB : LA;
+  cplx<T>* sl = I.slices + (size_t)t * npts;
+  cplx<T> nx[R1];
+  int tile = blockIdx.x;
+  if (tile < ntiles) {
+    const size_t b = (size_t)min(tile * LPC + line, nrows - 1) * N;
+#pragma unroll
+    for (int r = 0; r < R1; ++r) nx[r] = spec[b + F::out_index(lt, r)];
+  }
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int row0 = tile * LPC + line;
+    const bool valid = row0 < nrows;
+    const size_t base = (size_t)(valid ? row0 : nrows - 1) * N;
+    cplx<T> v[R1];
+#pragma unroll
+    for (int r = 0; r < R1; ++r) v[r] = nx[r];
+    const int nxt = tile + gridDim.x;
+    if (nxt < ntiles) {
+      const size_t b = (size_t)min(nxt * LPC + line, nrows - 1) * N;
+#pragma unroll
+      for (int r = 0; r < R1; ++r) nx[r] = spec[b + F::out_index(lt, r)];
+    }
+    F::inverse(v, sc, tw, lt);
+#pragma unroll
+    for (int m = 0; m < R1; ++m) {
+      const size_t g = base + F::in_index(lt, m);
+      const T fa = ef[g], fb = eb[g], la = lf[g], lbv = lb[g];
+      const cplx<T> q = mk<T>(emul(v[m].x, fa, la), emul(v[m].y, fb, lbv));
+      if (valid) sl[g] = q;
+      if (more) {
+        const T ga = (ef2 == ef) ? fa : ef2[g];
+        const T gb = (eb2 == eb) ? fb : eb2[g];
+        const T ha = (ef2 == ef) ? la : lf2[g];
+        const T hb = (eb2 == eb) ? lbv : lb2[g];
+        v[m] = mk<T>(emul(q.x, ga, ha), emul(q.y, gb, hb));
+      }
+    }
+    if (!more) continue;
+    F::forward(v, sc, tw, lt);
+    if (valid) {
+#pragma unroll
+      for (int r = 0; r < R1; ++r) spec[base + F::out_index(lt, r)] = v[r];
+    }
   }
 }

@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI (include/adscf.h): context, host copies, SCF driver.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -191,6 +192,10 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
   ctx->p.dss = nullptr; ctx->p.dz = nullptr; ctx->p.ext_potential = nullptr; ctx->p.graft = nullptr;
   ctx->geometry = p->geometry;
   ctx->prec = p->precision;
+  // kernel-variant switches for A/B checks (results are identical in exact
+  // arithmetic): the generic mixed-radix FFT, and the non-persistent passes
+  ctx->use_generic = std::getenv("ADSCF_GENERIC_FFT") != nullptr;
+  ctx->no_persistent = std::getenv("ADSCF_NO_PERSISTENT") != nullptr;
   ctx->gx = p->gx; ctx->gy = p->gy; ctx->gz = p->gz;
   ctx->nplanes = p->geometry == ADSCF_BULK ? p->gz : p->gz + 1;
   ctx->npts = p->gx * p->gy * ctx->nplanes;
@@ -251,7 +256,7 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
     rc = bulk_create(ctx);
   } else {
     // per-plane integration weights and wall potential (films / brush)
-    rc = film_create(ctx);
+    rc = film_create(ctx, p);
   }
   if (rc) return fail(rc);
 
@@ -271,7 +276,7 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
   S.homopolymer = ctx->geometry == ADSCF_BRUSH;
   S.ensemble = p->ensemble;
   S.rho = p->rho; S.mu = p->mu; S.volume = ctx->volume;
-  S.chain_len = p->ds * ctx->ns;
+  if (ctx->geometry == ADSCF_BULK) S.chain_len = p->ds * ctx->ns;
   S.dist = ctx->d_dist;
   S.dens = ctx->d_dens;
   S.hx = ctx->d_hx; S.hr = ctx->d_hr;
@@ -322,6 +327,7 @@ int adscf_propagate_diblock_dev(adscf_ctx* ctx, const double* d_field, double* d
     if ((rc = bulk_enqueue_propagate(ctx))) return rc;
   } else {
     if ((rc = film_enqueue_propagate(ctx, d_field))) return rc;
+    if ((rc = film_check_pivot(ctx))) return rc;
   }
   ScfDev S2 = ctx->S;
   S2.dens = d_density;
@@ -354,6 +360,7 @@ int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* den
   int rc = h2d(ctx, d_w, field, nv);
   if (rc) return rc;
   if ((rc = film_enqueue_propagate(ctx, d_w))) return rc;
+  if ((rc = film_check_pivot(ctx))) return rc;
   ScfDev S2 = ctx->S;
   S2.dens = d_out;
   k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, 0);
@@ -372,7 +379,7 @@ int adscf_propagate_step(adscf_ctx* ctx, double* prop, const double* aux, double
   if ((rc = h2d(ctx, d_p, prop, n))) return rc;
   if ((rc = h2d(ctx, d_a, aux, n))) return rc;
   if (ctx->geometry == ADSCF_BULK) rc = bulk_step_single(ctx, d_p, d_a);
-  else rc = film_step_single(ctx, d_p, d_a, ds > 0 ? ds : ctx->p.ds);
+  else if (!(rc = film_step_single(ctx, d_p, d_a, ds > 0 ? ds : ctx->p.ds))) rc = film_check_pivot(ctx);
   if (rc) return rc;
   return d2h(ctx, prop, d_p, n);
 }
@@ -537,6 +544,7 @@ int adscf_scf_run(adscf_ctx* ctx, int n_iter, double tol, adscf_iter_result* out
   adscf_iter_result r{};
   rc = read_result(ctx, &r, nullptr);  // synchronises the stream
   if (out) *out = r;
+  if (!rc && ctx->film) rc = film_check_pivot(ctx);
   return rc;
 }
 

@@ -1,19 +1,297 @@
-// film.cu -- Crank-Nicolson / ADI film and brush propagators (in progress).
+// film.cu -- film (Film_1D, Film_3D) and brush contexts: meshes, contour
+// schedules, weights and launch sequences.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "film_kernels.cuh"
 #include "internal.h"
 
-int film_create(adscf_ctx* ctx) {
-  return set_err(ctx, ADSCF_E_ARG, "film and brush geometries are not built yet");
+struct FilmState {
+  bool t64 = true;              // FP64 sweeps (FP64 context, or split with a graded mesh)
+  FilmDev<double> f64{};
+  FilmDev<float> f32{};
+  double* d_alpha = nullptr;
+  double* d_beta = nullptr;
+  double* d_gamma = nullptr;
+  double* d_dss = nullptr;
+  double* d_wA = nullptr;
+  double* d_wB = nullptr;
+  double* d_graft = nullptr;
+  void* d_q = nullptr;
+  void* d_qd = nullptr;
+  void* d_gam = nullptr;
+  void* d_w1 = nullptr;
+  int* d_err = nullptr;
+  double max_ratio = 1.0;       // largest neighbour spacing ratio of the mesh
+};
+
+namespace {
+
+int nint_f(double x) { return x >= 0 ? (int)std::floor(x + 0.5) : -(int)std::floor(-x + 0.5); }
+
+template <typename T>
+FilmDev<T>& fdev(FilmState* F);
+template <>
+FilmDev<double>& fdev<double>(FilmState* F) { return F->f64; }
+template <>
+FilmDev<float>& fdev<float>(FilmState* F) { return F->f32; }
+
+FieldRef make_ref(adscf_ctx* ctx, const double* d_w) {
+  FieldRef r;
+  r.direct = d_w;
+  r.hx = ctx->d_hx;
+  r.iter = ctx->d_iter;
+  r.slots = ctx->hist_slots;
+  r.nv = (size_t)ctx->ntypes * ctx->npts;
+  return r;
 }
-void film_destroy(adscf_ctx*) {}
-int film_enqueue_propagate(adscf_ctx* ctx, const double*) {
-  return set_err(ctx, ADSCF_E_STATE, "film geometry not built");
+
+template <typename T>
+int chains_t(adscf_ctx* ctx, const double* d_w) {
+  FilmState* F = ctx->film;
+  FilmDev<T> D = fdev<T>(F);
+  const FieldRef fr = make_ref(ctx, d_w);
+  cudaStream_t s = ctx->stream;
+  if (ctx->geometry == ADSCF_FILM_3D) {
+    // node 0 of both chains = 1, then ns Douglas ADI steps (three sweeps each)
+    k_film_fill<T><<<std::max(1, (D.npts + 255) / 256), 256, 0, s>>>(D.q, D.qd, D.npts);
+    const dim3 gx_((D.gy * (D.gz - 1) + FILM_THREADS - 1) / FILM_THREADS, 2);
+    const dim3 gy_((D.gx * (D.gz - 1) + FILM_THREADS - 1) / FILM_THREADS, 2);
+    const dim3 gz_((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 2);
+    for (int st = 1; st <= D.ns; ++st) {
+      k_adi_x<T><<<gx_, FILM_THREADS, 0, s>>>(D, fr, st);
+      k_adi_y<T><<<gy_, FILM_THREADS, 0, s>>>(D, st);
+      k_adi_z<T><<<gz_, FILM_THREADS, 0, s>>>(D, fr, st);
+    }
+  } else {
+    const dim3 g((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 2);
+    k_film1d_chains<T><<<g, FILM_THREADS, 0, s>>>(D, fr);
+  }
+  CK(cudaGetLastError());
+  return ADSCF_OK;
 }
-int film_step_single(adscf_ctx* ctx, double*, const double*, double) {
-  return set_err(ctx, ADSCF_E_STATE, "film geometry not built");
+
+template <typename T>
+int contour_t(adscf_ctx* ctx) {
+  FilmDev<T> D = fdev<T>(ctx->film);
+  k_film_contour<T><<<ctx->contour_blocks, 256, 0, ctx->stream>>>(D);
+  CK(cudaGetLastError());
+  return ADSCF_OK;
 }
-int film_enqueue_chains(adscf_ctx* ctx, const double*) {
-  return set_err(ctx, ADSCF_E_STATE, "film geometry not built");
+
+// one step of one propagator: slice 0 <- prop, step with field w and ds,
+// prop <- slice 1
+template <typename T>
+int step_single_t(adscf_ctx* ctx, double* d_prop, const double* d_w, double ds) {
+  FilmState* F = ctx->film;
+  FilmDev<T> D = fdev<T>(F);
+  cudaStream_t s = ctx->stream;
+  double h_dss[2] = {0.0, ds};
+  // a one-step schedule in the 2 spare entries past the contour schedule
+  CK(cudaMemcpyAsync(F->d_dss + D.ns + 1, h_dss, sizeof(h_dss), cudaMemcpyHostToDevice, s));
+  D.dss = F->d_dss + D.ns + 1;
+  D.ns = 1;
+  D.na = 1;
+  D.single = 1;
+  D.brush = 0;
+  const size_t n = (size_t)ctx->npts;
+  k_convert<T, double><<<std::max<size_t>(1, (n + 255) / 256), 256, 0, s>>>(d_prop, D.q, n);
+  FieldRef fr{};
+  fr.direct = d_w;
+  if (ctx->geometry == ADSCF_FILM_3D) {
+    const dim3 gx_((D.gy * (D.gz - 1) + FILM_THREADS - 1) / FILM_THREADS, 1);
+    const dim3 gy_((D.gx * (D.gz - 1) + FILM_THREADS - 1) / FILM_THREADS, 1);
+    const dim3 gz_((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 1);
+    k_adi_x<T><<<gx_, FILM_THREADS, 0, s>>>(D, fr, 1);
+    k_adi_y<T><<<gy_, FILM_THREADS, 0, s>>>(D, 1);
+    k_adi_z<T><<<gz_, FILM_THREADS, 0, s>>>(D, fr, 1);
+  } else {
+    const dim3 g((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 1);
+    k_film1d_chains<T><<<g, FILM_THREADS, 0, s>>>(D, fr);
+  }
+  k_convert<double, T><<<std::max<size_t>(1, (n + 255) / 256), 256, 0, s>>>(D.q + n, d_prop, n);
+  CK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+template <typename T>
+int alloc_t(adscf_ctx* ctx, FilmState* F, size_t gam_elems) {
+  const size_t n = (size_t)ctx->npts;
+  const size_t sl = (size_t)(ctx->ns + 1) * n;
+  if (cudaMalloc(&F->d_q, sl * sizeof(T)) || cudaMalloc(&F->d_qd, sl * sizeof(T)) ||
+      cudaMalloc(&F->d_gam, gam_elems * sizeof(T)) ||
+      (ctx->geometry == ADSCF_FILM_3D && cudaMalloc(&F->d_w1, 2 * n * sizeof(T)))) {
+    cudaGetLastError();
+    return set_err(ctx, ADSCF_E_OOM, "device allocation of film propagators failed");
+  }
+  return ADSCF_OK;
+}
+
+template <typename T>
+void fill_dev(adscf_ctx* ctx, FilmState* F, const adscf_params* p) {
+  FilmDev<T>& D = fdev<T>(F);
+  D.gx = ctx->gx; D.gy = ctx->gy; D.gz = ctx->gz;
+  D.nlines = ctx->gx * ctx->gy;
+  D.npts = ctx->npts;
+  D.ns = ctx->ns; D.na = ctx->na;
+  D.ntypes = ctx->ntypes;
+  D.brush = ctx->geometry == ADSCF_BRUSH;
+  D.single = 0;
+  D.span = p->int_span;
+  D.alpha = F->d_alpha; D.beta = F->d_beta; D.gamma = F->d_gamma;
+  D.dss = F->d_dss; D.wA = F->d_wA; D.wB = F->d_wB;
+  D.wz = ctx->d_wz;
+  D.graft = F->d_graft;
+  D.q = static_cast<T*>(F->d_q);
+  D.qd = static_cast<T*>(F->d_qd);
+  D.gam = static_cast<T*>(F->d_gam);
+  D.dist = ctx->d_dist;
+  D.qpart = ctx->d_qpart;
+  D.err = F->d_err;
+  D.dx = p->sizex / p->gx;
+  D.dy = p->sizey / p->gy;
+  D.w1 = static_cast<T*>(F->d_w1);
+}
+
+}  // namespace
+
+int film_create(adscf_ctx* ctx, const adscf_params* p) {
+  FilmState* F = new (std::nothrow) FilmState();
+  if (!F) return ADSCF_E_OOM;
+  ctx->film = F;
+  const int gz = ctx->gz;
+  if (gz < 2) return set_err(ctx, ADSCF_E_ARG, "films need gz >= 2 intervals");
+  if (ctx->geometry == ADSCF_FILM_3D && (ctx->gx < 1 || ctx->gy < 1))
+    return set_err(ctx, ADSCF_E_ARG, "grid");
+  std::vector<double> dz(p->dz, p->dz + gz + 1);
+  for (int i = 1; i <= gz; ++i)
+    if (!(dz[i] > 0)) return set_err(ctx, ADSCF_E_ARG, "dz[1..gz] must be positive");
+  // z coefficients: Film_1D / Brush form b = ds (h1+h2)/h1/h2/(h1+h2)
+  // (Film_1D/.../mod_realspace.f90:36-43), Film_3D form b = ds/h1/h2 (:70-76)
+  std::vector<double> al(gz + 1, 0.0), be(gz + 1, 0.0), ga(gz + 1, 0.0);
+  for (int z = 1; z < gz; ++z) {
+    const double h1 = dz[z], h2 = dz[z + 1];
+    al[z] = 1.0 / h1 / (h1 + h2);
+    ga[z] = 1.0 / h2 / (h1 + h2);
+    be[z] = ctx->geometry == ADSCF_FILM_3D ? 1.0 / h1 / h2 : (h1 + h2) / h1 / h2 / (h1 + h2);
+    F->max_ratio = std::max(F->max_ratio, std::max(h1 / h2, h2 / h1));
+  }
+  // integrator weights dx dy w_z (Film_3D/.../mod_realspace.f90:267-281 for
+  // span 0, Film_1D :201-218 and Brush mod_adaptive.f90:124-143 for span 1)
+  const double dx = p->sizex / p->gx, dy = p->sizey / p->gy;
+  std::vector<double> wz(gz + 1, 0.0);
+  if (p->int_scheme == 0) {
+    const int lo = p->int_span == 0 ? 0 : 1;
+    for (int i = lo; i <= gz - 1; ++i) wz[i] += dz[i];
+  } else {
+    const int hi = p->int_span == 0 ? gz : gz - 1;
+    for (int i = 1; i <= hi; ++i) { wz[i - 1] += 0.5 * dz[i]; wz[i] += 0.5 * dz[i]; }
+  }
+  for (double& v : wz) v *= dx * dy;
+  // contour schedule: dss[0..ns]
+  std::vector<double> dss(ctx->ns + 1, 0.0);
+  if (p->dss) {
+    for (int s = 0; s <= ctx->ns; ++s) dss[s] = p->dss[s];
+  } else {
+    for (int s = 1; s <= ctx->ns; ++s) dss[s] = p->ds;
+  }
+  double len = 0.0;
+  for (int s = 1; s <= ctx->ns; ++s) len += dss[s];
+  ctx->S.chain_len = len;
+  // contour weights: diblock = trapezoid per block with the step sizes
+  // (mod_diblock.f90:143-154 for uniform steps); brush = the
+  // 1/2 (dss_s + dss_{s+1}) rule of mod_homopolymer.f90:231-239, dss_0 = 0
+  std::vector<double> wA(ctx->ns + 1, 0.0), wB(ctx->ns + 1, 0.0);
+  if (ctx->geometry == ADSCF_BRUSH) {
+    const int N = ctx->ns;
+    wA[0] = 0.5 * dss[0];
+    for (int s = 1; s < N; ++s) wA[s] = 0.5 * (dss[s] + dss[s + 1]);
+    wA[N] = 0.5 * dss[N];
+  } else {
+    for (int s = 0; s < ctx->na; ++s) { wA[s] += 0.5 * dss[s + 1]; wA[s + 1] += 0.5 * dss[s + 1]; }
+    for (int s = ctx->na; s < ctx->ns; ++s) { wB[s] += 0.5 * dss[s + 1]; wB[s + 1] += 0.5 * dss[s + 1]; }
+  }
+  // precision: FP32 sweeps on the split path unless the mesh is graded past
+  // a neighbour spacing ratio of 1.5, where the Thomas sweep stays FP64
+  F->t64 = !(ctx->prec == ADSCF_SPLIT && F->max_ratio <= 1.5);
+  const size_t L = (size_t)ctx->gx * ctx->gy;
+  size_t gam_elems = 2 * (size_t)(gz + 1) * L;
+  if (ctx->geometry == ADSCF_FILM_3D) {
+    const size_t lx = (size_t)ctx->gy * (gz - 1), ly = (size_t)ctx->gx * (gz - 1);
+    gam_elems = std::max(gam_elems, std::max(2 * 2 * (size_t)ctx->gx * lx, 2 * 2 * (size_t)ctx->gy * ly));
+  }
+  CK(cudaMalloc(&F->d_alpha, (gz + 1) * sizeof(double)));
+  CK(cudaMalloc(&F->d_beta, (gz + 1) * sizeof(double)));
+  CK(cudaMalloc(&F->d_gamma, (gz + 1) * sizeof(double)));
+  CK(cudaMalloc(&F->d_dss, (ctx->ns + 3) * sizeof(double)));
+  CK(cudaMalloc(&F->d_wA, (ctx->ns + 1) * sizeof(double)));
+  CK(cudaMalloc(&F->d_wB, (ctx->ns + 1) * sizeof(double)));
+  CK(cudaMalloc(&F->d_err, sizeof(int)));
+  CK(cudaMalloc(&ctx->d_wz, (gz + 1) * sizeof(double)));
+  CK(cudaMemcpy(F->d_alpha, al.data(), (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(F->d_beta, be.data(), (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(F->d_gamma, ga.data(), (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(F->d_dss, dss.data(), (ctx->ns + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(F->d_wA, wA.data(), (ctx->ns + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(F->d_wB, wB.data(), (ctx->ns + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_wz, wz.data(), (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemset(F->d_err, 0, sizeof(int)));
+  if (p->ext_potential) {
+    CK(cudaMalloc(&ctx->d_ext, (size_t)ctx->ntypes * (gz + 1) * sizeof(double)));
+    CK(cudaMemcpy(ctx->d_ext, p->ext_potential, (size_t)ctx->ntypes * (gz + 1) * sizeof(double),
+                  cudaMemcpyHostToDevice));
+  }
+  if (ctx->geometry == ADSCF_BRUSH) {
+    if (!p->graft) return set_err(ctx, ADSCF_E_ARG, "brush needs the grafting distribution");
+    CK(cudaMalloc(&F->d_graft, (gz + 1) * sizeof(double)));
+    CK(cudaMemcpy(F->d_graft, p->graft, (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  ctx->contour_blocks = (int)std::min<size_t>(((size_t)ctx->npts + 255) / 256, 152 * 4);
+  CK(cudaMalloc(&ctx->d_qpart, ctx->contour_blocks * sizeof(double)));
+  int rc = F->t64 ? alloc_t<double>(ctx, F, gam_elems) : alloc_t<float>(ctx, F, gam_elems);
+  if (rc) return rc;
+  if (F->t64) fill_dev<double>(ctx, F, p);
+  else fill_dev<float>(ctx, F, p);
+  ctx->film_launches = ctx->geometry == ADSCF_FILM_3D ? 1 + 3 * ctx->ns : 1;
+  ctx->film_contour_launches = 1;
+  return ADSCF_OK;
+}
+
+void film_destroy(adscf_ctx* ctx) {
+  FilmState* F = ctx->film;
+  if (!F) return;
+  cudaFree(F->d_alpha); cudaFree(F->d_beta); cudaFree(F->d_gamma);
+  cudaFree(F->d_dss); cudaFree(F->d_wA); cudaFree(F->d_wB); cudaFree(F->d_graft);
+  cudaFree(F->d_q); cudaFree(F->d_qd); cudaFree(F->d_gam); cudaFree(F->d_w1);
+  cudaFree(F->d_err); cudaFree(ctx->d_qpart);
+  delete F;
+  ctx->film = nullptr;
+}
+
+int film_enqueue_chains(adscf_ctx* ctx, const double* d_w) {
+  return ctx->film->t64 ? chains_t<double>(ctx, d_w) : chains_t<float>(ctx, d_w);
 }
 int film_enqueue_contour(adscf_ctx* ctx) {
-  return set_err(ctx, ADSCF_E_STATE, "film geometry not built");
+  return ctx->film->t64 ? contour_t<double>(ctx) : contour_t<float>(ctx);
+}
+int film_enqueue_propagate(adscf_ctx* ctx, const double* d_w) {
+  int rc = film_enqueue_chains(ctx, d_w);
+  return rc ? rc : film_enqueue_contour(ctx);
+}
+int film_step_single(adscf_ctx* ctx, double* d_prop, const double* d_w, double ds) {
+  return ctx->film->t64 ? step_single_t<double>(ctx, d_prop, d_w, ds)
+                        : step_single_t<float>(ctx, d_prop, d_w, ds);
+}
+// pivot flag set by any sweep since the last check (cleared on read)
+int film_check_pivot(adscf_ctx* ctx) {
+  if (!ctx->film) return ADSCF_OK;
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, ctx->film->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (e) {
+    CK(cudaMemsetAsync(ctx->film->d_err, 0, sizeof(int), ctx->stream));
+    return set_err(ctx, ADSCF_E_PIVOT, "zero pivot in a tridiagonal sweep (TriDiag Error)");
+  }
+  return ADSCF_OK;
 }

@@ -40,6 +40,8 @@ struct adscf_ctx {
   size_t smem_x = 0, smem_y = 0, smem_z = 0;
   int regx = 0, regy = 0, regz = 0;   // register-FFT line length per pass (0: generic)
   int use_generic = 0;                // force the generic mixed-radix kernels
+  int no_persistent = 0;              // disable the persistent pipelined passes
+  int pgrid_x = 0, pgrid_y = 0, pgrid_z = 0;  // persistent grid sizes (0: not used)
   int contour_blocks = 0;
 
   // ---- SCF state (FP64)
@@ -91,7 +93,8 @@ int bulk_r2c(adscf_ctx* ctx, const double* d_prop, double* h_half);
 int bulk_c2r(adscf_ctx* ctx, const double* h_half, double* d_prop);
 int bulk_mix_e(adscf_ctx* ctx);                 // k_mix with E update
 // films (film.cu)
-int film_create(adscf_ctx* ctx);
+int film_create(adscf_ctx* ctx, const adscf_params* p);
+int film_check_pivot(adscf_ctx* ctx);
 void film_destroy(adscf_ctx* ctx);
 int film_enqueue_propagate(adscf_ctx* ctx, const double* d_w);
 int film_enqueue_chains(adscf_ctx* ctx, const double* d_w);

@@ -408,7 +408,7 @@ k_mix(ScfDev S, T* E, T* Elo, double ds) {
     }
     S.hx[(size_t)nxt * nv + i] = x;
     if (E) {
-      const double e = exp(-0.5 * ds * x);
+      const double e = exp_boltzmann(-0.5 * ds * x);
       const T h = (T)e;
       E[i] = h;
       if (Elo) Elo[i] = (T)(e - (double)h);

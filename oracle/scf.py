@@ -41,3 +41,37 @@ def bulk_scf(field, n_iter, grid, size, ds, block_length, kappa, chi,
         field = mixer(field, dfield, it)
         density = newdensity
     return field, hist
+
+
+def film_scf(field, n_iter, dz, dss, n_a, step, kappa, chi, surface, sizes,
+             int_scheme=1, span="full", mixing_type=2, lam=0.1, m=2,
+             lam00=1.0e-3, warm=None, rho=1.0, density0=None, gram=True):
+    """Film SCF loop, Film_CK_AD/Film_1D/Main_Diblock_Melt/main_diblock_melt.f90:
+    155-169: densities (film Propagate_Diblock), Check_Accuracy over all
+    planes, Calculate_Mean_Ext_Fields with the wall potential ``surface``
+    ([2][0:gz]), and Mix_Fields over the interior planes 1..gz-1 only
+    (:362-378).  ``step(prop, w, ds)`` is the geometry's propagator step."""
+    from . import film
+    field = np.array(field, dtype=np.float64, copy=True)
+    density = np.zeros_like(field) if density0 is None else np.array(density0, dtype=np.float64)
+    gz = dz.shape[0] - 1
+    interior = (slice(None), slice(1, gz))
+    nvar = field[interior].size
+    mixer = iterate.Mixer(nvar, mixing_type, lam, m=m, lam00=lam00, warm=warm, gram=gram)
+    dx = sizes[0] / (field.shape[-1] if field.ndim == 4 else 1)
+    dy = sizes[1] / (field.shape[-2] if field.ndim == 4 else 1)
+    ext = (slice(None), slice(None)) + (None,) * (field.ndim - 2)
+    hist = []
+    for it in range(1, n_iter + 1):
+        r = film.film_propagate_diblock(field, dz, dss, n_a, step, rho=rho, dx=dx, dy=dy,
+                                        int_scheme=int_scheme, span=span, sizes=sizes)
+        newdensity = r["density"]
+        acc = interactions.check_accuracy(density, newdensity)
+        newfield = interactions.mean_fields(newdensity, kappa, chi, surface=surface[ext])
+        hist.append(dict(iter=it, accuracy=acc, Qsum=r["Qsum"], density=newdensity,
+                         field=field.copy()))
+        dfield = newfield - field
+        x = mixer(field[interior].copy(), dfield[interior].copy(), it)
+        field[interior] = x
+        density = newdensity
+    return field, hist

@@ -1,0 +1,161 @@
+"""Film (Film_1D CN, Film_3D Douglas ADI) and brush propagators on the GPU,
+through the C ABI, against the FP64 oracle (oracle/film.py).  Tolerances:
+FP64 relative 1e-11; split (FP32 sweeps on a mildly graded mesh) 2e-5."""
+import numpy as np
+import pytest
+
+from oracle import film as of
+from oracle import interactions as oi
+from oracle import scf as oscf
+
+pytestmark = pytest.mark.gpu
+
+from adscf_gb300 import (FILM_1D, FILM_3D, BRUSH, FP64, SPLIT, MIX_LAMBDA,
+                         MIX_ANDERSON, AdscfError, Context)
+
+
+def film_ctx(geom, grid, dz, size, ds=0.01, f=(0.5, 0.5), prec=FP64, **kw):
+    return Context(geom, grid=grid, size=size, ds=ds, block_length=f, dz=dz,
+                   precision=prec, **kw)
+
+
+@pytest.mark.parametrize("mesh", [0, 1])
+def test_film1d_cn_step(mesh, rng):
+    gz, D, ds = 40, 3.0, 0.01
+    dz, zr = of.generate_mesh(mesh, gz, D, film3d=False)
+    q = rng.random(gz + 1) + 0.5
+    w = rng.standard_normal(gz + 1)
+    ref = of.cn_step_1d(q, w, dz, ds, solver="inplace")
+    with film_ctx(FILM_1D, (1, 1, gz), dz, (1.0, 1.0, D), ds) as c:
+        out = c.propagate_step(q, w, ds)
+    assert np.max(np.abs(out - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("ensemble", [1, 2])
+def test_film1d_propagate_diblock(ensemble, rng):
+    gz, D, ds = 64, 4.0, 0.02
+    dz, zr = of.tanh_mesh(gz, D)
+    field = 0.5 * rng.standard_normal((2, gz + 1))
+    dss = np.r_[0.0, np.full(50, ds)]
+    step = lambda p, w, h: of.cn_step_1d(p, w, dz, h)
+    ref = of.film_propagate_diblock(field, dz, dss, 25, step, rho=1.0, int_scheme=1,
+                                    span="interior", ensemble=ensemble, mu=0.4,
+                                    sizes=(1.0, 1.0, D))
+    with film_ctx(FILM_1D, (1, 1, gz), dz, (1.0, 1.0, D), ds, int_scheme=1, int_span=1,
+                  ensemble=ensemble, mu=0.4) as c:
+        dens, res = c.propagate_diblock(field)
+    assert abs(res.Qsum / ref["Qsum"] - 1) < 1e-12
+    assert np.max(np.abs(dens - ref["density"])) < 1e-11 * np.max(np.abs(ref["density"]))
+
+
+def test_film1d_many_lines_adaptive_contour(rng):
+    """gx*gy independent lines on one mesh, end-refined contour steps."""
+    gx, gy, gz, D = 5, 3, 48, 3.0
+    dz, zr = of.tanh_mesh(gz, D)
+    dss = of.contour_steps(60, ds_scheme=1)
+    field = rng.standard_normal((2, gz + 1, gy, gx))
+    step = lambda p, w, h: of.cn_step_1d(p, w, dz, h)
+    ref = of.film_propagate_diblock(field, dz, dss, 30, step, rho=1.0, dx=1.0, dy=1.0,
+                                    int_scheme=1, span="full", sizes=(gx, gy, D))
+    with film_ctx(FILM_1D, (gx, gy, gz), dz, (gx * 1.0, gy * 1.0, D), dss=dss, n_a=30,
+                  int_scheme=1, int_span=0) as c:
+        dens, res = c.propagate_diblock(field)
+    assert abs(res.Qsum / ref["Qsum"] - 1) < 1e-12
+    assert np.max(np.abs(dens - ref["density"])) < 1e-11 * np.max(np.abs(ref["density"]))
+
+
+def test_film1d_split_precision(rng):
+    gz, D, ds = 64, 3.0, 0.01
+    dz, zr = of.generate_mesh(0, gz, D)
+    field = rng.standard_normal((2, gz + 1))
+    dss = np.r_[0.0, np.full(100, ds)]
+    step = lambda p, w, h: of.cn_step_1d(p, w, dz, h)
+    ref = of.film_propagate_diblock(field, dz, dss, 50, step, sizes=(1.0, 1.0, D))
+    with film_ctx(FILM_1D, (1, 1, gz), dz, (1.0, 1.0, D), ds, prec=SPLIT) as c:
+        dens, res = c.propagate_diblock(field)
+    assert abs(np.log(res.Qsum) - np.log(ref["Qsum"])) < 2e-5
+    assert np.max(np.abs(dens - ref["density"])) < 2e-5 * np.max(np.abs(ref["density"]))
+
+
+def test_film3d_adi_step(rng):
+    gx, gy, gz, ds = 8, 6, 12, 0.02
+    dz, zr = of.generate_mesh(1, gz, 2.5)
+    size = (3.0, 2.4, 2.5)
+    q = rng.random((gz + 1, gy, gx)) + 0.5
+    w = rng.standard_normal((gz + 1, gy, gx))
+    ref = of.adi_step_3d(q, w, dz, size[0] / gx, size[1] / gy, ds)
+    with film_ctx(FILM_3D, (gx, gy, gz), dz, size, ds) as c:
+        out = c.propagate_step(q, w, ds)
+    assert np.max(np.abs(out - ref)) < 1e-12 * np.max(np.abs(ref))
+
+
+def test_film3d_propagate_diblock(rng):
+    gx, gy, gz, ds = 8, 6, 10, 0.05
+    dz, zr = of.tanh_mesh(gz, 3.0)
+    size = (3.0, 2.4, 3.0)
+    field = 0.5 * rng.standard_normal((2, gz + 1, gy, gx))
+    dss = np.r_[0.0, np.full(20, ds)]
+    step = lambda p, w, h: of.adi_step_3d(p, w, dz, size[0] / gx, size[1] / gy, h)
+    ref = of.film_propagate_diblock(field, dz, dss, 5, step, dx=size[0] / gx,
+                                    dy=size[1] / gy, int_scheme=1, span="full", sizes=size)
+    with film_ctx(FILM_3D, (gx, gy, gz), dz, size, ds, f=(0.25, 0.75)) as c:
+        dens, res = c.propagate_diblock(field)
+    assert abs(res.Qsum / ref["Qsum"] - 1) < 1e-11
+    assert np.max(np.abs(dens - ref["density"])) < 1e-10 * np.max(np.abs(ref["density"]))
+
+
+def test_brush_propagate_homopolymer(rng):
+    gz, D = 80, 5.0
+    dz, zr = of.generate_mesh(0, gz, D)
+    dss = of.contour_steps(120, ds_scheme=1)
+    graft = np.zeros(gz + 1)
+    graft[4] = 1.0
+    wts = of.integrator_weights(dz, 1, "interior")
+    graft /= np.dot(wts, graft)                      # mod_homopolymer.f90:145-150
+    field = 0.3 * rng.standard_normal(gz + 1)
+    ref = of.propagate_homopolymer(field, dz, dss, graft, 0.4, int_scheme=1,
+                                   span="interior", sizes=(1.0, 1.0, D))
+    with Context(BRUSH, grid=(1, 1, gz), size=(1.0, 1.0, D), dss=dss, dz=dz, graft=graft,
+                 rho=0.4, int_scheme=1, int_span=1, ww=1.0) as c:
+        dens, res = c.propagate_homopolymer(field)
+    assert abs(res.Qsum / ref["Qsum"] - 1) < 1e-11
+    assert np.max(np.abs(dens - ref["density"])) < 1e-10 * np.max(np.abs(ref["density"]))
+    assert abs(res.mu - ref["mu"]) < 1e-10
+
+
+@pytest.mark.parametrize("mtype", [MIX_LAMBDA, MIX_ANDERSON])
+def test_film1d_scf_loop_with_walls(mtype, rng):
+    gz, D, ds = 48, 3.0, 0.02
+    dz, zr = of.tanh_mesh(gz, D)
+    surf = np.stack([0.8 * oi.wall_potential_shape(zr, D, 0.4), -0.4 * oi.wall_potential_shape(zr, D, 0.4)])
+    z = zr / D
+    field = np.stack([2.0 * np.cos(2 * np.pi * z), -2.0 * np.cos(2 * np.pi * z)])
+    field[:, 0] = field[:, -1] = 0.0
+    dss = np.r_[0.0, np.full(50, ds)]
+    step = lambda p, w, h: of.cn_step_1d(p, w, dz, h)
+    xr, hist = oscf.film_scf(field, 8, dz, dss, 25, step, 25.0, 15.0, surf, (1.0, 1.0, D),
+                             int_scheme=1, span="full", mixing_type=mtype, lam=0.1, m=2,
+                             lam00=0.05, warm=3)
+    with film_ctx(FILM_1D, (1, 1, gz), dz, (1.0, 1.0, D), ds, kappa=25.0, chi=15.0,
+                  ext_potential=surf, int_scheme=1, int_span=0, mixing_type=mtype,
+                  mixing_dim=2, lam=0.1, lam_warm=0.05, warm_iters=3) as c:
+        c.set_field(field)
+        res = c.scf_run(8)
+        xg = c.get_field().reshape(2, gz + 1)
+    assert res.iter == 8
+    assert abs(res.accuracy - hist[-1]["accuracy"]) <= 1e-8 * hist[-1]["accuracy"] + 1e-18
+    assert np.max(np.abs(xg - xr)) < 1e-9 * (1 + np.max(np.abs(xr)))
+
+
+def test_zero_pivot_returns_status():
+    """A zero Thomas pivot (the reference's 'TriDiag Error' stop) becomes
+    ADSCF_E_PIVOT: uniform h = 0.5, ds = 0.25 gives b = 1 and a field of -16
+    at plane 1 makes the first interior diagonal exactly zero."""
+    gz = 8
+    dz = np.r_[0.0, np.full(gz, 0.5)]
+    w = np.zeros(gz + 1)
+    w[1] = -16.0
+    with film_ctx(FILM_1D, (1, 1, gz), dz, (1.0, 1.0, 4.0), 0.25) as c:
+        with pytest.raises(AdscfError) as e:
+            c.propagate_step(np.ones(gz + 1), w, 0.25)
+    assert e.value.code == 3
