@@ -211,6 +211,21 @@ int create_t(adscf_ctx* ctx) {
     const double a = -2.0 * M_PI * (double)z / (double)ctx->gz;
     tw64[z] = make_double2(std::cos(a), std::sin(a));
   }
+  // circular-convolution kernel of the (kx, ky) = (0, 0) pencil:
+  // c(d) = sum_kz G(kz) cos(2 pi kz d / gz), G(kz) = exp(-ds kz^2)/N (FP64;
+  // the phase index kz*d is reduced mod gz before the cosine)
+  {
+    std::vector<double> c(ctx->gz, 0.0);
+    for (int d = 0; d < ctx->gz; ++d) {
+      double s = 0.0;
+      for (int k = 0; k < ctx->gz; ++k) {
+        const long long m = ((long long)k * d) % ctx->gz;
+        s += g64[k] * std::cos(2.0 * M_PI * (double)m / (double)ctx->gz);
+      }
+      c[d] = s;
+    }
+    g64 = c;
+  }
   I.tw64_off = 0;
   I.g64_off = 0;
   CK(cudaMalloc(&ctx->d_tw64, tw64.size() * sizeof(double2)));

@@ -62,6 +62,64 @@ __device__ __forceinline__ int chain_type_fwd(const BulkDev<T>& I, int t) { retu
 template <typename T>
 __device__ __forceinline__ int chain_type_bwd(const BulkDev<T>& I, int t) { return t <= I.nb ? 1 : 0; }
 
+// ---------------------------------------------------------------------------
+// The (kx, ky) = (0, 0) z pencil carries the mean of both propagators; FP32
+// rounding of it would be coherent over the whole box and accumulate over the
+// contour.  Its forward z-FFT, factor exp(-ds kz^2)/N and inverse z-FFT are a
+// circular convolution with the real kernel c(d) = sum_kz G(kz) cos(2 pi kz
+// d / gz) (FP64 table), evaluated here in float-float arithmetic: exact
+// products (TwoProd) and compensated sums (TwoSum), ~48-bit accurate on FP32
+// units.  All threads of the block call dc_pencil_load / _apply / _store.
+// ---------------------------------------------------------------------------
+struct DcPencil {
+  float2* in;    // [n] pencil before the pass (as loaded)
+  float2* out;   // [n] convolved pencil
+  float2* c;     // [n] kernel, (hi, lo) FP32 split of c(d)
+};
+
+template <typename T>
+__device__ __forceinline__ void dc_pencil_load(const cplx<T>* spec, size_t es, int n,
+                                               const double* c64, DcPencil D) {
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const cplx<T> v = spec[(size_t)j * es];
+    D.in[j] = make_float2((float)v.x, (float)v.y);
+    const double c = c64[j];
+    const float h = (float)c;
+    D.c[j] = make_float2(h, (float)(c - (double)h));
+  }
+}
+
+__device__ __forceinline__ void ff_fma(float& sh, float& sl, float ch, float cl, float x) {
+  const float p = ch * x;
+  const float e = fmaf(ch, x, -p) + cl * x;   // exact product plus the lo term
+  const float s = sh + p;
+  const float bb = s - sh;
+  const float t = (sh - (s - bb)) + (p - bb) + sl + e;
+  sh = s + t;
+  sl = t - (sh - s);
+}
+
+__device__ __forceinline__ void dc_pencil_apply(int n, DcPencil D) {
+  for (int z = threadIdx.x; z < n; z += blockDim.x) {
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    for (int d = 0; d < n; ++d) {
+      int zz = z - d;
+      if (zz < 0) zz += n;
+      const float2 p = D.in[zz];
+      const float2 c = D.c[d];
+      ff_fma(rh, rl, c.x, c.y, p.x);
+      ff_fma(ih, il, c.x, c.y, p.y);
+    }
+    D.out[z] = make_float2(rh + rl, ih + il);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dc_pencil_store(cplx<T>* spec, size_t es, int n, DcPencil D) {
+  for (int j = threadIdx.x; j < n; j += blockDim.x)
+    spec[(size_t)j * es] = mk<T>((T)D.out[j].x, (T)D.out[j].y);
+}
+
 // shared-memory carve-up for one pass: twiddles (N) + two line buffers
 template <typename T>
 __device__ __forceinline__ void carve(unsigned char* raw, const Plan1D& P, cplx<T>*& tw,
@@ -230,26 +288,22 @@ k_bulk_strided(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ wo
   __syncthreads();
   cplx<T>* r;
   if (kind == 2) {
-    // The (kx, ky) = (0, 0) pencil carries the mean of the propagator; in FP32
-    // its rounding would be coherent over the whole box and accumulate over the
-    // contour, so it is transformed in FP64 (one line, negligible cost).
+    // the (kx, ky) = (0, 0) pencil in float-float (see DcPencil)
     constexpr bool dc64 = sizeof(T) == 4;
-    double2* a64 = nullptr;
-    double2* b64 = nullptr;
-    double2* tw64 = nullptr;
-    Plan1D P64 = P;
-    if (dc64 && L0 == 0) {
-      unsigned char* tail = reinterpret_cast<unsigned char*>(b1 + P.lpc * P.ld);
-      tail = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tail) + 15) & ~uintptr_t(15));
-      tw64 = reinterpret_cast<double2*>(tail);
-      a64 = tw64 + ((N + 1) & ~1);
-      b64 = a64 + P.ld;
-      P64.tw_off = 0;
+    const bool dcline = dc64 && L0 == 0;
+    unsigned char* tail = reinterpret_cast<unsigned char*>(b1 + P.lpc * P.ld);
+    tail = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(tail) + 15) & ~uintptr_t(15));
+    float2* dcf = reinterpret_cast<float2*>(tail);
+    const DcPencil dcp{dcf, dcf + N, dcf + 2 * N};
+    if (dcline) {
       for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        tw64[i] = gtw64[I.tw64_off + i];
-        a64[i] = make_double2((double)b0[i].x, (double)b0[i].y);
+        dcf[i] = make_float2((float)b0[i].x, (float)b0[i].y);   // line 0 = (x, y) = (0, 0)
+        const double c = g64[I.g64_off + i];
+        const float h = (float)c;
+        dcp.c[i] = make_float2(h, (float)(c - (double)h));
       }
       __syncthreads();
+      dc_pencil_apply(N, dcp);
     }
     r = fft_lines<T>(b0, b1, tw, P, line, lt, active, +1);
     // exp(-ds (kx^2 + ky^2 + kz^2)) / N from the separable tables, applied with
@@ -274,18 +328,9 @@ k_bulk_strided(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ wo
     __syncthreads();
     cplx<T>* o = (r == b0) ? b1 : b0;
     r = fft_lines<T>(r, o, tw, P, line, lt, active, -1);
-    if (dc64 && L0 == 0) {
-      const bool act = threadIdx.x < P64.tpl;
-      double2* rr = fft_lines<double>(a64, b64, tw64, P64, 0, threadIdx.x, act, +1);
-      for (int j = threadIdx.x; j < N; j += blockDim.x) {
-        const double f = g64[I.g64_off + j];
-        rr[j] = make_double2(rr[j].x * f, rr[j].y * f);
-      }
-      __syncthreads();
-      double2* oo = (rr == a64) ? b64 : a64;
-      rr = fft_lines<double>(rr, oo, tw64, P64, 0, threadIdx.x, act, -1);
+    if (dcline) {
       for (int j = threadIdx.x; j < N; j += blockDim.x)
-        r[j] = mk<T>((T)rr[j].x, (T)rr[j].y);
+        r[j] = mk<T>((T)dcp.out[j].x, (T)dcp.out[j].y);
       __syncthreads();
     }
   } else {

@@ -27,7 +27,7 @@ struct Layout {
   static constexpr size_t sc_off = ((tw_bytes + gz_bytes + 15) / 16) * 16;
   static constexpr size_t sc_bytes = (size_t)LPC * F::LS * sizeof(cplx<T>);
   static constexpr size_t dc_off = ((sc_off + sc_bytes + 15) / 16) * 16;
-  static constexpr size_t bytes = dc_off + N * sizeof(double2);
+  static constexpr size_t bytes = dc_off + 3 * N * sizeof(float2);
 };
 
 __device__ __forceinline__ int ilog2(int v) { return __ffs(v) - 1; }
@@ -166,7 +166,6 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smraw);
   T* gzs = reinterpret_cast<T*>(smraw + LY::tw_bytes);
   cplx<T>* scr = reinterpret_cast<cplx<T>*>(smraw + LY::sc_off);
-  double2* dcb = reinterpret_cast<double2*>(smraw + LY::dc_off);
   const int2 w = work[blockIdx.x];
   const BulkDev<T>& I = insts[w.x];
   if (t > I.ns) return;
@@ -202,15 +201,18 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
       if (valid) spec[base + (size_t)F::in_index(lt, m) * es] = v[m];
     return;
   }
+  // (0, 0) pencil in float-float (CTA of tile 0), read before it is overwritten
+  constexpr bool dc64 = sizeof(T) == 4 && KIND == 2;
+  const bool dcline = dc64 && L0 == 0;
+  float2* dcf = reinterpret_cast<float2*>(smraw + LY::dc_off);
+  const DcPencil dcp{dcf, dcf + N, dcf + 2 * N};
+  if (dcline) {
+    dc_pencil_load<T>(spec, es, N, g64 + I.g64_off, dcp);
+    __syncthreads();
+    dc_pencil_apply(N, dcp);
+  }
 #pragma unroll
   for (int m = 0; m < R1; ++m) v[m] = spec[base + (size_t)F::in_index(lt, m) * es];
-  constexpr bool dc64 = sizeof(T) == 4 && KIND == 2;
-  const bool dcline = dc64 && L0 == 0;  // CTA holding the (0,0) pencil
-  if (dcline && line == 0) {
-#pragma unroll
-    for (int m = 0; m < R1; ++m)
-      dcb[F::in_index(lt, m)] = make_double2((double)v[m].x, (double)v[m].y);
-  }
   F::forward(v, sc, tw, lt);
   if constexpr (KIND == 0 || KIND == 3) {
     if (valid) {
@@ -244,31 +246,9 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
 #pragma unroll
     for (int m = 0; m < R1; ++m) spec[base + (size_t)F::in_index(lt, m) * es] = v[m];
   }
-  if constexpr (!dc64) return;
-  if (!dcline) return;
-  // (kx, ky) = (0, 0) pencil again in FP64: it carries the mean of both
-  // propagators, whose FP32 rounding would be coherent over the whole box
-  __syncthreads();
-  if (threadIdx.x >= 32) return;
-  using F64 = RegFFT<double, F::R1, F::TPL>;
-  double2* sc64 = reinterpret_cast<double2*>(smraw + LY::sc_off) + line * F64::LS;
-  double2* tw64 = reinterpret_cast<double2*>(smraw + LY::sc_off) + (32 / TPL) * F64::LS;
-  for (int i = threadIdx.x; i < N; i += 32) tw64[i] = gtw64[I.tw64_off + i];
-  __syncwarp();
-  double2 u[R1];
-#pragma unroll
-  for (int m = 0; m < R1; ++m) u[m] = dcb[F::in_index(lt, m)];
-  F64::forward(u, sc64, tw64, lt);
-#pragma unroll
-  for (int r = 0; r < R1; ++r) {
-    const double f = g64[I.g64_off + F::out_index(lt, r)];
-    u[r] = make_double2(u[r].x * f, u[r].y * f);
-  }
-  F64::inverse(u, sc64, tw64, lt);
-  if (line == 0) {
-#pragma unroll
-    for (int m = 0; m < R1; ++m)
-      spec[(size_t)F::in_index(lt, m) * es] = mk<T>((T)u[m].x, (T)u[m].y);
+  if (dcline) {
+    __syncthreads();
+    dc_pencil_store<T>(spec, es, N, dcp);
   }
 }
 
@@ -293,7 +273,6 @@ k_rs_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restri
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smraw);
   T* gzs = reinterpret_cast<T*>(smraw + LY::tw_bytes);
   cplx<T>* scr = reinterpret_cast<cplx<T>*>(smraw + LY::sc_off);
-  double2* dcb = reinterpret_cast<double2*>(smraw + LY::dc_off);
   const BulkDev<T>& I = insts[0];
   if (t > I.ns) return;
   const int gx = I.gx, gy = I.gy;
@@ -314,6 +293,16 @@ k_rs_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restri
   const T* gxy = fk + I.gxy_off;
   auto line_of = [&](int tile) { return min(tile * LPC + line, nlines - 1); };
   auto base_of = [&](int L) { return (size_t)(L >> lgx) * ostride + (L & (gx - 1)); };
+  // (0, 0) pencil in float-float: read before CTA 0 overwrites it (tile 0)
+  constexpr bool dc64 = sizeof(T) == 4 && KIND == 2;
+  float2* dcf = reinterpret_cast<float2*>(smraw + LY::dc_off);
+  const DcPencil dcp{dcf, dcf + N, dcf + 2 * N};
+  const bool dcblk = dc64 && blockIdx.x == 0;
+  if (dcblk) {
+    dc_pencil_load<T>(spec, es, N, g64 + I.g64_off, dcp);
+    __syncthreads();
+    dc_pencil_apply(N, dcp);
+  }
   cplx<T> nx[R1];
   int tile = blockIdx.x;
   if (tile < ntiles) {
@@ -336,12 +325,6 @@ k_rs_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restri
 #pragma unroll
       for (int r = 0; r < R1; ++r)
         nx[r] = spec[b + (size_t)(in_dout ? F::out_index(lt, r) : F::in_index(lt, r)) * es];
-    }
-    constexpr bool dc64 = sizeof(T) == 4 && KIND == 2;
-    const bool dcblk = dc64 && tile == 0;
-    if (dcblk && line == 0) {
-#pragma unroll
-      for (int m = 0; m < R1; ++m) dcb[F::in_index(lt, m)] = make_double2((double)v[m].x, (double)v[m].y);
     }
     if constexpr (KIND == 1) {
       F::inverse(v, sc, tw, lt);
@@ -371,36 +354,10 @@ k_rs_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restri
       for (int r = 0; r < R1; ++r)
         spec[base + (size_t)(out_dout ? F::out_index(lt, r) : F::in_index(lt, r)) * es] = v[r];
     }
-    if constexpr (dc64) {
-      if (dcblk) {
-        // the (kx, ky) = (0, 0) pencil again in FP64 (see k_rs)
-        __syncthreads();
-        if (threadIdx.x < 32) {
-          // FP64 exchange scratch and twiddles reuse the FP32 exchange region
-          using F64 = RegFFT<double, F::R1, F::TPL>;
-          double2* dsc = reinterpret_cast<double2*>(smraw + LY::sc_off);
-          double2* tw64 = dsc + (32 / TPL) * F64::LS;
-          for (int i = threadIdx.x; i < N; i += 32) tw64[i] = gtw64[I.tw64_off + i];
-          __syncwarp();
-          double2 u[R1];
-#pragma unroll
-          for (int m = 0; m < R1; ++m) u[m] = dcb[F::in_index(lt, m)];
-          F64::forward(u, dsc + line * F64::LS, tw64, lt);
-#pragma unroll
-          for (int r = 0; r < R1; ++r) {
-            const double f = g64[I.g64_off + F::out_index(lt, r)];
-            u[r] = make_double2(u[r].x * f, u[r].y * f);
-          }
-          F64::inverse(u, dsc + line * F64::LS, tw64, lt);
-          if (line == 0) {
-#pragma unroll
-            for (int m = 0; m < R1; ++m)
-              spec[(size_t)F::in_index(lt, m) * es] = mk<T>((T)u[m].x, (T)u[m].y);
-          }
-        }
-        __syncthreads();
-      }
-    }
+  }
+  if (dcblk) {
+    __syncthreads();
+    dc_pencil_store<T>(spec, es, N, dcp);
   }
 }
 
