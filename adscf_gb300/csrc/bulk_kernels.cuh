@@ -37,8 +37,7 @@ struct BulkDev {
   int tw64_off, g64_off;     // FP64 twiddles / factors of the (0,0) z pencil
   cplx<T>* spec;             // [npts] complex spectrum / work buffer
   cplx<T>* slices;           // [(ns+1)][npts] (q_t, qdag_t)
-  T* E;                      // [2][npts] exp(-ds w/2), species A, B
-  T* Elo;                    // [2][npts] FP32 residue of E (null in FP64)
+  T* E;                      // [npts] interleaved exp(-ds w/2) (see EPt)
   double* dist;              // [2][npts] contour integrals (block A, block B)
   double* qpart;             // [gridDim] partial sums of q_N
 };
@@ -56,6 +55,27 @@ struct XAux {
 // factor exact to ~1e-14 so its rounding cannot bias every step the same way
 __device__ __forceinline__ float emul(float z, float hi, float lo) { return fmaf(z, hi, z * lo); }
 __device__ __forceinline__ double emul(double z, double hi, double) { return z * hi; }
+
+// Boltzmann factors of one point, stored interleaved so one 16-byte (FP32)
+// or 16-byte (FP64) load brings both species: FP32 keeps (A, B, A residue,
+// B residue) as float4, FP64 keeps (A, B) as double2.
+template <typename T>
+struct EPt { T a, b, al, bl; };
+__device__ __forceinline__ EPt<float> load_ept(const float* E, size_t g) {
+  const float4 v = reinterpret_cast<const float4*>(E)[g];
+  return {v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ EPt<double> load_ept(const double* E, size_t g) {
+  const double2 v = reinterpret_cast<const double2*>(E)[g];
+  return {v.x, v.y, 0.0, 0.0};
+}
+// e = exp(-ds w/2) of species c at point p
+__device__ __forceinline__ void store_ept(float* E, size_t p, int c, double e) {
+  const float h = (float)e;
+  E[4 * p + c] = h;
+  E[4 * p + 2 + c] = (float)(e - (double)h);
+}
+__device__ __forceinline__ void store_ept(double* E, size_t p, int c, double e) { E[2 * p + c] = e; }
 
 template <typename T>
 __device__ __forceinline__ int chain_type_fwd(const BulkDev<T>& I, int t) { return t <= I.na ? 0 : 1; }
@@ -159,20 +179,15 @@ k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work
   const int line = threadIdx.x / P.tpl, lt = threadIdx.x % P.tpl;
   const bool active = line < nl;
 
-  const T* EA = I.E;
-  const T* EB = I.E + I.npts;
-  const T* LA = I.Elo ? I.Elo : I.E;             // residues (unused in FP64)
-  const T* LB = I.Elo ? I.Elo + I.npts : I.E + I.npts;
   if (mode == XM_INIT) {
     // slice 0 = (1, 1); z = (E_f(1), E_b(1)) -> forward
-    const bool fa = chain_type_fwd(I, 1) == 0, fb = chain_type_bwd(I, 1) == 0;
-    const T* ef = fa ? EA : EB;
-    const T* eb = fb ? EA : EB;
+    const bool fA = chain_type_fwd(I, 1) == 0, bA = chain_type_bwd(I, 1) == 0;
     cplx<T>* s0 = I.slices;
     for (int e = threadIdx.x; e < tot; e += blockDim.x) {
       const size_t g = base + e;
       s0[g] = mk<T>((T)1, (T)1);
-      b0[(e / N) * P.ld + (e % N)] = mk<T>(ef[g], eb[g]);
+      const EPt<T> ev = load_ept(I.E, g);
+      b0[(e / N) * P.ld + (e % N)] = mk<T>(fA ? ev.a : ev.b, bA ? ev.a : ev.b);
     }
     __syncthreads();
     cplx<T>* r = fft_lines<T>(b0, b1, tw, P, line, lt, active, +1);
@@ -212,34 +227,22 @@ k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work
     }
     return;
   }
-  // contour node t of both chains
-  const bool ta = chain_type_fwd(I, t) == 0, tb = chain_type_bwd(I, t) == 0;
-  const T* ef = ta ? EA : EB;
-  const T* eb = tb ? EA : EB;
-  const T* lf = ta ? LA : LB;
-  const T* lb = tb ? LA : LB;
+  // contour node t of both chains (A or B factor per chain and step)
+  const bool fA = chain_type_fwd(I, t) == 0, bA = chain_type_bwd(I, t) == 0;
   const bool more = t < I.ns;
-  const bool ta2 = chain_type_fwd(I, t + 1) == 0, tb2 = chain_type_bwd(I, t + 1) == 0;
-  const T* ef2 = ta2 ? EA : EB;
-  const T* eb2 = tb2 ? EA : EB;
-  const T* lf2 = ta2 ? LA : LB;
-  const T* lb2 = tb2 ? LA : LB;
+  const bool fA2 = chain_type_fwd(I, t + 1) == 0, bA2 = chain_type_bwd(I, t + 1) == 0;
   cplx<T>* sl = I.slices + (size_t)t * I.npts;
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     const size_t g = base + e;
     const int si = (e / N) * P.ld + (e % N);
     const cplx<T> z = r[si];
-    const T fa = ef[g], fb = eb[g];
-    const T la = lf[g], lbv = lb[g];
-    const cplx<T> q = mk<T>(emul(z.x, fa, la), emul(z.y, fb, lbv));
+    const EPt<T> ev = load_ept(I.E, g);
+    const cplx<T> q = mk<T>(emul(z.x, fA ? ev.a : ev.b, fA ? ev.al : ev.bl),
+                            emul(z.y, bA ? ev.a : ev.b, bA ? ev.al : ev.bl));
     sl[g] = q;
-    if (more) {
-      const T ga = (ef2 == ef) ? fa : ef2[g];
-      const T gb = (eb2 == eb) ? fb : eb2[g];
-      const T ha = (ef2 == ef) ? la : lf2[g];
-      const T hb = (eb2 == eb) ? lbv : lb2[g];
-      o[si] = mk<T>(emul(q.x, ga, ha), emul(q.y, gb, hb));
-    }
+    if (more)
+      o[si] = mk<T>(emul(q.x, fA2 ? ev.a : ev.b, fA2 ? ev.al : ev.bl),
+                    emul(q.y, bA2 ? ev.a : ev.b, bA2 ? ev.al : ev.bl));
   }
   if (!more) return;
   __syncthreads();
@@ -439,15 +442,12 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts, double ds) {
 }
 
 // E = exp(-0.5 ds w) for both species (Calculate_Expfield, mod_propagate.f90:28)
-// (Elo: FP32 residue E - (float)E, or null)
+// w [2][npts] -> interleaved factors (see EPt)
 template <typename T>
-__global__ void k_expfield(const double* __restrict__ w, T* __restrict__ E, T* __restrict__ Elo,
-                           size_t n, double ds) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const double e = exp_boltzmann(-0.5 * ds * w[i]);
-    const T h = (T)e;
-    E[i] = h;
-    if (Elo) Elo[i] = (T)(e - (double)h);
+__global__ void k_expfield(const double* __restrict__ w, T* __restrict__ E, size_t npts, double ds) {
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npts; p += (size_t)gridDim.x * blockDim.x) {
+    store_ept(E, p, 0, exp_boltzmann(-0.5 * ds * w[p]));
+    store_ept(E, p, 1, exp_boltzmann(-0.5 * ds * w[npts + p]));
   }
 }
 

@@ -63,21 +63,17 @@ k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
   cplx<T>* sc = scr + line * F::LS;
   const size_t base = (size_t)row * N;
   cplx<T>* spec = I.spec;
-  const T* EA = I.E;
-  const T* EB = I.E + npts;
-  const T* LA = I.Elo ? I.Elo : I.E;
-  const T* LB = I.Elo ? I.Elo + npts : I.E + npts;
   cplx<T> v[R1];
 
   if (mode == XM_INIT || mode == XM_R2S) {
     if (mode == XM_INIT) {
-      const T* ef = (1 <= I.na) ? EA : EB;
-      const T* eb = (1 <= I.nb) ? EB : EA;
+      const bool fA = 1 <= I.na, bA = 1 > I.nb;
       cplx<T>* s0 = I.slices;
 #pragma unroll
       for (int m = 0; m < R1; ++m) {
         const size_t g = base + F::in_index(lt, m);
-        v[m] = mk<T>(ef[g], eb[g]);
+        const EPt<T> ev = load_ept(I.E, g);
+        v[m] = mk<T>(fA ? ev.a : ev.b, bA ? ev.a : ev.b);
         if (valid) s0[g] = mk<T>((T)1, (T)1);
       }
     } else {
@@ -116,31 +112,21 @@ k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
     }
     return;
   }
-  const bool ta = t <= I.na, tb = t <= I.nb;
-  const T* ef = ta ? EA : EB;
-  const T* eb = tb ? EB : EA;
-  const T* lf = ta ? LA : LB;
-  const T* lb = tb ? LB : LA;
+  // A or B factor per chain and step (forward A then B, backward B then A)
+  const bool fA = t <= I.na, bA = t > I.nb;
   const bool more = t < ns;
-  const bool ta2 = (t + 1) <= I.na, tb2 = (t + 1) <= I.nb;
-  const T* ef2 = ta2 ? EA : EB;
-  const T* eb2 = tb2 ? EB : EA;
-  const T* lf2 = ta2 ? LA : LB;
-  const T* lb2 = tb2 ? LB : LA;
+  const bool fA2 = (t + 1) <= I.na, bA2 = (t + 1) > I.nb;
   cplx<T>* sl = I.slices + (size_t)t * npts;
 #pragma unroll
   for (int m = 0; m < R1; ++m) {
     const size_t g = base + F::in_index(lt, m);
-    const T fa = ef[g], fb = eb[g], la = lf[g], lbv = lb[g];
-    const cplx<T> q = mk<T>(emul(v[m].x, fa, la), emul(v[m].y, fb, lbv));
+    const EPt<T> ev = load_ept(I.E, g);
+    const cplx<T> q = mk<T>(emul(v[m].x, fA ? ev.a : ev.b, fA ? ev.al : ev.bl),
+                            emul(v[m].y, bA ? ev.a : ev.b, bA ? ev.al : ev.bl));
     if (valid) sl[g] = q;
-    if (more) {
-      const T ga = (ef2 == ef) ? fa : ef2[g];
-      const T gb = (eb2 == eb) ? fb : eb2[g];
-      const T ha = (ef2 == ef) ? la : lf2[g];
-      const T hb = (eb2 == eb) ? lbv : lb2[g];
-      v[m] = mk<T>(emul(q.x, ga, ha), emul(q.y, gb, hb));
-    }
+    if (more)
+      v[m] = mk<T>(emul(q.x, fA2 ? ev.a : ev.b, fA2 ? ev.al : ev.bl),
+                   emul(q.y, bA2 ? ev.a : ev.b, bA2 ? ev.al : ev.bl));
   }
   if (!more) return;
   F::forward(v, sc, tw, lt);
@@ -381,21 +367,10 @@ k_rx_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restri
   const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
   cplx<T>* sc = scr + line * F::LS;
   cplx<T>* spec = I.spec;
-  const T* EA = I.E;
-  const T* EB = I.E + npts;
-  const T* LA = I.Elo ? I.Elo : I.E;
-  const T* LB = I.Elo ? I.Elo + npts : I.E + npts;
-  const bool ta = t <= I.na, tb = t <= I.nb;
-  const T* ef = ta ? EA : EB;
-  const T* eb = tb ? EB : EA;
-  const T* lf = ta ? LA : LB;
-  const T* lb = tb ? LB : LA;
+  // A or B factor per chain and step (forward A then B, backward B then A)
+  const bool fA = t <= I.na, bA = t > I.nb;
   const bool more = t < ns;
-  const bool ta2 = (t + 1) <= I.na, tb2 = (t + 1) <= I.nb;
-  const T* ef2 = ta2 ? EA : EB;
-  const T* eb2 = tb2 ? EB : EA;
-  const T* lf2 = ta2 ? LA : LB;
-  const T* lb2 = tb2 ? LB : LA;
+  const bool fA2 = (t + 1) <= I.na, bA2 = (t + 1) > I.nb;
   cplx<T>* sl = I.slices + (size_t)t * npts;
   cplx<T> nx[R1];
   int tile = blockIdx.x;
@@ -421,16 +396,13 @@ k_rx_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restri
 #pragma unroll
     for (int m = 0; m < R1; ++m) {
       const size_t g = base + F::in_index(lt, m);
-      const T fa = ef[g], fb = eb[g], la = lf[g], lbv = lb[g];
-      const cplx<T> q = mk<T>(emul(v[m].x, fa, la), emul(v[m].y, fb, lbv));
+      const EPt<T> ev = load_ept(I.E, g);
+      const cplx<T> q = mk<T>(emul(v[m].x, fA ? ev.a : ev.b, fA ? ev.al : ev.bl),
+                              emul(v[m].y, bA ? ev.a : ev.b, bA ? ev.al : ev.bl));
       if (valid) sl[g] = q;
-      if (more) {
-        const T ga = (ef2 == ef) ? fa : ef2[g];
-        const T gb = (eb2 == eb) ? fb : eb2[g];
-        const T ha = (ef2 == ef) ? la : lf2[g];
-        const T hb = (eb2 == eb) ? lbv : lb2[g];
-        v[m] = mk<T>(emul(q.x, ga, ha), emul(q.y, gb, hb));
-      }
+      if (more)
+        v[m] = mk<T>(emul(q.x, fA2 ? ev.a : ev.b, fA2 ? ev.al : ev.bl),
+                     emul(q.y, bA2 ? ev.a : ev.b, bA2 ? ev.al : ev.bl));
     }
     if (!more) continue;
     F::forward(v, sc, tw, lt);

@@ -1,0 +1,244 @@
+// bulk_tma.cuh -- TMA-fed strided passes (Y and Z) of the FP32 bulk propagator.
+//
+// The strided passes read and write lines that run across rows of the
+// spectrum; issued from the threads, every warp access touches eight rows and
+// the L1/LSU pipe becomes the limit.  Here the tiles move between global and
+// shared memory by TMA (cp.async.bulk.tensor), off the LSU pipe:
+//   - a tile is LPC = 32 consecutive x-lines x N points, fetched as two
+//     16-line boxes {16, N, 1} (Y) or {16, 1, N} (Z) of 8-byte complex values;
+//   - boxes land 128-byte swizzled: the 16-byte chunk index of row j is XORed
+//     with j mod 8, so the eight lanes of one line (rows t + 8m) hit eight
+//     different chunks -- conflict-free column reads;
+//   - persistent CTAs run a two-stage pipeline: thread 0 prefetches tile i+1
+//     (mbarrier with transaction bytes) while the CTA transforms tile i in
+//     registers (RegFFT), writes it back in place and TMA-stores it;
+//   - every mbarrier wait is bounded; on expiry the CTA sets an error flag,
+//     drains its bulk copies and returns (no hang).
+#pragma once
+#include <cuda.h>
+
+#include "bulk_reg.cuh"
+
+namespace tmak {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false when the phase did not complete within `limit` polls
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int limit) {
+  for (int i = 0; i < limit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x,
+                                            int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* src, int x, int y,
+                                             int z) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(map),
+               "r"(x), "r"(y), "r"(z), "r"(smem_u32(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// element offset of (row j, column c) in a 16-column box with 128-byte swizzle
+__device__ __forceinline__ int swz(int j, int c) {
+  return j * 16 + ((((c >> 1) ^ (j & 7)) << 1) | (c & 1));
+}
+
+constexpr int kBoxCols = 16;           // 16 x 8 B = 128 B inner box
+constexpr int kWaitPolls = 1 << 22;    // bound of one mbarrier wait
+
+template <int N>
+struct TmaLayout {
+  using F = RegFFT<float, regk::Cfg<N>::R1, regk::Cfg<N>::TPL>;
+  static constexpr int LPC = BULK_THREADS / F::TPL;     // lines per tile
+  static constexpr int NB = LPC / kBoxCols;             // boxes per tile
+  static constexpr int box_elems = N * kBoxCols;
+  static constexpr int tile_elems = NB * box_elems;
+  static constexpr uint32_t tile_bytes = tile_elems * 8;
+  // [buf0 | buf1] (1024-aligned) | twiddles N | z factors 2N | exchange | dc 3N | 2 barriers
+  static constexpr size_t buf_off = 0;
+  static constexpr size_t tw_off = 2 * (size_t)tile_bytes;
+  static constexpr size_t gz_off = tw_off + N * sizeof(float2);
+  static constexpr size_t ex_off = ((gz_off + 2 * N * sizeof(float) + 15) / 16) * 16;
+  static constexpr size_t dc_off = ex_off + (size_t)LPC * F::LS * sizeof(float2);
+  static constexpr size_t bar_off = ((dc_off + 3 * N * sizeof(float2) + 15) / 16) * 16;
+  static constexpr size_t bytes = bar_off + 2 * sizeof(uint64_t) + 1024;  // + alignment slack
+  static_assert(LPC % kBoxCols == 0, "tile must be whole boxes");
+};
+
+}  // namespace tmak
+
+// KIND 0: forward y, 1: inverse y, 2: z (forward, exp(-ds k^2)/N, inverse).
+// One instance, gx a multiple of 32, every line length N.
+template <int N, int KIND>
+__global__ void __launch_bounds__(BULK_THREADS, 2)
+k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUtensorMap tmap,
+         int ntiles, const float2* __restrict__ gtw, const float* __restrict__ fk,
+         const double* __restrict__ g64, int t, int* __restrict__ err) {
+  using LY = tmak::TmaLayout<N>;
+  using F = typename LY::F;
+  constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
+  constexpr bool zdir = KIND == 2;
+  constexpr bool in_dout = KIND == 1;
+  constexpr bool out_dout = KIND == 0;
+  extern __shared__ __align__(1024) unsigned char smraw_[];
+  // 1024-byte alignment of the swizzled boxes
+  unsigned char* smraw = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smraw_) + 1023) & ~uintptr_t(1023));
+  float2* buf = reinterpret_cast<float2*>(smraw + LY::buf_off);
+  float2* tw = reinterpret_cast<float2*>(smraw + LY::tw_off);
+  float* gzs = reinterpret_cast<float*>(smraw + LY::gz_off);
+  float2* ex = reinterpret_cast<float2*>(smraw + LY::ex_off);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw + LY::bar_off);
+  const BulkDev<float>& I = insts[0];
+  if (t > I.ns) return;
+  const int gx = I.gx, gy = I.gy;
+  const int lgx = regk::ilog2(gx);
+  const int tw_off = zdir ? I.pz.tw_off : I.py.tw_off;
+  if (threadIdx.x == 0) {
+    tmak::mbar_init(&bar[0], 1);
+    tmak::mbar_init(&bar[1], 1);
+    tmak::fence_mbar_init();
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
+  if constexpr (KIND == 2) {
+    const float* gzt = fk + I.gz_off;
+    for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) gzs[i] = gzt[i];
+  }
+  const size_t es = zdir ? (size_t)gx * gy : (size_t)gx;
+  float2* spec = I.spec;
+  // (0, 0) pencil in float-float (CTA 0 handles tile 0 first)
+  const bool dcblk = zdir && blockIdx.x == 0;
+  float2* dcf = reinterpret_cast<float2*>(smraw + LY::dc_off);
+  const DcPencil dcp{dcf, dcf + N, dcf + 2 * N};
+  __syncthreads();
+  if (dcblk) {
+    dc_pencil_load<float>(spec, es, N, g64 + I.g64_off, dcp);
+    __syncthreads();
+    dc_pencil_apply(N, dcp);
+  }
+  auto coords = [&](int tile, int b, int& cx, int& cy, int& cz) {
+    const int L0 = tile * LPC;
+    const int o = L0 >> lgx, x0 = (L0 & (gx - 1)) + b * tmak::kBoxCols;
+    cx = x0;
+    if (zdir) { cy = o; cz = 0; } else { cy = 0; cz = o; }
+  };
+  auto issue_load = [&](int tile, int s) {
+    tmak::mbar_expect_tx(&bar[s], LY::tile_bytes);
+    for (int b = 0; b < LY::NB; ++b) {
+      int cx, cy, cz;
+      coords(tile, b, cx, cy, cz);
+      tmak::tma_load_3d(buf + (size_t)s * LY::tile_elems + b * LY::box_elems, &tmap, &bar[s], cx, cy, cz);
+    }
+  };
+  // loads issued / completed per stage (thread 0), to drain on an early exit
+  int issued[2] = {0, 0}, done[2] = {0, 0};
+  if (threadIdx.x == 0 && blockIdx.x < ntiles) { issue_load(blockIdx.x, 0); issued[0] = 1; }
+  const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
+  const int box = line / tmak::kBoxCols, col = line % tmak::kBoxCols;
+  float2* sc = ex + line * F::LS;
+  const float* gxy = fk + I.gxy_off;
+  int it = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int s = it & 1;
+    const int nxt = tile + gridDim.x;
+    if (threadIdx.x == 0 && nxt < ntiles) {
+      tmak::bulk_wait_read0();  // the store of the tile last held in stage s^1 has read it
+      issue_load(nxt, s ^ 1);
+      ++issued[s ^ 1];
+    }
+    const bool got = tmak::mbar_wait_bounded(&bar[s], (it >> 1) & 1, tmak::kWaitPolls);
+    if (!__syncthreads_and(got)) {
+      if (threadIdx.x == 0) atomicOr(err, 2);
+      break;
+    }
+    ++done[s];
+    float2* tb = buf + (size_t)s * LY::tile_elems + box * LY::box_elems;
+    float2 v[R1];
+#pragma unroll
+    for (int r = 0; r < R1; ++r) {
+      const int j = in_dout ? F::out_index(lt, r) : F::in_index(lt, r);
+      v[r] = tb[tmak::swz(j, col)];
+    }
+    if constexpr (KIND == 1) {
+      F::inverse(v, sc, tw, lt);
+    } else if constexpr (KIND == 0) {
+      F::forward(v, sc, tw, lt);
+    } else {
+      F::forward(v, sc, tw, lt);
+      const int L = tile * LPC + line;
+      const float ah = gxy[L], al = gxy[gx * gy + L];
+#pragma unroll
+      for (int r = 0; r < R1; ++r) {
+        const int kz = F::out_index(lt, r);
+        const float bh = gzs[kz], bl = gzs[N + kz];
+        const float gh = ah * bh;
+        const float gl = fmaf(ah, bh, -gh) + fmaf(ah, bl, al * bh);
+        v[r] = make_float2(fmaf(v[r].x, gh, v[r].x * gl), fmaf(v[r].y, gh, v[r].y * gl));
+      }
+      F::inverse(v, sc, tw, lt);
+    }
+#pragma unroll
+    for (int r = 0; r < R1; ++r) {
+      const int j = out_dout ? F::out_index(lt, r) : F::in_index(lt, r);
+      tb[tmak::swz(j, col)] = v[r];
+    }
+    if (dcblk && tile == 0) {
+      __syncthreads();
+      float2* t0 = buf + (size_t)s * LY::tile_elems;  // line 0 = box 0, column 0
+      for (int j = threadIdx.x; j < N; j += blockDim.x) t0[tmak::swz(j, 0)] = dcp.out[j];
+    }
+    tmak::fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int b = 0; b < LY::NB; ++b) {
+        int cx, cy, cz;
+        coords(tile, b, cx, cy, cz);
+        tmak::tma_store_3d(&tmap, buf + (size_t)s * LY::tile_elems + b * LY::box_elems, cx, cy, cz);
+      }
+      tmak::bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) {
+    // loads still in flight after an early exit land before shared memory is released
+    for (int st = 0; st < 2; ++st)
+      for (int k = done[st]; k < issued[st]; ++k)
+        tmak::mbar_wait_bounded(&bar[st], k & 1, tmak::kWaitPolls);
+    tmak::bulk_wait0();
+  }
+}

@@ -78,6 +78,15 @@ int read_result(adscf_ctx* ctx, adscf_iter_result* out, adscf_chain_result* ch) 
     ch->rho = r[R_RHO];
     ch->energy = r[R_ENERGY];
   }
+  if (ctx->d_flags) {  // a bounded device wait expired (TMA passes)
+    int f = 0;
+    CK(cudaMemcpyAsync(&f, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (f) {
+      CK(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), ctx->stream));
+      return set_err(ctx, ADSCF_E_TIMEOUT, "a bounded wait for a TMA tile expired");
+    }
+  }
   if (r[R_STATUS] != 0.0) return set_err(ctx, ADSCF_E_NONFINITE, "non-finite or non-positive Q / accuracy");
   return ADSCF_OK;
 }
@@ -98,7 +107,7 @@ int enqueue_iteration(adscf_ctx* ctx) {
   k_solve<<<1, 64, 0, ctx->stream>>>(ctx->S, 1, 1);
   CK(cudaGetLastError());
   if (ctx->geometry == ADSCF_BULK) return bulk_mix_e(ctx);
-  k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, nullptr, nullptr, 0.0);
+  k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, nullptr, 0.0);
   CK(cudaGetLastError());
   return ADSCF_OK;
 }
@@ -196,6 +205,7 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
   // arithmetic): the generic mixed-radix FFT, and the non-persistent passes
   ctx->use_generic = std::getenv("ADSCF_GENERIC_FFT") != nullptr;
   ctx->no_persistent = std::getenv("ADSCF_NO_PERSISTENT") != nullptr;
+  ctx->no_tma = std::getenv("ADSCF_NO_TMA") != nullptr;
   ctx->gx = p->gx; ctx->gy = p->gy; ctx->gz = p->gz;
   ctx->nplanes = p->geometry == ADSCF_BULK ? p->gz : p->gz + 1;
   ctx->npts = p->gx * p->gy * ctx->nplanes;
@@ -466,7 +476,7 @@ int adscf_mix_dev(adscf_ctx* ctx, double* d_field, const double* d_dfield, int i
   S2.wall_mask = 0;  // the caller packs what is mixed (Mix_Fields)
   k_mixdots<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2);
   k_solve<<<1, 64, 0, ctx->stream>>>(S2, 0, 1);
-  k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, nullptr, nullptr, 0.0);
+  k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, nullptr, 0.0);
   CK(cudaGetLastError());
   const int nxt = (iter + 1) % ctx->hist_slots;
   CK(cudaMemcpyAsync(d_field, hx_slot(ctx, nxt), nv * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -615,7 +625,7 @@ int adscf_enqueue(adscf_ctx* ctx, int stage, int repeats) {
       k_solve<<<1, 64, 0, ctx->stream>>>(ctx->S, 1, 1);
       CK(cudaGetLastError());
       rc = ctx->geometry == ADSCF_BULK ? bulk_mix_e(ctx)
-           : (k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, nullptr, nullptr, 0.0),
+           : (k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, nullptr, 0.0),
               cudaGetLastError() == cudaSuccess ? ADSCF_OK : ADSCF_E_CUDA);
     } else {
       return set_err(ctx, ADSCF_E_ARG, "unknown stage");

@@ -1,5 +1,6 @@
 // internal.h -- host-side context of the SCF library (not part of the ABI).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <string>
 #include <vector>
@@ -42,6 +43,12 @@ struct adscf_ctx {
   int use_generic = 0;                // force the generic mixed-radix kernels
   int no_persistent = 0;              // disable the persistent pipelined passes
   int pgrid_x = 0, pgrid_y = 0, pgrid_z = 0;  // persistent grid sizes (0: not used)
+  // TMA-fed strided passes (FP32, one line length on all axes)
+  int tma = 0, no_tma = 0;
+  CUtensorMap tmap_y{}, tmap_z{};
+  int tma_tiles_y = 0, tma_tiles_z = 0, tma_grid = 0;
+  size_t tma_smem = 0;
+  int* d_flags = nullptr;             // device error flags (bounded-wait expiry)
   int contour_blocks = 0;
 
   // ---- SCF state (FP64)

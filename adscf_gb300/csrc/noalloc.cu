@@ -149,7 +149,6 @@ int build_tables(DevState& D, int gx, int gy, int gz, double lx, double ly, doub
   I.spec = reinterpret_cast<double2*>(D.base + kOffSpec);
   I.slices = nullptr;
   I.E = nullptr;
-  I.Elo = nullptr;
   const int nwx = (gy * gz + I.px.lpc - 1) / I.px.lpc;
   const int nwy = (gx * gz + I.py.lpc - 1) / I.py.lpc;
   const int nwz = (gx * gy + I.pz.lpc - 1) / I.pz.lpc;

@@ -382,7 +382,7 @@ __global__ void k_solve(ScfDev S, int have_closure, int do_mix) {
 // E = exp(-ds x/2) for the pseudo-spectral propagator.
 template <typename T>
 __global__ void __launch_bounds__(SCF_THREADS)
-k_mix(ScfDev S, T* E, T* Elo, double ds) {
+k_mix(ScfDev S, T* E, double ds) {
   __shared__ double ca[SCF_MAX_SLOTS], cb[SCF_MAX_SLOTS];
   const int kn = *S.iter;               // already advanced to k+1
   const int nxt = kn % S.slots;
@@ -407,11 +407,9 @@ k_mix(ScfDev S, T* E, T* Elo, double ds) {
       }
     }
     S.hx[(size_t)nxt * nv + i] = x;
-    if (E) {
-      const double e = exp_boltzmann(-0.5 * ds * x);
-      const T h = (T)e;
-      E[i] = h;
-      if (Elo) Elo[i] = (T)(e - (double)h);
+    if (E) {  // interleaved Boltzmann factors of the next propagation (two species)
+      const int c = i >= (size_t)S.npts;
+      store_ept(E, i - (size_t)c * S.npts, c, exp_boltzmann(-0.5 * ds * x));
     }
   }
 }

@@ -41,6 +41,9 @@ KAPPA = 25.0
 M_HIST = 10
 LAM = 0.1
 SEED = 3
+# DRAM bytes of one 128^3 FP32 double step (Yf, Z, Yi, X launches), measured with
+# ncu on GB300: 17.53 MB, against 50.3 MB of algorithmic bytes (24 B per point)
+DSTEP_TRAFFIC = 17_531_648
 
 
 def c3_fields(n=GRID, length=L, seed=SEED):
@@ -376,7 +379,11 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "propagator double step (Yf, Z, Yi, X passes)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_kind": peak_kind,
-                     "algorithmic_bytes": alg_dstep, "traffic": None,
+                     "algorithmic_bytes": alg_dstep, "traffic": DSTEP_TRAFFIC,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum summed "
+                                       "over the four passes of one 128^3 double step "
+                                       "(--cache-control none; Boltzmann factors and spectrum "
+                                       "stay in L2, only the slice store reaches DRAM)",
                      "contour_GBs": alg_contour / (t_cont * 1e-3) / 1e9},
         "clocks": clk,
         "gpu_launches": launches_per_step * args.steps,

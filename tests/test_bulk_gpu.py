@@ -199,3 +199,29 @@ def test_bad_arguments_return_status():
         Context(BULK, grid=(7, 8, 8))     # 7 is not a product of 2, 3, 5
     with pytest.raises(AdscfError):
         Context(BULK, grid=(8, 8, 8), mixing_type=3, mixing_dim=40)
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_tma_passes_match_register_passes(n, rng, monkeypatch):
+    """The TMA-fed Y/Z passes move data differently but compute the same
+    arithmetic as the register passes: results must be bitwise identical."""
+    grid, size, ds = (n, n, n), (3.8, 3.8, 3.8), 0.05
+    field = 0.5 * rng.standard_normal((2, n, n, n))
+    monkeypatch.delenv("ADSCF_NO_TMA", raising=False)
+    with mkctx(grid, size, ds, SPLIT, f=(0.4, 0.6)) as c:
+        d1, r1 = c.propagate_diblock(field)
+    monkeypatch.setenv("ADSCF_NO_TMA", "1")
+    with mkctx(grid, size, ds, SPLIT, f=(0.4, 0.6)) as c:
+        d2, r2 = c.propagate_diblock(field)
+    assert r1.Qsum == r2.Qsum
+    assert np.array_equal(d1, d2)
+
+
+def test_split_64cube_against_oracle(rng):
+    grid, size, ds = (64, 64, 64), (3.8, 3.8, 3.8), 0.05
+    field = 2.0 * rng.standard_normal((2, 64, 64, 64))
+    ref = ob.propagate_diblock(field, grid, size, ds, (0.4, 0.6))
+    with mkctx(grid, size, ds, SPLIT, f=(0.4, 0.6)) as c:
+        dens, res = c.propagate_diblock(field)
+    assert abs(np.log(res.Qsum) - np.log(ref["Qsum"])) < 1e-6
+    assert np.max(np.abs(dens - ob.density_by_type(ref["density"]))) < 1e-5
