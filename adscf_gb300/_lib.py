@@ -100,6 +100,8 @@ SIGNATURES = {
     "adscf_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "adscf_enqueue": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "adscf_stage_launches": (C.c_int, [C.c_void_p, C.c_int]),
+    "adscf_forward": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "adscf_backward": (C.c_int, [C.c_void_p, _dp]),
     "adscf_propagate_step_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                                C.c_double, C.c_double, C.c_void_p, C.c_void_p,
                                                C.c_void_p]),

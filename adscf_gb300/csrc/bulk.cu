@@ -340,8 +340,14 @@ int create_t(adscf_ctx* ctx) {
                           : plan_smem<T>(I.pz) + 16 + (((I.pz.n + 1) & ~1) + 2 * (size_t)I.pz.ld) * sizeof(double2);
   size_t mx = std::max(ctx->smem_x, std::max(ctx->smem_y, ctx->smem_z));
   if (mx > 227 * 1024) return set_err(ctx, ADSCF_E_ARG, "grid line too long for shared memory");
-  CK(cudaFuncSetAttribute(k_bulk_xpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
-  CK(cudaFuncSetAttribute(k_bulk_strided<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
+  // the limit is a per-function setting shared by every context: raise it to
+  // the device maximum so a later, smaller context cannot lower it below what
+  // an earlier one launches with
+  int optin = 0;
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
+  if (mx > (size_t)optin) return set_err(ctx, ADSCF_E_ARG, "grid line too long for shared memory");
+  CK(cudaFuncSetAttribute(k_bulk_xpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  CK(cudaFuncSetAttribute(k_bulk_strided<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
   if ((rc = set_reg_attrs<T>(ctx))) return rc;
   // the persistent passes need one register length on all three axes
   if (ctx->regx && ctx->regx == ctx->regy && ctx->regx == ctx->regz && !ctx->no_persistent) {

@@ -314,6 +314,7 @@ int adscf_ctx_destroy(adscf_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->g_iter) cudaGraphExecDestroy(ctx->g_iter);
   if (ctx->g_prop) cudaGraphExecDestroy(ctx->g_prop);
+  adj_destroy(ctx);
   if (ctx->geometry == ADSCF_BULK) bulk_destroy(ctx);
   else film_destroy(ctx);
   cudaFree(ctx->d_dist); cudaFree(ctx->d_dens); cudaFree(ctx->d_tmp);
@@ -330,6 +331,7 @@ int adscf_ctx_destroy(adscf_ctx* ctx) {
 int adscf_propagate_diblock_dev(adscf_ctx* ctx, const double* d_field, double* d_density,
                                 adscf_chain_result* out) {
   if (!ctx || !d_field || !d_density) return ADSCF_E_ARG;
+  ++ctx->prop_gen;
   if (ctx->geometry == ADSCF_BRUSH) return set_err(ctx, ADSCF_E_STATE, "brush context: use adscf_propagate_homopolymer");
   int rc;
   if (ctx->geometry == ADSCF_BULK) {
@@ -363,6 +365,7 @@ int adscf_propagate_diblock(adscf_ctx* ctx, const double* field, double* density
 int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* density,
                                 adscf_chain_result* out) {
   if (!ctx || !field || !density) return ADSCF_E_ARG;
+  ++ctx->prop_gen;
   if (ctx->geometry != ADSCF_BRUSH) return set_err(ctx, ADSCF_E_STATE, "not a brush context");
   const size_t nv = nvar(ctx);
   double* d_w = ctx->d_tmp;
@@ -382,6 +385,7 @@ int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* den
 
 int adscf_propagate_step(adscf_ctx* ctx, double* prop, const double* aux, double ds) {
   if (!ctx || !prop || !aux) return ADSCF_E_ARG;
+  ++ctx->prop_gen;
   const size_t n = ctx->npts;
   double* d_p = ctx->d_tmp;
   double* d_a = ctx->d_tmp + n;
@@ -396,6 +400,7 @@ int adscf_propagate_step(adscf_ctx* ctx, double* prop, const double* aux, double
 
 int adscf_real2fourier(adscf_ctx* ctx, const double* prop, double* spectrum) {
   if (!ctx || !prop || !spectrum) return ADSCF_E_ARG;
+  ++ctx->prop_gen;
   if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "bulk only");
   // the spectrum staging uses d_tmp (2*npts doubles); stage the input in d_dist
   int rc = h2d(ctx, ctx->d_dist, prop, ctx->npts);
@@ -405,6 +410,7 @@ int adscf_real2fourier(adscf_ctx* ctx, const double* prop, double* spectrum) {
 
 int adscf_fourier2real(adscf_ctx* ctx, const double* spectrum, double* prop) {
   if (!ctx || !prop || !spectrum) return ADSCF_E_ARG;
+  ++ctx->prop_gen;
   if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "bulk only");
   int rc = bulk_c2r(ctx, spectrum, ctx->d_dist);
   if (rc) return rc;
@@ -540,6 +546,7 @@ int adscf_get_density(adscf_ctx* ctx, double* density) {
 
 int adscf_scf_run(adscf_ctx* ctx, int n_iter, double tol, adscf_iter_result* out) {
   if (!ctx || n_iter < 0) return ADSCF_E_ARG;
+  ++ctx->prop_gen;
   int rc = build_iteration_graph(ctx);
   if (rc) return rc;
   for (int i = 0; i < n_iter; ++i) {
@@ -560,6 +567,7 @@ int adscf_scf_run(adscf_ctx* ctx, int n_iter, double tol, adscf_iter_result* out
 
 int adscf_scf_iteration(adscf_ctx* ctx, double* field, double* density, adscf_iter_result* out) {
   if (!ctx || !field || !density) return ADSCF_E_ARG;
+  ++ctx->prop_gen;
   int rc = build_iteration_graph(ctx);
   if (rc) return rc;
   int k = 1;
@@ -607,6 +615,7 @@ int adscf_stage_launches(const adscf_ctx* ctx, int stage) {
 
 int adscf_enqueue(adscf_ctx* ctx, int stage, int repeats) {
   if (!ctx || repeats < 0) return ADSCF_E_ARG;
+  ++ctx->prop_gen;
   int rc;
   if (stage == ADSCF_STAGE_ITERATION) {
     if ((rc = build_iteration_graph(ctx))) return rc;

@@ -10,6 +10,7 @@
 #include "scf_kernels.cuh"
 
 struct FilmState;  // film / brush device state (film.cu)
+struct AdjState;   // adjoint buffers and work lists (adjoint.cu)
 
 struct adscf_ctx {
   adscf_params p{};
@@ -77,6 +78,11 @@ struct adscf_ctx {
   cudaGraphExec_t g_prop = nullptr;
 
   FilmState* film = nullptr;
+
+  // adjoint (adjoint.cu): state of the last adscf_forward, and a counter that
+  // every propagating entry point advances so a stale forward is detected
+  AdjState* adj = nullptr;
+  long long prop_gen = 0;
 };
 
 // errors
@@ -99,6 +105,8 @@ int bulk_step_single(adscf_ctx* ctx, double* d_prop, const double* d_e);
 int bulk_r2c(adscf_ctx* ctx, const double* d_prop, double* h_half);
 int bulk_c2r(adscf_ctx* ctx, const double* h_half, double* d_prop);
 int bulk_mix_e(adscf_ctx* ctx);                 // k_mix with E update
+// adjoint (adjoint.cu)
+void adj_destroy(adscf_ctx* ctx);
 // films (film.cu)
 int film_create(adscf_ctx* ctx, const adscf_params* p);
 int film_check_pivot(adscf_ctx* ctx);

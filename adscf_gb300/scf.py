@@ -196,6 +196,22 @@ class Context:
         self._ck(self.lib.adscf_scf_run(self.h, int(n_iter), float(tol), C.byref(res)))
         return res
 
+    # -- differentiation (FP64 bulk) ----------------------------------------
+    def forward(self, field):
+        """Free energy per chain at `field` [2][npts], no mixing; keeps the
+        propagator slices for ``backward``."""
+        w = _f64(field, 2 * self.npts)
+        out = C.c_double()
+        self._ck(self.lib.adscf_forward(self.h, L.dptr(w), C.byref(out)))
+        return out.value
+
+    def backward(self):
+        """(dF/dL_x, dF/dL_y, dF/dL_z, dF/dchi) at the fields of the last
+        ``forward`` (reverse-mode adjoint of the discrete chain)."""
+        g = np.empty(4)
+        self._ck(self.lib.adscf_backward(self.h, L.dptr(g)))
+        return g
+
     def scf_iteration(self, field, density_out=None):
         x = _f64(field).copy()
         d = np.empty_like(x) if density_out is None else density_out

@@ -215,6 +215,24 @@ ADSCF_API int adscf_enqueue(adscf_ctx *ctx, int stage, int repeats);
 /* kernel launches one run of a stage makes (for launch accounting) */
 ADSCF_API int adscf_stage_launches(const adscf_ctx *ctx, int stage);
 
+/* ---- differentiation (bulk, FP64 context, canonical ensemble) ----------
+ * No counterpart in the reference, which has no derivatives; it replaces
+ * the reference's practice of differencing converged free energies of
+ * neighbouring box sizes (main_diblock.f90's Calculate_Energy, re-run).
+ * adscf_forward: free energy per chain at the host fields [2][gz][gy][gx]
+ * without mixing -- chain term log(rho V/Q) - 1 minus dvol sum(phi w) plus
+ * Interaction_Energy (mod_FloryHuggins.f90:74-96), over rho V, with phi
+ * from Propagate_Diblock (mod_diblock.f90:100-173) -- keeping every
+ * propagator slice on the device.
+ * adscf_backward: reverse-mode adjoint of that discrete free energy at the
+ * same fields: grad[0..2] = dF/dL_x, dF/dL_y, dF/dL_z (cell stress),
+ * grad[3] = dF/dchi.  Exact for the discretisation (pseudo-spectral steps,
+ * trapezoid contour), so at a converged saddle point grad[0..2] are the
+ * derivatives of the equilibrium free energy.  Any other propagating call
+ * on the context between the two returns ADSCF_E_STATE.                  */
+ADSCF_API int adscf_forward(adscf_ctx *ctx, const double *field, double *free_energy);
+ADSCF_API int adscf_backward(adscf_ctx *ctx, double *grad);
+
 /* ---- allocation-free propagator step ----------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (a pre-partitioned or quota-limited GPU, a driver that owns every
