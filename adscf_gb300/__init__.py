@@ -7,7 +7,7 @@ module procedures over that ABI.
 from . import _lib
 from ._lib import (BULK, FILM_1D, FILM_3D, BRUSH, FP64, SPLIT, MIX_SIMPLE,
                    MIX_LAMBDA, MIX_ANDERSON, AdscfError)
-from .scf import Context
+from .scf import Batch, Context, make_params
 
-__all__ = ["Context", "AdscfError", "BULK", "FILM_1D", "FILM_3D", "BRUSH",
+__all__ = ["Batch", "Context", "make_params", "AdscfError", "BULK", "FILM_1D", "FILM_3D", "BRUSH",
            "FP64", "SPLIT", "MIX_SIMPLE", "MIX_LAMBDA", "MIX_ANDERSON"]

@@ -102,6 +102,18 @@ SIGNATURES = {
     "adscf_stage_launches": (C.c_int, [C.c_void_p, C.c_int]),
     "adscf_forward": (C.c_int, [C.c_void_p, _dp, _dp]),
     "adscf_backward": (C.c_int, [C.c_void_p, _dp]),
+    "adscf_batch_create": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p)]),
+    "adscf_batch_destroy": (C.c_int, [C.c_void_p]),
+    "adscf_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "adscf_batch_offset": (C.c_longlong, [C.c_void_p, C.c_int]),
+    "adscf_batch_set_fields": (C.c_int, [C.c_void_p, _dp]),
+    "adscf_batch_get_fields": (C.c_int, [C.c_void_p, _dp]),
+    "adscf_batch_get_densities": (C.c_int, [C.c_void_p, _dp]),
+    "adscf_batch_scf_run": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(IterResult)]),
+    "adscf_batch_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "adscf_batch_enqueue": (C.c_int, [C.c_void_p, C.c_int]),
+    "adscf_batch_results": (C.c_int, [C.c_void_p, C.POINTER(IterResult)]),
+    "adscf_batch_launches": (C.c_int, [C.c_void_p]),
     "adscf_propagate_step_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                                C.c_double, C.c_double, C.c_void_p, C.c_void_p,
                                                C.c_void_p]),

@@ -6,44 +6,12 @@
 #include "internal.h"
 #include "bulk_reg.cuh"
 #include "bulk_tma.cuh"
+#include "bulk_host.h"
 
 namespace {
 
-int pow2_floor(int v) {
-  int p = 1;
-  while (p * 2 <= v) p *= 2;
-  return p;
-}
-
-bool make_plan(int n, Plan1D& P) {
-  std::memset(&P, 0, sizeof(P));
-  P.n = n;
-  int m = n;
-  while (m % 8 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 8; m /= 8; }
-  while (m % 4 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 4; m /= 4; }
-  while (m % 2 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 2; m /= 2; }
-  while (m % 3 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 3; m /= 3; }
-  while (m % 5 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 5; m /= 5; }
-  if (m != 1) return false;
-  int tpl = pow2_floor(n / 8 > 0 ? n / 8 : 1);
-  if (tpl > 64) tpl = 64;
-  P.tpl = tpl;
-  P.lpc = BULK_THREADS / tpl;
-  P.ld = n + 1;
-  return true;
-}
-
-// signed wave number of index i (mod_fourier.f90:178-186)
-double wavenum(int i, int n, double L) {
-  double m = (i > n / 2) ? double(i - n) : double(i);
-  return 2.0 * M_PI * m / L;
-}
-
-template <typename T>
-size_t plan_smem(const Plan1D& P) {
-  size_t twn = (P.n + 1) & ~1;
-  return (twn + 2 * (size_t)P.lpc * P.ld) * sizeof(cplx<T>);
-}
+using bulkhost::make_plan;
+using bulkhost::plan_smem;
 
 template <typename T>
 BulkDev<T>& hb(adscf_ctx* c);
@@ -220,71 +188,27 @@ int create_t(adscf_ctx* ctx) {
   I.gx = ctx->gx; I.gy = ctx->gy; I.gz = ctx->gz;
   I.npts = ctx->npts;
   I.ns = ctx->ns; I.na = ctx->na; I.nb = ctx->nb;
+  I.ds = ctx->p.ds;
   if (!make_plan(ctx->gx, I.px) || !make_plan(ctx->gy, I.py) || !make_plan(ctx->gz, I.pz))
     return set_err(ctx, ADSCF_E_ARG, "grid sizes must be products of 2, 3 and 5");
   // twiddle tables W_n^m = exp(-2 pi i m / n), computed in FP64
-  std::vector<int> ns = {ctx->gx, ctx->gy, ctx->gz};
   std::vector<cplx<T>> tw;
-  int offs[3];
-  for (int d = 0; d < 3; ++d) {
-    int found = -1;
-    for (int e = 0; e < d; ++e)
-      if (ns[e] == ns[d]) found = offs[e];
-    if (found >= 0) { offs[d] = found; continue; }
-    offs[d] = (int)tw.size();
-    for (int m = 0; m < ns[d]; ++m) {
-      const double a = -2.0 * M_PI * (double)m / (double)ns[d];
-      tw.push_back(mk<T>((T)std::cos(a), (T)std::sin(a)));
-    }
-  }
-  I.px.tw_off = offs[0]; I.py.tw_off = offs[1]; I.pz.tw_off = offs[2];
-  // diffusion factors exp(-ds k^2) (mod_fourier.f90:188): g_xy[y][x] and
-  // g_z[z]/N, each as T plus its rounding residue (hi, lo)
-  const double ds = ctx->p.ds;
-  const double invn = 1.0 / ((double)ctx->gx * ctx->gy * ctx->gz);
-  const int nxy = ctx->gx * ctx->gy;
-  std::vector<T> fk(2 * (size_t)nxy + 2 * (size_t)ctx->gz);
-  I.gxy_off = 0;
-  I.gz_off = 2 * nxy;
-  for (int y = 0; y < ctx->gy; ++y) {
-    const double ky = wavenum(y, ctx->gy, ctx->p.sizey);
-    for (int x = 0; x < ctx->gx; ++x) {
-      const double kx = wavenum(x, ctx->gx, ctx->p.sizex);
-      const double g = std::exp(-ds * kx * kx) * std::exp(-ds * ky * ky);
-      const T h = (T)g;
-      fk[(size_t)y * ctx->gx + x] = h;
-      fk[(size_t)nxy + y * ctx->gx + x] = (T)(g - (double)h);
-    }
-  }
-  std::vector<double> g64(ctx->gz);
+  std::vector<std::pair<int, int>> seen;
+  I.px.tw_off = bulkhost::twiddle_offset<T>(ctx->gx, tw, seen);
+  I.py.tw_off = bulkhost::twiddle_offset<T>(ctx->gy, tw, seen);
+  I.pz.tw_off = bulkhost::twiddle_offset<T>(ctx->gz, tw, seen);
+  // diffusion factors exp(-ds k^2) (mod_fourier.f90:188) and the (0,0)
+  // pencil's circulant kernel
+  std::vector<T> fk;
+  std::vector<double> g64;
+  bulkhost::append_tables<T>(ctx->gx, ctx->gy, ctx->gz, ctx->p.sizex, ctx->p.sizey, ctx->p.sizez,
+                             ctx->p.ds, fk, g64, I.gxy_off, I.gz_off, I.g64_off);
   std::vector<double2> tw64(ctx->gz);
   for (int z = 0; z < ctx->gz; ++z) {
-    const double kz = wavenum(z, ctx->gz, ctx->p.sizez);
-    const double g = std::exp(-ds * kz * kz) * invn;
-    const T h = (T)g;
-    fk[I.gz_off + z] = h;
-    fk[I.gz_off + ctx->gz + z] = (T)(g - (double)h);
-    g64[z] = g;
     const double a = -2.0 * M_PI * (double)z / (double)ctx->gz;
     tw64[z] = make_double2(std::cos(a), std::sin(a));
   }
-  // circular-convolution kernel of the (kx, ky) = (0, 0) pencil:
-  // c(d) = sum_kz G(kz) cos(2 pi kz d / gz), G(kz) = exp(-ds kz^2)/N (FP64;
-  // the phase index kz*d is reduced mod gz before the cosine)
-  {
-    std::vector<double> c(ctx->gz, 0.0);
-    for (int d = 0; d < ctx->gz; ++d) {
-      double s = 0.0;
-      for (int k = 0; k < ctx->gz; ++k) {
-        const long long m = ((long long)k * d) % ctx->gz;
-        s += g64[k] * std::cos(2.0 * M_PI * (double)m / (double)ctx->gz);
-      }
-      c[d] = s;
-    }
-    g64 = c;
-  }
   I.tw64_off = 0;
-  I.g64_off = 0;
   CK(cudaMalloc(&ctx->d_tw64, tw64.size() * sizeof(double2)));
   CK(cudaMemcpy(ctx->d_tw64, tw64.data(), tw64.size() * sizeof(double2), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&ctx->d_g64, g64.size() * sizeof(double)));
@@ -438,7 +362,7 @@ int chains_t(adscf_ctx* ctx) {
 template <typename T>
 int contour_t(adscf_ctx* ctx) {
   const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
-  k_bulk_contour<T><<<dim3(ctx->contour_blocks, 1), BULK_THREADS, 0, ctx->stream>>>(d, ctx->p.ds);
+  k_bulk_contour<T><<<dim3(ctx->contour_blocks, 1), BULK_THREADS, 0, ctx->stream>>>(d);
   CK(cudaGetLastError());
   return ADSCF_OK;
 }

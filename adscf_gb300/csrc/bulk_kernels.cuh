@@ -40,6 +40,7 @@ struct BulkDev {
   T* E;                      // [npts] interleaved exp(-ds w/2) (see EPt)
   double* dist;              // [2][npts] contour integrals (block A, block B)
   double* qpart;             // [gridDim] partial sums of q_N
+  double ds;                 // contour step
 };
 
 // X-pass modes
@@ -382,9 +383,10 @@ __device__ __forceinline__ void ff_add_prod(FF& a, float x, float y, float wgt) 
 
 template <typename T>
 __global__ void __launch_bounds__(BULK_THREADS)
-k_bulk_contour(const BulkDev<T>* __restrict__ insts, double ds) {
+k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
   __shared__ double red[32];
   const BulkDev<T> I = insts[blockIdx.y];
+  const double ds = I.ds;
   const int N = I.ns, NA = I.na;
   const cplx<T>* sl = I.slices;
   const size_t np = I.npts;

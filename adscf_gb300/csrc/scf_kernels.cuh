@@ -63,6 +63,8 @@ struct ScfDev {
   double* coef;              // [2][slots]
   int* iter;                 // 1-based iteration counter
   double* res;               // [R_COUNT]
+  void* mixE;                // batched mixing: this instance's Boltzmann factors (T*)
+  double mixds;              //   and contour step
 };
 
 __device__ __forceinline__ double q_total(const ScfDev& S) {
@@ -78,17 +80,21 @@ __device__ __forceinline__ double density_scale(const ScfDev& S, double Q) {
 // flags for k_closure
 enum { CL_MEANFIELD = 1, CL_MIXDOTS = 2, CL_KEEP_OLD = 4 };
 
-// Non-template kernels are defined once, in scf.cu.
+// Non-template kernels are defined once, in scf.cu.  The `_b` forms run a
+// batch of independent instances: instance blockIdx.y (closure, mix) or
+// blockIdx.x (solve) of the ScfDev array, with per-instance partials.
 __global__ void k_closure(ScfDev S, int flags);
+__global__ void k_closure_b(const ScfDev* __restrict__ Ss, int flags);
 __global__ void k_mixdots(ScfDev S);
 __global__ void k_solve(ScfDev S, int have_closure, int do_mix);
+__global__ void k_solve_b(const ScfDev* __restrict__ Ss, int have_closure, int do_mix);
 __global__ void k_meanfield_only(ScfDev S, const double* __restrict__ dens, double* __restrict__ field);
 
 #ifdef ADSCF_SCF_IMPL
 // Per point: phi_new = scale*dist; accuracy; mean field; residual into the
-// history slot of iteration k; energy and mixing partial sums.
-__global__ void __launch_bounds__(SCF_THREADS)
-k_closure(ScfDev S, int flags) {
+// history slot of iteration k; energy and mixing partial sums.  Block `bid`
+// of `nb` blocks working on this instance.
+__device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid, int nb) {
   __shared__ double red[NPART * 32];
   const double Q = q_total(S);
   const double scale = density_scale(S, Q);
@@ -103,7 +109,7 @@ k_closure(ScfDev S, int flags) {
   double acc[NPART];
 #pragma unroll
   for (int i = 0; i < NPART; ++i) acc[i] = 0.0;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < S.npts; p += gridDim.x * blockDim.x) {
+  for (int p = bid * blockDim.x + threadIdx.x; p < S.npts; p += nb * blockDim.x) {
     const int z = p / S.plane;
     const double wgt = S.wz ? S.wz[z] : S.dvol;
     const bool interior = !S.wall_mask || (z > 0 && z < S.nplanes - 1);
@@ -168,8 +174,18 @@ k_closure(ScfDev S, int flags) {
   if (threadIdx.x < NPART) {
     double r = 0.0;
     for (int w = 0; w < nw; ++w) r += red[threadIdx.x * 32 + w];
-    S.part[(size_t)blockIdx.x * NPART + threadIdx.x] = r;
+    S.part[(size_t)bid * NPART + threadIdx.x] = r;
   }
+}
+
+__global__ void __launch_bounds__(SCF_THREADS)
+k_closure(ScfDev S, int flags) { closure_body(S, flags, blockIdx.x, gridDim.x); }
+
+__global__ void __launch_bounds__(SCF_THREADS)
+k_closure_b(const ScfDev* __restrict__ Ss, int flags) {
+  const ScfDev S = Ss[blockIdx.y];
+  if ((int)blockIdx.x >= S.npart_blocks) return;
+  closure_body(S, flags, blockIdx.x, S.npart_blocks);
 }
 
 // Mixing dots only (for adscf_mix): x_k, r_k already in the history slot.
@@ -277,7 +293,7 @@ __device__ void lu_solve_nr(double* a, double* b, int n) {
 // One CTA: reduce partials, closure scalars, energy, mixing coefficients,
 // advance the iteration counter.  `have_closure` = partials include the
 // density/energy terms (k_closure) rather than only mixing dots.
-__global__ void k_solve(ScfDev S, int have_closure, int do_mix) {
+__device__ __forceinline__ void solve_body(const ScfDev& S, int have_closure, int do_mix) {
   __shared__ double tot[NPART];
   if (threadIdx.x < NPART) {
     double r = 0.0;
@@ -376,13 +392,19 @@ __global__ void k_solve(ScfDev S, int have_closure, int do_mix) {
   *S.iter = k + 1;
 }
 
+__global__ void k_solve(ScfDev S, int have_closure, int do_mix) { solve_body(S, have_closure, do_mix); }
+
+__global__ void k_solve_b(const ScfDev* __restrict__ Ss, int have_closure, int do_mix) {
+  const ScfDev S = Ss[blockIdx.x];
+  solve_body(S, have_closure, do_mix);
+}
+
 #endif  // ADSCF_SCF_IMPL
 
 // x_{k+1} = sum_j a_j x_j + b_j r_j into the next history slot; optional
 // E = exp(-ds x/2) for the pseudo-spectral propagator.
 template <typename T>
-__global__ void __launch_bounds__(SCF_THREADS)
-k_mix(ScfDev S, T* E, double ds) {
+__device__ __forceinline__ void mix_body(const ScfDev& S, T* E, double ds, int bid, int nb) {
   __shared__ double ca[SCF_MAX_SLOTS], cb[SCF_MAX_SLOTS];
   const int kn = *S.iter;               // already advanced to k+1
   const int nxt = kn % S.slots;
@@ -393,7 +415,7 @@ k_mix(ScfDev S, T* E, double ds) {
   }
   __syncthreads();
   const size_t nv = (size_t)S.ntypes * S.npts;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nv; i += (size_t)gridDim.x * blockDim.x) {
+  for (size_t i = bid * (size_t)blockDim.x + threadIdx.x; i < nv; i += (size_t)nb * blockDim.x) {
     double x;
     const int z = (int)((i % S.npts) / S.plane);
     const bool interior = !S.wall_mask || (z > 0 && z < S.nplanes - 1);
@@ -412,6 +434,18 @@ k_mix(ScfDev S, T* E, double ds) {
       store_ept(E, i - (size_t)c * S.npts, c, exp_boltzmann(-0.5 * ds * x));
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SCF_THREADS)
+k_mix(ScfDev S, T* E, double ds) { mix_body<T>(S, E, ds, blockIdx.x, gridDim.x); }
+
+// batch: instance blockIdx.y, its Boltzmann factors and ds from the ScfDev
+template <typename T>
+__global__ void __launch_bounds__(SCF_THREADS)
+k_mix_b(const ScfDev* __restrict__ Ss, int nblocks) {
+  const ScfDev S = Ss[blockIdx.y];
+  mix_body<T>(S, static_cast<T*>(S.mixE), S.mixds, blockIdx.x, nblocks);
 }
 
 #ifdef ADSCF_SCF_IMPL

@@ -32,6 +32,46 @@ def _f64(a, n=None):
     return a
 
 
+def make_params(geometry=L.BULK, grid=(32, 32, 32), size=(4.0, 4.0, 4.0), ds=0.01,
+                block_length=(0.5, 0.5), ensemble=1, rho=1.0, mu=0.0, kappa=25.0, chi=20.0,
+                monomer_volume=(1.0, 1.0), precision=L.FP64, mixing_type=L.MIX_LAMBDA,
+                mixing_dim=2, lam=0.1, lam_warm=1.0e-3, warm_iters=0, dss=None, n_a=0,
+                dz=None, int_scheme=1, int_span=0, ext_potential=None, ww=1.0, graft=None):
+    """adscf_params of one instance; returns (params, arrays it points into)."""
+    keep = []
+    p = L.Params()
+    p.geometry = geometry
+    p.gx, p.gy, p.gz = grid
+    p.sizex, p.sizey, p.sizez = size
+    p.ds = ds
+    if dss is not None:
+        dss = _f64(dss)
+        keep.append(dss)
+        p.dss = L.dptr(dss)
+        p.ns = dss.size - 1
+        p.n_a = n_a
+    p.block_length[0], p.block_length[1] = block_length
+    p.ensemble = ensemble
+    p.rho, p.mu = rho, mu
+    p.kappa, p.chi = kappa, chi
+    p.monomer_volume[0], p.monomer_volume[1] = monomer_volume
+    p.precision = precision
+    p.mixing_type = mixing_type
+    p.mixing_dim = mixing_dim
+    p.lam = lam
+    p.lam_warm = lam_warm
+    p.warm_iters = warm_iters
+    for name, arr in (("dz", dz), ("ext_potential", ext_potential), ("graft", graft)):
+        if arr is not None:
+            arr = _f64(arr)
+            keep.append(arr)
+            setattr(p, name, L.dptr(arr))
+    p.int_scheme = int_scheme
+    p.int_span = int_span
+    p.ww = ww
+    return p, keep
+
+
 class Context:
     """One SCF context (geometry, grid, chain, interactions, mixing)."""
 
@@ -43,37 +83,13 @@ class Context:
                  dz=None, int_scheme=1, int_span=0, ext_potential=None,
                  ww=1.0, graft=None, lib=None):
         self.lib = lib or L.load()
-        p = L.Params()
-        p.geometry = geometry
-        p.gx, p.gy, p.gz = grid
-        p.sizex, p.sizey, p.sizez = size
-        p.ds = ds
-        self._keep = []
-        if dss is not None:
-            dss = _f64(dss)
-            self._keep.append(dss)
-            p.dss = L.dptr(dss)
-            p.ns = dss.size - 1
-            p.n_a = n_a
-        p.block_length[0], p.block_length[1] = block_length
-        p.ensemble = ensemble
-        p.rho, p.mu = rho, mu
-        p.kappa, p.chi = kappa, chi
-        p.monomer_volume[0], p.monomer_volume[1] = monomer_volume
-        p.precision = precision
-        p.mixing_type = mixing_type
-        p.mixing_dim = mixing_dim
-        p.lam = lam
-        p.lam_warm = lam_warm
-        p.warm_iters = warm_iters
-        for name, arr in (("dz", dz), ("ext_potential", ext_potential), ("graft", graft)):
-            if arr is not None:
-                arr = _f64(arr)
-                self._keep.append(arr)
-                setattr(p, name, L.dptr(arr))
-        p.int_scheme = int_scheme
-        p.int_span = int_span
-        p.ww = ww
+        p, self._keep = make_params(
+            geometry=geometry, grid=grid, size=size, ds=ds, block_length=block_length,
+            ensemble=ensemble, rho=rho, mu=mu, kappa=kappa, chi=chi,
+            monomer_volume=monomer_volume, precision=precision, mixing_type=mixing_type,
+            mixing_dim=mixing_dim, lam=lam, lam_warm=lam_warm, warm_iters=warm_iters,
+            dss=dss, n_a=n_a, dz=dz, int_scheme=int_scheme, int_span=int_span,
+            ext_potential=ext_potential, ww=ww, graft=graft)
         self.params = p
         h = C.c_void_p()
         rc = self.lib.adscf_ctx_create(C.byref(p), C.byref(h))
@@ -218,3 +234,88 @@ class Context:
         res = L.IterResult()
         self._ck(self.lib.adscf_scf_iteration(self.h, L.dptr(x), L.dptr(d), C.byref(res)))
         return x, d, res
+
+
+class Batch:
+    """Independent bulk instances advanced together (adscf_batch_*).
+
+    ``instances`` is a list of keyword dicts for :func:`make_params` (bulk,
+    one precision).  Fields and densities are lists of [2][gz][gy][gx]
+    arrays, one per instance."""
+
+    def __init__(self, instances, lib=None):
+        self.lib = lib or L.load()
+        self.n = len(instances)
+        arr = (L.Params * self.n)()
+        self._keep = []
+        self.grids = []
+        for i, kw in enumerate(instances):
+            kw = dict(kw)
+            kw.setdefault("geometry", L.BULK)
+            p, keep = make_params(**kw)
+            self._keep += keep
+            arr[i] = p
+            self.grids.append(tuple(kw.get("grid", (32, 32, 32))))
+        h = C.c_void_p()
+        rc = self.lib.adscf_batch_create(arr, self.n, C.byref(h))
+        if rc != L.ADSCF_OK:
+            raise L.AdscfError(rc, self.lib.adscf_status_string(rc).decode())
+        self.h = h
+        self.offsets = [int(self.lib.adscf_batch_offset(h, i)) for i in range(self.n + 1)]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.adscf_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc != L.ADSCF_OK:
+            detail = self.lib.adscf_batch_last_error(self.h).decode()
+            raise L.AdscfError(rc, f"{self.lib.adscf_status_string(rc).decode()} ({detail})")
+
+    def _pack(self, arrays):
+        out = np.empty(self.offsets[-1])
+        for i, a in enumerate(arrays):
+            out[self.offsets[i]:self.offsets[i + 1]] = np.ravel(a)
+        return out
+
+    def _unpack(self, flat):
+        res = []
+        for i, (gx, gy, gz) in enumerate(self.grids):
+            res.append(flat[self.offsets[i]:self.offsets[i + 1]].reshape(2, gz, gy, gx))
+        return res
+
+    def set_fields(self, fields):
+        self._ck(self.lib.adscf_batch_set_fields(self.h, L.dptr(self._pack(fields))))
+
+    def get_fields(self):
+        out = np.empty(self.offsets[-1])
+        self._ck(self.lib.adscf_batch_get_fields(self.h, L.dptr(out)))
+        return self._unpack(out)
+
+    def get_densities(self):
+        out = np.empty(self.offsets[-1])
+        self._ck(self.lib.adscf_batch_get_densities(self.h, L.dptr(out)))
+        return self._unpack(out)
+
+    def scf_run(self, n_iter, tol=-1.0):
+        res = (L.IterResult * self.n)()
+        self._ck(self.lib.adscf_batch_scf_run(self.h, int(n_iter), float(tol), res))
+        return list(res)
+
+    def results(self):
+        res = (L.IterResult * self.n)()
+        self._ck(self.lib.adscf_batch_results(self.h, res))
+        return list(res)

@@ -233,6 +233,36 @@ ADSCF_API int adscf_stage_launches(const adscf_ctx *ctx, int stage);
 ADSCF_API int adscf_forward(adscf_ctx *ctx, const double *field, double *free_energy);
 ADSCF_API int adscf_backward(adscf_ctx *ctx, double *grad);
 
+/* ---- batches of independent bulk instances ------------------------------
+ * No single reference counterpart: the reference runs a phase-diagram or
+ * box-size scan as separate invocations of the bulk driver
+ * (Bulk_3D_FFT/Main_Diblock_Melt/main_diblock.f90), one parameter set each.
+ * A batch holds n bulk instances (geometry ADSCF_BULK, one precision, any
+ * grid of 2/3/5 factors, box, ds, block lengths, chi, kappa, mixing) and
+ * advances all of them by one SCF iteration per step: one launch per line
+ * pass and contour step over every instance still on its contour, batched
+ * closure, Anderson solve and mixing with per-instance histories, captured as
+ * one CUDA graph.  Fields and densities are packed: instance i occupies
+ * [2][gz_i][gy_i][gx_i] doubles starting at adscf_batch_offset(b, i);
+ * adscf_batch_offset(b, n) is the total.  adscf_batch_scf_run stops early
+ * once every instance's accuracy is <= tol (tol < 0: run n_iter) and fills
+ * out[n].                                                                 */
+typedef struct adscf_batch adscf_batch;
+ADSCF_API int adscf_batch_create(const adscf_params *params, int n, adscf_batch **out);
+ADSCF_API int adscf_batch_destroy(adscf_batch *b);
+ADSCF_API const char *adscf_batch_last_error(const adscf_batch *b);
+ADSCF_API long long adscf_batch_offset(const adscf_batch *b, int i);
+ADSCF_API int adscf_batch_set_fields(adscf_batch *b, const double *fields);
+ADSCF_API int adscf_batch_get_fields(adscf_batch *b, double *fields);
+ADSCF_API int adscf_batch_get_densities(adscf_batch *b, double *densities);
+ADSCF_API int adscf_batch_scf_run(adscf_batch *b, int n_iter, double tol, adscf_iter_result *out);
+ADSCF_API int adscf_batch_set_stream(adscf_batch *b, void *cuda_stream);
+/* enqueue `repeats` batch iterations without host synchronisation */
+ADSCF_API int adscf_batch_enqueue(adscf_batch *b, int repeats);
+ADSCF_API int adscf_batch_results(adscf_batch *b, adscf_iter_result *out);
+/* kernel launches of one batch iteration */
+ADSCF_API int adscf_batch_launches(const adscf_batch *b);
+
 /* ---- allocation-free propagator step ----------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (a pre-partitioned or quota-limited GPU, a driver that owns every
