@@ -1,4 +1,5 @@
-// batch.cu -- many independent bulk diblock SCF instances as one device job.
+// batch.cu -- many independent SCF instances (bulk, or one-line films and
+// brushes) as one device job.
 //
 // Each instance is the bulk SCF loop of Bulk_3D_FFT/Main_Diblock_Melt/
 // main_diblock.f90:410-429 with its own grid, box, contour step, block
@@ -10,15 +11,27 @@
 // launches with each instance's mixing history on the device.  One batch
 // iteration is one CUDA graph.  The line passes are the generic mixed-radix
 // kernels of bulk_kernels.cuh (any grid of 2, 3 and 5 factors).
+//
+// Film batches (Film_CK_AD/Film_1D, Brush_CK_AD: one z line per film with its
+// own graded mesh, adaptive contour and wall potential) sweep every film's
+// two chains in one launch (one thread per film and chain, CN with the NR
+// Thomas solve), take one contour launch and the same batched closure,
+// solve and mix.  A film whose mesh is graded past a spacing ratio of 1.5
+// keeps its sweep in FP64 on the split path (a second list and launch).
 #include <algorithm>
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
 #include "bulk_host.h"
+#include "film_host.h"
+#include "film_kernels.cuh"
 
 struct adscf_batch {
   int n = 0, prec = ADSCF_SPLIT;
@@ -45,6 +58,15 @@ struct adscf_batch {
   cudaGraphExec_t g_iter = nullptr;
   double* h_pinned = nullptr;
   size_t pinned_bytes = 0;
+  // film batches (Film_1D / brush, one line per film)
+  bool film = false;
+  int ntypes = 2;
+  void* d_f32 = nullptr;                // FilmDev<float>[n]
+  void* d_f64 = nullptr;                // FilmDev<double>[n]
+  int* d_list32 = nullptr;              // films sweeping in FP32 / FP64, by contour length
+  int* d_list64 = nullptr;
+  int n32 = 0, n64 = 0;
+  int* d_err = nullptr;                 // zero-pivot flag of the sweeps
 };
 
 namespace {
@@ -241,6 +263,212 @@ int build(adscf_batch* b) {
   return ADSCF_OK;
 }
 
+int check_film(const adscf_params& q, int prec, int geom, std::string& why) {
+  if (q.geometry != geom) { why = "one geometry for the whole batch"; return ADSCF_E_ARG; }
+  if (q.precision != prec) { why = "one precision for the whole batch"; return ADSCF_E_ARG; }
+  if (q.gx != 1 || q.gy != 1) { why = "batched films are one line (gx = gy = 1)"; return ADSCF_E_ARG; }
+  if (q.gz < 2 || !q.dz) { why = "films need gz >= 2 and dz"; return ADSCF_E_ARG; }
+  if (!(q.sizex > 0 && q.sizey > 0 && q.sizez > 0)) { why = "box size"; return ADSCF_E_ARG; }
+  if (!q.dss && !(q.ds > 0)) { why = "ds or dss"; return ADSCF_E_ARG; }
+  if (q.mixing_type < 1 || q.mixing_type > 3) { why = "mixing_type"; return ADSCF_E_ARG; }
+  if (q.mixing_type == 3 && (q.mixing_dim < 1 || q.mixing_dim > SCF_MAX_HIST)) { why = "mixing_dim"; return ADSCF_E_ARG; }
+  if (q.ensemble != 1 && q.ensemble != 2) { why = "ensemble"; return ADSCF_E_ARG; }
+  if (geom == ADSCF_BRUSH && !q.graft) { why = "brush needs the grafting distribution"; return ADSCF_E_ARG; }
+  return ADSCF_OK;
+}
+
+// Film batch: one line per film; tables (coefficients, weights, schedules,
+// wall potentials) in one FP64 array, propagators and SCF state in the pool.
+int build_film(adscf_batch* b) {
+  const int n = b->n;
+  const int geom = b->p[0].geometry;
+  const bool brush = geom == ADSCF_BRUSH;
+  b->film = true;
+  b->ntypes = brush ? 1 : 2;
+  const int nt = b->ntypes;
+  std::vector<FilmTables> tb(n);
+  std::vector<int> na(n), t64(n);
+  b->ns.resize(n); b->npts.resize(n); b->slots.resize(n); b->foff.assign(n + 1, 0);
+  b->hS.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const adscf_params& q = b->p[i];
+    std::string why;
+    if (check_film(q, b->prec, geom, why)) return berr(b, ADSCF_E_ARG, "instance " + std::to_string(i) + ": " + why);
+    int ns, a;
+    if (q.dss) {
+      ns = q.ns;
+      a = brush ? q.ns : q.n_a;
+    } else {
+      a = nint_b(q.block_length[0] / q.ds);
+      ns = a + (brush ? 0 : nint_b(q.block_length[1] / q.ds));
+    }
+    if (ns < 1 || a < 0 || a > ns) return berr(b, ADSCF_E_ARG, "instance " + std::to_string(i) + ": contour");
+    if (film_tables(q, ns, a, tb[i], why)) return berr(b, ADSCF_E_ARG, "instance " + std::to_string(i) + ": " + why);
+    b->ns[i] = ns;
+    na[i] = a;
+    b->npts[i] = q.gz + 1;
+    b->slots[i] = q.mixing_type == 3 ? q.mixing_dim + 1 : 2;
+    b->foff[i + 1] = b->foff[i] + (size_t)nt * b->npts[i];
+    b->maxns = std::max(b->maxns, ns);
+    t64[i] = film_sweep_fp64(b->prec, tb[i].max_ratio) ? 1 : 0;
+  }
+  // FP64 tables: al, be, ga, wz [npts]; dss, wA, wB [ns+1]; ext [nt][npts]; graft [npts]
+  std::vector<double> tab;
+  struct TOff { size_t al, be, ga, wz, dss, wA, wB, ext, graft; };
+  std::vector<TOff> to(n);
+  auto put = [&](const double* v, size_t cnt) {
+    const size_t o = tab.size();
+    tab.insert(tab.end(), v, v + cnt);
+    tab.resize((tab.size() + 3) & ~size_t(3));   // 32-byte granules
+    return o;
+  };
+  for (int i = 0; i < n; ++i) {
+    const size_t np = b->npts[i], ns1 = b->ns[i] + 1;
+    to[i].al = put(tb[i].al.data(), np); to[i].be = put(tb[i].be.data(), np);
+    to[i].ga = put(tb[i].ga.data(), np); to[i].wz = put(tb[i].wz.data(), np);
+    to[i].dss = put(tb[i].dss.data(), ns1); to[i].wA = put(tb[i].wA.data(), ns1);
+    to[i].wB = put(tb[i].wB.data(), ns1);
+    to[i].ext = b->p[i].ext_potential ? put(b->p[i].ext_potential, (size_t)nt * np) : SIZE_MAX;
+    to[i].graft = brush ? put(b->p[i].graft, np) : SIZE_MAX;
+  }
+  BK(cudaMalloc(&b->d_fk, tab.size() * sizeof(double)));
+  BK(cudaMemcpyAsync(b->d_fk, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  const double* dtab = static_cast<const double*>(b->d_fk);
+  // pool
+  Carve c;
+  struct Off { size_t q, qd, gam, dist, dens, hx, hr, qpart, part, gram, coef; };
+  std::vector<Off> o(n);
+  for (int i = 0; i < n; ++i) {
+    const size_t np = b->npts[i], es = t64[i] ? 8 : 4;
+    o[i].q = c.take((size_t)(b->ns[i] + 1) * np * es);
+    o[i].qd = c.take((size_t)(b->ns[i] + 1) * np * es);
+    o[i].gam = c.take(2 * np * es);
+    o[i].dist = c.take((size_t)nt * np * sizeof(double));
+    o[i].dens = c.take((size_t)nt * np * sizeof(double));
+    o[i].hx = c.take((size_t)b->slots[i] * nt * np * sizeof(double));
+    o[i].hr = c.take((size_t)b->slots[i] * nt * np * sizeof(double));
+    o[i].qpart = c.take(sizeof(double));
+    o[i].part = c.take(NPART * sizeof(double));
+    o[i].gram = c.take(SCF_MAX_SLOTS * SCF_MAX_SLOTS * sizeof(double));
+    o[i].coef = c.take(2 * SCF_MAX_SLOTS * sizeof(double));
+  }
+  const size_t o_res = c.take((size_t)n * R_COUNT * sizeof(double));
+  const size_t o_iter = c.take((size_t)n * sizeof(int));
+  const size_t o_err = c.take(sizeof(int));
+  if (cudaMalloc(&b->pool, c.off) != cudaSuccess) {
+    cudaGetLastError();
+    return berr(b, ADSCF_E_OOM, "batch pool of " + std::to_string(c.off >> 20) + " MiB");
+  }
+  unsigned char* base = static_cast<unsigned char*>(b->pool);
+  BK(cudaMemsetAsync(b->pool, 0, c.off, b->stream));
+  b->d_resall = reinterpret_cast<double*>(base + o_res);
+  b->d_iterall = reinterpret_cast<int*>(base + o_iter);
+  b->d_err = reinterpret_cast<int*>(base + o_err);
+  std::vector<FilmDev<float>> f32(n);
+  std::vector<FilmDev<double>> f64(n);
+  std::vector<int> l32, l64;
+  for (int i = 0; i < n; ++i) {
+    const adscf_params& q = b->p[i];
+    const size_t np = b->npts[i];
+    auto fill = [&](auto& D) {
+      using T = std::remove_reference_t<decltype(*D.q)>;
+      D.gx = 1; D.gy = 1; D.gz = q.gz;
+      D.nlines = 1; D.npts = (int)np;
+      D.ns = b->ns[i]; D.na = na[i];
+      D.ntypes = nt; D.brush = brush; D.single = 0; D.span = q.int_span;
+      D.alpha = dtab + to[i].al; D.beta = dtab + to[i].be; D.gamma = dtab + to[i].ga;
+      D.dss = dtab + to[i].dss; D.wA = dtab + to[i].wA; D.wB = dtab + to[i].wB;
+      D.wz = dtab + to[i].wz;
+      D.graft = brush ? dtab + to[i].graft : nullptr;
+      D.q = reinterpret_cast<T*>(base + o[i].q);
+      D.qd = reinterpret_cast<T*>(base + o[i].qd);
+      D.gam = reinterpret_cast<T*>(base + o[i].gam);
+      D.dist = reinterpret_cast<double*>(base + o[i].dist);
+      D.qpart = reinterpret_cast<double*>(base + o[i].qpart);
+      D.err = b->d_err;
+      D.dx = q.sizex; D.dy = q.sizey;
+      D.w1 = nullptr;
+    };
+    if (t64[i]) { fill(f64[i]); l64.push_back(i); }
+    else { fill(f32[i]); l32.push_back(i); }
+    ScfDev& S = b->hS[i];
+    S = ScfDev{};
+    const double volume = q.sizex * q.sizey * q.sizez;
+    S.npts = (int)np; S.ntypes = nt; S.plane = 1; S.nplanes = q.gz + 1; S.wall_mask = 1;
+    S.dvol = volume / (double)q.gz;
+    S.wz = dtab + to[i].wz;
+    S.ext = b->p[i].ext_potential ? dtab + to[i].ext : nullptr;
+    S.kappa = q.kappa; S.chi = q.chi;
+    S.v0 = q.monomer_volume[0] != 0 ? q.monomer_volume[0] : 1.0;
+    S.v1 = q.monomer_volume[1] != 0 ? q.monomer_volume[1] : 1.0;
+    S.ww = q.ww; S.homopolymer = brush;
+    S.ensemble = q.ensemble; S.rho = q.rho; S.mu = q.mu; S.volume = volume;
+    S.chain_len = tb[i].chain_len;
+    S.dist = reinterpret_cast<double*>(base + o[i].dist);
+    S.dens = reinterpret_cast<double*>(base + o[i].dens);
+    S.hx = reinterpret_cast<double*>(base + o[i].hx);
+    S.hr = reinterpret_cast<double*>(base + o[i].hr);
+    S.slots = b->slots[i];
+    S.mixing_type = q.mixing_type;
+    S.warm = q.warm_iters > q.mixing_dim ? q.warm_iters : q.mixing_dim;
+    S.lambda = q.lambda;
+    S.lam_warm = q.lam_warm > 0 ? q.lam_warm : 1.0e-3;
+    S.qpart = reinterpret_cast<double*>(base + o[i].qpart); S.nqpart = 1; S.qscale = 1.0;
+    S.part = reinterpret_cast<double*>(base + o[i].part); S.npart_blocks = 1;
+    S.gram = reinterpret_cast<double*>(base + o[i].gram);
+    S.coef = reinterpret_cast<double*>(base + o[i].coef);
+    S.iter = b->d_iterall + i;
+    S.res = b->d_resall + (size_t)i * R_COUNT;
+    S.mixE = nullptr;
+    S.mixds = 0.0;
+  }
+  // longest contours first: a warp's threads then walk similar step counts
+  auto by_work = [&](int a, int c2) {
+    return (long long)b->ns[a] * b->npts[a] > (long long)b->ns[c2] * b->npts[c2];
+  };
+  std::stable_sort(l32.begin(), l32.end(), by_work);
+  std::stable_sort(l64.begin(), l64.end(), by_work);
+  b->n32 = (int)l32.size();
+  b->n64 = (int)l64.size();
+  BK(cudaMalloc(&b->d_f32, n * sizeof(FilmDev<float>)));
+  BK(cudaMalloc(&b->d_f64, n * sizeof(FilmDev<double>)));
+  BK(cudaMemcpyAsync(b->d_f32, f32.data(), n * sizeof(FilmDev<float>), cudaMemcpyHostToDevice, b->stream));
+  BK(cudaMemcpyAsync(b->d_f64, f64.data(), n * sizeof(FilmDev<double>), cudaMemcpyHostToDevice, b->stream));
+  BK(cudaMalloc(&b->d_list32, std::max<size_t>(1, l32.size()) * sizeof(int)));
+  BK(cudaMalloc(&b->d_list64, std::max<size_t>(1, l64.size()) * sizeof(int)));
+  if (!l32.empty())
+    BK(cudaMemcpyAsync(b->d_list32, l32.data(), l32.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  if (!l64.empty())
+    BK(cudaMemcpyAsync(b->d_list64, l64.data(), l64.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  BK(cudaMalloc(&b->d_S, n * sizeof(ScfDev)));
+  BK(cudaMemcpyAsync(b->d_S, b->hS.data(), n * sizeof(ScfDev), cudaMemcpyHostToDevice, b->stream));
+  std::vector<int> ones(n, 1);
+  BK(cudaMemcpyAsync(b->d_iterall, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  b->clos_grid = 1;
+  b->mix_grid = 1;
+  BK(cudaStreamSynchronize(b->stream));
+  return ADSCF_OK;
+}
+
+int enqueue_film(adscf_batch* b) {
+  cudaStream_t s = b->stream;
+  const FilmDev<float>* f32 = static_cast<const FilmDev<float>*>(b->d_f32);
+  const FilmDev<double>* f64 = static_cast<const FilmDev<double>*>(b->d_f64);
+  if (b->n32)
+    k_film1d_chains_b<float><<<dim3((b->n32 + FILM_THREADS - 1) / FILM_THREADS, 2), FILM_THREADS, 0, s>>>(
+        f32, b->d_S, b->d_list32, b->n32);
+  if (b->n64)
+    k_film1d_chains_b<double><<<dim3((b->n64 + FILM_THREADS - 1) / FILM_THREADS, 2), FILM_THREADS, 0, s>>>(
+        f64, b->d_S, b->d_list64, b->n64);
+  if (b->n32) k_film_contour_b<float><<<b->n32, 256, 0, s>>>(f32, b->d_list32);
+  if (b->n64) k_film_contour_b<double><<<b->n64, 256, 0, s>>>(f64, b->d_list64);
+  k_closure_b<<<dim3(1, b->n), SCF_THREADS, 0, s>>>(b->d_S, CL_MEANFIELD | CL_MIXDOTS);
+  k_solve_b<<<b->n, 64, 0, s>>>(b->d_S, 1, 1);
+  k_mix_b<float><<<dim3(1, b->n), SCF_THREADS, 0, s>>>(b->d_S, 1);
+  BK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
 template <typename T>
 int enqueue_iteration(adscf_batch* b) {
   const BulkDev<T>* d = static_cast<const BulkDev<T>*>(b->d_inst);
@@ -264,6 +492,7 @@ int enqueue_iteration(adscf_batch* b) {
 }
 
 int enqueue(adscf_batch* b) {
+  if (b->film) return enqueue_film(b);
   return b->prec == ADSCF_SPLIT ? enqueue_iteration<float>(b) : enqueue_iteration<double>(b);
 }
 
@@ -319,6 +548,19 @@ int read_results(adscf_batch* b, adscf_iter_result* out, double* max_acc) {
   return ADSCF_OK;
 }
 
+// zero-pivot flag of the film sweeps since the last check (cleared on read)
+int check_pivot(adscf_batch* b) {
+  if (!b->d_err) return ADSCF_OK;
+  int e = 0;
+  BK(cudaMemcpyAsync(&e, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  BK(cudaStreamSynchronize(b->stream));
+  if (e) {
+    BK(cudaMemsetAsync(b->d_err, 0, sizeof(int), b->stream));
+    return berr(b, ADSCF_E_PIVOT, "zero pivot in a tridiagonal sweep (TriDiag Error)");
+  }
+  return ADSCF_OK;
+}
+
 template <typename T>
 int set_fields_t(adscf_batch* b, const double* fields) {
   const size_t tot = b->foff[b->n];
@@ -327,12 +569,13 @@ int set_fields_t(adscf_batch* b, const double* fields) {
   std::memcpy(b->h_pinned, fields, tot * sizeof(double));
   for (int i = 0; i < b->n; ++i) {
     const ScfDev& S = b->hS[i];
-    const size_t nv = 2 * (size_t)S.npts;
+    const size_t nv = (size_t)S.ntypes * S.npts;
     BK(cudaMemsetAsync(S.hx, 0, (size_t)S.slots * nv * sizeof(double), b->stream));
     BK(cudaMemsetAsync(S.hr, 0, (size_t)S.slots * nv * sizeof(double), b->stream));
     BK(cudaMemsetAsync(S.gram, 0, SCF_MAX_SLOTS * SCF_MAX_SLOTS * sizeof(double), b->stream));
     double* x1 = S.hx + (size_t)(1 % S.slots) * nv;
     BK(cudaMemcpyAsync(x1, b->h_pinned + b->foff[i], nv * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    if (b->film) continue;
     const int gb = (int)std::min<size_t>((nv + 255) / 256, 152 * 8);
     k_expfield<T><<<gb, 256, 0, b->stream>>>(x1, static_cast<T*>(b->E[i]), (size_t)S.npts, b->p[i].ds);
   }
@@ -352,7 +595,7 @@ int get_t(adscf_batch* b, double* out, bool fields) {
   if ((rc = pinned(b, tot * sizeof(double)))) return rc;
   for (int i = 0; i < b->n; ++i) {
     const ScfDev& S = b->hS[i];
-    const size_t nv = 2 * (size_t)S.npts;
+    const size_t nv = (size_t)S.ntypes * S.npts;
     const double* src = fields ? S.hx + (size_t)(it[i] % S.slots) * nv : S.dens;
     BK(cudaMemcpyAsync(b->h_pinned + b->foff[i], src, nv * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   }
@@ -375,10 +618,10 @@ int adscf_batch_create(const adscf_params* params, int n, adscf_batch** out) {
   b->prec = params[0].precision;
   if (b->prec != ADSCF_FP64 && b->prec != ADSCF_SPLIT) { delete b; return ADSCF_E_ARG; }
   b->p.assign(params, params + n);
-  for (int i = 0; i < n; ++i) {
+  const bool film = params[0].geometry == ADSCF_FILM_1D || params[0].geometry == ADSCF_BRUSH;
+  for (int i = 0; i < n && !film; ++i) {
     std::string why;
     if (check_params(b->p[i], b->prec, why)) { delete b; return ADSCF_E_ARG; }
-    b->p[i].dss = nullptr; b->p[i].dz = nullptr; b->p[i].ext_potential = nullptr; b->p[i].graft = nullptr;
   }
   if (cudaGetDevice(&b->dev) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -387,7 +630,9 @@ int adscf_batch_create(const adscf_params* params, int n, adscf_batch** out) {
     return ADSCF_E_CUDA;
   }
   b->stream = b->own_stream;
-  const int rc = b->prec == ADSCF_SPLIT ? build<float>(b) : build<double>(b);
+  const int rc = film ? build_film(b) : b->prec == ADSCF_SPLIT ? build<float>(b) : build<double>(b);
+  // the caller's arrays were read during the build only
+  for (adscf_params& q : b->p) { q.dss = nullptr; q.dz = nullptr; q.ext_potential = nullptr; q.graft = nullptr; }
   if (rc) {
     adscf_batch_destroy(b);
     return rc;
@@ -403,6 +648,7 @@ int adscf_batch_destroy(adscf_batch* b) {
   cudaFree(b->pool); cudaFree(b->d_inst); cudaFree(b->d_S);
   cudaFree(b->d_tw); cudaFree(b->d_fk); cudaFree(b->d_g64);
   cudaFree(b->d_wx); cudaFree(b->d_wy); cudaFree(b->d_wz);
+  cudaFree(b->d_f32); cudaFree(b->d_f64); cudaFree(b->d_list32); cudaFree(b->d_list64);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;
@@ -440,10 +686,11 @@ int adscf_batch_scf_run(adscf_batch* b, int n_iter, double tol, adscf_iter_resul
     if (tol >= 0.0) {
       double mx = 0.0;
       if ((rc = read_results(b, out, &mx))) return rc;
-      if (!(mx > tol)) return ADSCF_OK;
+      if (!(mx > tol)) return check_pivot(b);
     }
   }
-  return read_results(b, out, nullptr);
+  rc = read_results(b, out, nullptr);
+  return rc ? rc : check_pivot(b);
 }
 
 int adscf_batch_set_stream(adscf_batch* b, void* cuda_stream) {
@@ -466,6 +713,10 @@ int adscf_batch_results(adscf_batch* b, adscf_iter_result* out) {
   return read_results(b, out, nullptr);
 }
 
-int adscf_batch_launches(const adscf_batch* b) { return b ? 1 + 4 * b->maxns + 4 : -1; }
+int adscf_batch_launches(const adscf_batch* b) {
+  if (!b) return -1;
+  if (b->film) return 2 * ((b->n32 > 0) + (b->n64 > 0)) + 3;
+  return 1 + 4 * b->maxns + 4;
+}
 
 }  // extern "C"

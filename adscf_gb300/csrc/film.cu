@@ -4,6 +4,7 @@
 #include <cstring>
 #include <vector>
 
+#include "film_host.h"
 #include "film_kernels.cuh"
 #include "internal.h"
 
@@ -161,60 +162,21 @@ int film_create(adscf_ctx* ctx, const adscf_params* p) {
   if (!F) return ADSCF_E_OOM;
   ctx->film = F;
   const int gz = ctx->gz;
-  if (gz < 2) return set_err(ctx, ADSCF_E_ARG, "films need gz >= 2 intervals");
   if (ctx->geometry == ADSCF_FILM_3D && (ctx->gx < 1 || ctx->gy < 1))
     return set_err(ctx, ADSCF_E_ARG, "grid");
-  std::vector<double> dz(p->dz, p->dz + gz + 1);
-  for (int i = 1; i <= gz; ++i)
-    if (!(dz[i] > 0)) return set_err(ctx, ADSCF_E_ARG, "dz[1..gz] must be positive");
-  // z coefficients: Film_1D / Brush form b = ds (h1+h2)/h1/h2/(h1+h2)
-  // (Film_1D/.../mod_realspace.f90:36-43), Film_3D form b = ds/h1/h2 (:70-76)
-  std::vector<double> al(gz + 1, 0.0), be(gz + 1, 0.0), ga(gz + 1, 0.0);
-  for (int z = 1; z < gz; ++z) {
-    const double h1 = dz[z], h2 = dz[z + 1];
-    al[z] = 1.0 / h1 / (h1 + h2);
-    ga[z] = 1.0 / h2 / (h1 + h2);
-    be[z] = ctx->geometry == ADSCF_FILM_3D ? 1.0 / h1 / h2 : (h1 + h2) / h1 / h2 / (h1 + h2);
-    F->max_ratio = std::max(F->max_ratio, std::max(h1 / h2, h2 / h1));
-  }
-  // integrator weights dx dy w_z (Film_3D/.../mod_realspace.f90:267-281 for
-  // span 0, Film_1D :201-218 and Brush mod_adaptive.f90:124-143 for span 1)
-  const double dx = p->sizex / p->gx, dy = p->sizey / p->gy;
-  std::vector<double> wz(gz + 1, 0.0);
-  if (p->int_scheme == 0) {
-    const int lo = p->int_span == 0 ? 0 : 1;
-    for (int i = lo; i <= gz - 1; ++i) wz[i] += dz[i];
-  } else {
-    const int hi = p->int_span == 0 ? gz : gz - 1;
-    for (int i = 1; i <= hi; ++i) { wz[i - 1] += 0.5 * dz[i]; wz[i] += 0.5 * dz[i]; }
-  }
-  for (double& v : wz) v *= dx * dy;
-  // contour schedule: dss[0..ns]
-  std::vector<double> dss(ctx->ns + 1, 0.0);
-  if (p->dss) {
-    for (int s = 0; s <= ctx->ns; ++s) dss[s] = p->dss[s];
-  } else {
-    for (int s = 1; s <= ctx->ns; ++s) dss[s] = p->ds;
-  }
-  double len = 0.0;
-  for (int s = 1; s <= ctx->ns; ++s) len += dss[s];
-  ctx->S.chain_len = len;
-  // contour weights: diblock = trapezoid per block with the step sizes
-  // (mod_diblock.f90:143-154 for uniform steps); brush = the
-  // 1/2 (dss_s + dss_{s+1}) rule of mod_homopolymer.f90:231-239, dss_0 = 0
-  std::vector<double> wA(ctx->ns + 1, 0.0), wB(ctx->ns + 1, 0.0);
-  if (ctx->geometry == ADSCF_BRUSH) {
-    const int N = ctx->ns;
-    wA[0] = 0.5 * dss[0];
-    for (int s = 1; s < N; ++s) wA[s] = 0.5 * (dss[s] + dss[s + 1]);
-    wA[N] = 0.5 * dss[N];
-  } else {
-    for (int s = 0; s < ctx->na; ++s) { wA[s] += 0.5 * dss[s + 1]; wA[s + 1] += 0.5 * dss[s + 1]; }
-    for (int s = ctx->na; s < ctx->ns; ++s) { wB[s] += 0.5 * dss[s + 1]; wB[s + 1] += 0.5 * dss[s + 1]; }
-  }
-  // precision: FP32 sweeps on the split path unless the mesh is graded past
-  // a neighbour spacing ratio of 1.5, where the Thomas sweep stays FP64
-  F->t64 = !(ctx->prec == ADSCF_SPLIT && F->max_ratio <= 1.5);
+  FilmTables tb;
+  std::string why;
+  if (film_tables(*p, ctx->ns, ctx->na, tb, why)) return set_err(ctx, ADSCF_E_ARG, why);
+  F->max_ratio = tb.max_ratio;
+  ctx->S.chain_len = tb.chain_len;
+  const std::vector<double>& al = tb.al;
+  const std::vector<double>& be = tb.be;
+  const std::vector<double>& ga = tb.ga;
+  const std::vector<double>& wz = tb.wz;
+  const std::vector<double>& dss = tb.dss;
+  const std::vector<double>& wA = tb.wA;
+  const std::vector<double>& wB = tb.wB;
+  F->t64 = film_sweep_fp64(ctx->prec, F->max_ratio);
   const size_t L = (size_t)ctx->gx * ctx->gy;
   size_t gam_elems = 2 * (size_t)(gz + 1) * L;
   if (ctx->geometry == ADSCF_FILM_3D) {

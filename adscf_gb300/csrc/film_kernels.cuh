@@ -15,6 +15,7 @@
 // (consecutive lines) touch consecutive addresses.
 #pragma once
 #include "common.cuh"
+#include "scf_kernels.cuh"
 
 #define FILM_THREADS 128
 
@@ -78,12 +79,7 @@ __device__ __forceinline__ double film_ds(const double* dss, int dir, int s, int
 // blockIdx.y = chain (0 forward, 1 backward).
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(FILM_THREADS)
-k_film1d_chains(FilmDev<T> F, FieldRef fr) {
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  const int dir = blockIdx.y;
-  if (line >= F.nlines) return;
-  const double* field = fr.get();
+__device__ __forceinline__ void film1d_chain(const FilmDev<T>& F, const double* field, int line, int dir) {
   const int L = F.nlines, gz = F.gz;
   T* chain = dir == 0 ? F.q : F.qd;
   T* gam = F.gam + (size_t)dir * (gz + 1) * L;
@@ -134,6 +130,14 @@ k_film1d_chains(FilmDev<T> F, FieldRef fr) {
       unext = u;
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FILM_THREADS)
+k_film1d_chains(FilmDev<T> F, FieldRef fr) {
+  const int line = blockIdx.x * blockDim.x + threadIdx.x;
+  if (line >= F.nlines) return;
+  film1d_chain<T>(F, fr.get(), line, blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -307,13 +311,12 @@ __global__ void k_film_fill(T* __restrict__ q, T* __restrict__ qd, int n) {
 // 226), with the per-plane weights wz.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(256)
-k_film_contour(FilmDev<T> F) {
+__device__ __forceinline__ void film_contour_body(const FilmDev<T>& F, int bid, int nb) {
   __shared__ double red[32];
   const int N = F.ns;
   const size_t np = F.npts;
   double qs = 0.0;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < F.npts; p += gridDim.x * blockDim.x) {
+  for (int p = bid * blockDim.x + threadIdx.x; p < F.npts; p += nb * blockDim.x) {
     double a0 = 0.0, a1 = 0.0;
     for (int s = 0; s <= N; ++s) {
       const double pr = (double)F.q[(size_t)s * np + p] * (double)F.qd[(size_t)(N - s) * np + p];
@@ -328,5 +331,35 @@ k_film_contour(FilmDev<T> F) {
     qs += F.wz[z] * qn;
   }
   const double tot = block_reduce_1(qs, red);
-  if (threadIdx.x == 0) F.qpart[blockIdx.x] = tot;
+  if (threadIdx.x == 0) F.qpart[bid] = tot;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_film_contour(FilmDev<T> F) { film_contour_body<T>(F, blockIdx.x, gridDim.x); }
+
+// ---------------------------------------------------------------------------
+// Film batches: many independent one-line films (Film_1D or brush), each
+// with its own mesh, contour schedule and SCF state.  `films` lists the batch
+// instances that sweep in precision T (a graded mesh keeps FP64), ordered by
+// contour length so a warp's threads walk similar step counts.  The field of
+// instance f is the current slot of its SCF history.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(FILM_THREADS)
+k_film1d_chains_b(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__ Ss,
+                  const int* __restrict__ films, int nf) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nf) return;
+  const int f = films[k];
+  const ScfDev& S = Ss[f];
+  const double* field = S.hx + (size_t)((*S.iter) % S.slots) * ((size_t)S.ntypes * S.npts);
+  film1d_chain<T>(Fs[f], field, 0, blockIdx.y);
+}
+
+// one block per film of the list
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_film_contour_b(const FilmDev<T>* __restrict__ Fs, const int* __restrict__ films) {
+  film_contour_body<T>(Fs[films[blockIdx.x]], 0, 1);
 }

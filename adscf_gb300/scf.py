@@ -237,25 +237,31 @@ class Context:
 
 
 class Batch:
-    """Independent bulk instances advanced together (adscf_batch_*).
+    """Independent instances advanced together (adscf_batch_*).
 
-    ``instances`` is a list of keyword dicts for :func:`make_params` (bulk,
-    one precision).  Fields and densities are lists of [2][gz][gy][gx]
-    arrays, one per instance."""
+    ``instances`` is a list of keyword dicts for :func:`make_params`: all
+    bulk, or all one-line films (FILM_1D) or brushes, one precision.  Fields
+    and densities are lists of [ntypes][planes][gy][gx] arrays, one per
+    instance."""
 
     def __init__(self, instances, lib=None):
         self.lib = lib or L.load()
         self.n = len(instances)
         arr = (L.Params * self.n)()
         self._keep = []
-        self.grids = []
+        self.shapes = []
         for i, kw in enumerate(instances):
             kw = dict(kw)
             kw.setdefault("geometry", L.BULK)
             p, keep = make_params(**kw)
             self._keep += keep
             arr[i] = p
-            self.grids.append(tuple(kw.get("grid", (32, 32, 32))))
+            gx, gy, gz = kw.get("grid", (32, 32, 32))
+            geom = kw["geometry"]
+            if geom == L.BULK:
+                self.shapes.append((2, gz, gy, gx))
+            else:   # films and brushes carry both walls, planes 0..gz
+                self.shapes.append((1 if geom == L.BRUSH else 2, gz + 1, gy, gx))
         h = C.c_void_p()
         rc = self.lib.adscf_batch_create(arr, self.n, C.byref(h))
         if rc != L.ADSCF_OK:
@@ -292,10 +298,7 @@ class Batch:
         return out
 
     def _unpack(self, flat):
-        res = []
-        for i, (gx, gy, gz) in enumerate(self.grids):
-            res.append(flat[self.offsets[i]:self.offsets[i + 1]].reshape(2, gz, gy, gx))
-        return res
+        return [flat[self.offsets[i]:self.offsets[i + 1]].reshape(sh) for i, sh in enumerate(self.shapes)]
 
     def set_fields(self, fields):
         self._ck(self.lib.adscf_batch_set_fields(self.h, L.dptr(self._pack(fields))))
