@@ -9,8 +9,10 @@
 // on its contour (work lists sorted by Ns, so the active tiles of step t are
 // a prefix), one contour launch, and batched closure / Anderson solve / mix
 // launches with each instance's mixing history on the device.  One batch
-// iteration is one CUDA graph.  The line passes are the generic mixed-radix
-// kernels of bulk_kernels.cuh (any grid of 2, 3 and 5 factors).
+// iteration is one CUDA graph.  Instances are grouped by pass kernel: cubic
+// grids of 32..256 points run the register-FFT passes of bulk_reg.cuh, every
+// other grid of 2, 3 and 5 factors the generic mixed-radix passes of
+// bulk_kernels.cuh; each group has its own Ns-sorted work lists and launches.
 //
 // Film batches (Film_CK_AD/Film_1D, Brush_CK_AD: one z line per film with its
 // own graded mesh, adaptive contour and wall potential) sweep every film's
@@ -30,6 +32,7 @@
 
 #include "internal.h"
 #include "bulk_host.h"
+#include "bulk_reg.cuh"
 #include "film_host.h"
 #include "film_kernels.cuh"
 
@@ -51,9 +54,15 @@ struct adscf_batch {
   void* d_tw = nullptr;
   void* d_fk = nullptr;
   double* d_g64 = nullptr;
-  int2 *d_wx = nullptr, *d_wy = nullptr, *d_wz = nullptr;
-  std::vector<int> pre_x, pre_y, pre_z;  // tiles active at contour step t (t = 0..maxns)
-  size_t smx = 0, smy = 0, smz = 0;
+  // bulk instances grouped by pass kernel: register FFT of one line length
+  // on all three axes (32..256), or the generic mixed-radix kernels (n = 0)
+  struct PassClass {
+    int n = 0;
+    int2 *wx = nullptr, *wy = nullptr, *wz = nullptr;
+    std::vector<int> px, py, pz;        // tiles active at contour step t (t = 0..maxns)
+    size_t smx = 0, smy = 0, smz = 0;
+  };
+  std::vector<PassClass> cls;
   int maxns = 0, cont_blocks = 64, clos_grid = 0, mix_grid = 0;
   cudaGraphExec_t g_iter = nullptr;
   double* h_pinned = nullptr;
@@ -82,6 +91,24 @@ int berr(adscf_batch* b, int code, const std::string& m) {
   } while (0)
 
 int nint_b(double x) { return x >= 0 ? (int)std::floor(x + 0.5) : -(int)std::floor(-x + 0.5); }
+
+int reg_tpl(int n) {
+  switch (n) {
+    case 32: return regk::Cfg<32>::TPL;
+    case 64: return regk::Cfg<64>::TPL;
+    case 128: return regk::Cfg<128>::TPL;
+    default: return regk::Cfg<256>::TPL;
+  }
+}
+template <typename T>
+size_t reg_smem(int n) {
+  switch (n) {
+    case 32: return regk::Layout<T, 32>::bytes;
+    case 64: return regk::Layout<T, 64>::bytes;
+    case 128: return regk::Layout<T, 128>::bytes;
+    default: return regk::Layout<T, 256>::bytes;
+  }
+}
 
 struct Carve {
   size_t off = 0;
@@ -223,42 +250,69 @@ int build(adscf_batch* b) {
   std::vector<int> ones(n, 1);
   BK(cudaMemcpyAsync(b->d_iterall, ones.data(), n * sizeof(int), cudaMemcpyHostToDevice, b->stream));
 
-  // work lists, instances by descending Ns: the tiles of the instances still
-  // on their contour at step t are a prefix
+  // work lists per kernel class, instances by descending Ns: the tiles of the
+  // instances still on their contour at step t are a prefix
   std::vector<int> ord(n);
   for (int i = 0; i < n; ++i) ord[i] = i;
   std::stable_sort(ord.begin(), ord.end(), [&](int a, int c2) { return b->ns[a] > b->ns[c2]; });
-  std::vector<int2> wx, wy, wz;
-  std::vector<int> tx(n), ty(n), tz(n);
-  for (int i : ord) {
+  auto class_of = [&](int i) {
     const BulkDev<T>& d = I[i];
-    tx[i] = (d.gy * d.gz + d.px.lpc - 1) / d.px.lpc;
-    ty[i] = (d.gx * d.gz + d.py.lpc - 1) / d.py.lpc;
-    tz[i] = (d.gx * d.gy + d.pz.lpc - 1) / d.pz.lpc;
-    for (int k = 0; k < tx[i]; ++k) wx.push_back(make_int2(i, k));
-    for (int k = 0; k < ty[i]; ++k) wy.push_back(make_int2(i, k));
-    for (int k = 0; k < tz[i]; ++k) wz.push_back(make_int2(i, k));
-    b->smx = std::max(b->smx, bulkhost::plan_smem<T>(d.px));
-    b->smy = std::max(b->smy, bulkhost::plan_smem<T>(d.py));
-    b->smz = std::max(b->smz, bulkhost::plan_smem_z<T>(d.pz));
+    const int g = d.gx;
+    return (d.gy == g && d.gz == g && (g == 32 || g == 64 || g == 128 || g == 256)) ? g : 0;
+  };
+  for (int cn : {32, 64, 128, 256, 0}) {
+    adscf_batch::PassClass C;
+    C.n = cn;
+    std::vector<int2> wx, wy, wz;
+    std::vector<int> tx(n, 0), ty(n, 0), tz(n, 0);
+    for (int i : ord) {
+      if (class_of(i) != cn) continue;
+      const BulkDev<T>& d = I[i];
+      const int lx = cn ? BULK_THREADS / reg_tpl(cn) : d.px.lpc;
+      const int ly = cn ? BULK_THREADS / reg_tpl(cn) : d.py.lpc;
+      const int lz = cn ? BULK_THREADS / reg_tpl(cn) : d.pz.lpc;
+      tx[i] = (d.gy * d.gz + lx - 1) / lx;
+      ty[i] = (d.gx * d.gz + ly - 1) / ly;
+      tz[i] = (d.gx * d.gy + lz - 1) / lz;
+      for (int k = 0; k < tx[i]; ++k) wx.push_back(make_int2(i, k));
+      for (int k = 0; k < ty[i]; ++k) wy.push_back(make_int2(i, k));
+      for (int k = 0; k < tz[i]; ++k) wz.push_back(make_int2(i, k));
+      if (cn) {
+        C.smx = C.smy = C.smz = reg_smem<T>(cn);
+      } else {
+        C.smx = std::max(C.smx, bulkhost::plan_smem<T>(d.px));
+        C.smy = std::max(C.smy, bulkhost::plan_smem<T>(d.py));
+        C.smz = std::max(C.smz, bulkhost::plan_smem_z<T>(d.pz));
+      }
+    }
+    if (wx.empty()) continue;
+    C.px.assign(b->maxns + 1, 0); C.py.assign(b->maxns + 1, 0); C.pz.assign(b->maxns + 1, 0);
+    for (int t = 0; t <= b->maxns; ++t)
+      for (int i = 0; i < n; ++i)
+        if (class_of(i) == cn && b->ns[i] >= t) { C.px[t] += tx[i]; C.py[t] += ty[i]; C.pz[t] += tz[i]; }
+    BK(cudaMalloc(&C.wx, wx.size() * sizeof(int2)));
+    BK(cudaMalloc(&C.wy, wy.size() * sizeof(int2)));
+    BK(cudaMalloc(&C.wz, wz.size() * sizeof(int2)));
+    b->cls.push_back(C);   // owns the device lists from here (freed on destroy)
+    BK(cudaMemcpyAsync(C.wx, wx.data(), wx.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(C.wy, wy.data(), wy.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMemcpyAsync(C.wz, wz.data(), wz.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
   }
-  b->pre_x.assign(b->maxns + 1, 0); b->pre_y.assign(b->maxns + 1, 0); b->pre_z.assign(b->maxns + 1, 0);
-  for (int t = 0; t <= b->maxns; ++t)
-    for (int i : ord)
-      if (b->ns[i] >= t) { b->pre_x[t] += tx[i]; b->pre_y[t] += ty[i]; b->pre_z[t] += tz[i]; }
-  BK(cudaMalloc(&b->d_wx, wx.size() * sizeof(int2)));
-  BK(cudaMalloc(&b->d_wy, wy.size() * sizeof(int2)));
-  BK(cudaMalloc(&b->d_wz, wz.size() * sizeof(int2)));
-  BK(cudaMemcpyAsync(b->d_wx, wx.data(), wx.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
-  BK(cudaMemcpyAsync(b->d_wy, wy.data(), wy.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
-  BK(cudaMemcpyAsync(b->d_wz, wz.data(), wz.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+  size_t smmax = 0;
+  for (const auto& C : b->cls) smmax = std::max(smmax, std::max(C.smx, std::max(C.smy, C.smz)));
   int optin = 0;
   BK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev));
-  if (std::max(b->smx, std::max(b->smy, b->smz)) > (size_t)optin)
-    return berr(b, ADSCF_E_ARG, "grid line too long for shared memory");
-  // this translation unit's instances of the generic passes (own device module)
+  if (smmax > (size_t)optin) return berr(b, ADSCF_E_ARG, "grid line too long for shared memory");
+  // this translation unit's instances of the pass kernels (own device module)
   BK(cudaFuncSetAttribute(k_bulk_xpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
   BK(cudaFuncSetAttribute(k_bulk_strided<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+#define ADSCF_BATTR(NN)                                                                                   \
+  BK(cudaFuncSetAttribute(k_rx<T, NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));              \
+  BK(cudaFuncSetAttribute(k_rs<T, NN, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));           \
+  BK(cudaFuncSetAttribute(k_rs<T, NN, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));           \
+  BK(cudaFuncSetAttribute(k_rs<T, NN, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  ADSCF_BATTR(32) ADSCF_BATTR(64) ADSCF_BATTR(128) ADSCF_BATTR(256)
+#undef ADSCF_BATTR
   BK(cudaStreamSynchronize(b->stream));
   return ADSCF_OK;
 }
@@ -476,12 +530,44 @@ int enqueue_iteration(adscf_batch* b) {
   const T* fk = static_cast<const T*>(b->d_fk);
   cudaStream_t s = b->stream;
   const XAux none{nullptr, nullptr, nullptr};
-  k_bulk_xpass<T><<<b->pre_x[0], BULK_THREADS, b->smx, s>>>(d, b->d_wx, tw, 0, XM_INIT, none);
+  const double* g64 = b->d_g64;
+  // one launch per kernel class and pass; a class with no instance left on
+  // its contour at step t launches nothing
+  auto xpass = [&](const adscf_batch::PassClass& C, int grid, int t, int mode) {
+    if (grid <= 0) return;
+    switch (C.n) {
+      case 32: k_rx<T, 32><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
+      case 64: k_rx<T, 64><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
+      case 128: k_rx<T, 128><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
+      case 256: k_rx<T, 256><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
+      default: k_bulk_xpass<T><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none);
+    }
+  };
+  auto spass = [&](const adscf_batch::PassClass& C, int t, int kind) {
+    const bool z = kind == 2;
+    const int grid = z ? C.pz[t] : C.py[t];
+    const int2* w = z ? C.wz : C.wy;
+    const size_t sm = z ? C.smz : C.smy;
+    if (grid <= 0) return;
+#define ADSCF_BS(NN)                                                                              \
+  if (kind == 0) k_rs<T, NN, 0><<<grid, BULK_THREADS, sm, s>>>(d, w, tw, fk, nullptr, g64, t);     \
+  else if (kind == 1) k_rs<T, NN, 1><<<grid, BULK_THREADS, sm, s>>>(d, w, tw, fk, nullptr, g64, t); \
+  else k_rs<T, NN, 2><<<grid, BULK_THREADS, sm, s>>>(d, w, tw, fk, nullptr, g64, t);
+    switch (C.n) {
+      case 32: ADSCF_BS(32) break;
+      case 64: ADSCF_BS(64) break;
+      case 128: ADSCF_BS(128) break;
+      case 256: ADSCF_BS(256) break;
+      default: k_bulk_strided<T><<<grid, BULK_THREADS, sm, s>>>(d, w, tw, fk, nullptr, g64, t, kind);
+    }
+#undef ADSCF_BS
+  };
+  for (const auto& C : b->cls) xpass(C, C.px[0], 0, XM_INIT);
   for (int t = 1; t <= b->maxns; ++t) {
-    k_bulk_strided<T><<<b->pre_y[t], BULK_THREADS, b->smy, s>>>(d, b->d_wy, tw, fk, nullptr, b->d_g64, t, 0);
-    k_bulk_strided<T><<<b->pre_z[t], BULK_THREADS, b->smz, s>>>(d, b->d_wz, tw, fk, nullptr, b->d_g64, t, 2);
-    k_bulk_strided<T><<<b->pre_y[t], BULK_THREADS, b->smy, s>>>(d, b->d_wy, tw, fk, nullptr, b->d_g64, t, 1);
-    k_bulk_xpass<T><<<b->pre_x[t], BULK_THREADS, b->smx, s>>>(d, b->d_wx, tw, t, XM_STEP, none);
+    for (const auto& C : b->cls) spass(C, t, 0);
+    for (const auto& C : b->cls) spass(C, t, 2);
+    for (const auto& C : b->cls) spass(C, t, 1);
+    for (const auto& C : b->cls) xpass(C, C.px[t], t, XM_STEP);
   }
   k_bulk_contour<T><<<dim3(b->cont_blocks, b->n), BULK_THREADS, 0, s>>>(d);
   k_closure_b<<<dim3(b->clos_grid, b->n), SCF_THREADS, 0, s>>>(b->d_S, CL_MEANFIELD | CL_MIXDOTS);
@@ -647,7 +733,7 @@ int adscf_batch_destroy(adscf_batch* b) {
   if (b->g_iter) cudaGraphExecDestroy(b->g_iter);
   cudaFree(b->pool); cudaFree(b->d_inst); cudaFree(b->d_S);
   cudaFree(b->d_tw); cudaFree(b->d_fk); cudaFree(b->d_g64);
-  cudaFree(b->d_wx); cudaFree(b->d_wy); cudaFree(b->d_wz);
+  for (auto& C : b->cls) { cudaFree(C.wx); cudaFree(C.wy); cudaFree(C.wz); }
   cudaFree(b->d_f32); cudaFree(b->d_f64); cudaFree(b->d_list32); cudaFree(b->d_list64);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
@@ -716,7 +802,12 @@ int adscf_batch_results(adscf_batch* b, adscf_iter_result* out) {
 int adscf_batch_launches(const adscf_batch* b) {
   if (!b) return -1;
   if (b->film) return 2 * ((b->n32 > 0) + (b->n64 > 0)) + 3;
-  return 1 + 4 * b->maxns + 4;
+  int k = 4;   // contour, closure, solve, mix
+  for (const auto& C : b->cls) {
+    k += C.px[0] > 0;
+    for (int t = 1; t <= b->maxns; ++t) k += 2 * (C.py[t] > 0) + (C.pz[t] > 0) + (C.px[t] > 0);
+  }
+  return k;
 }
 
 }  // extern "C"

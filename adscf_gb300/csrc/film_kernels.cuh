@@ -352,14 +352,17 @@ k_film1d_chains_b(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__ 
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nf) return;
   const int f = films[k];
-  const ScfDev& S = Ss[f];
-  const double* field = S.hx + (size_t)((*S.iter) % S.slots) * ((size_t)S.ntypes * S.npts);
-  film1d_chain<T>(Fs[f], field, 0, blockIdx.y);
+  // by value: the sweep's stores could alias a struct read through a pointer,
+  // which would force a reload of every field pointer per point
+  const FilmDev<T> F = Fs[f];
+  const double* field = Ss[f].hx + (size_t)((*Ss[f].iter) % Ss[f].slots) * ((size_t)Ss[f].ntypes * Ss[f].npts);
+  film1d_chain<T>(F, field, 0, blockIdx.y);
 }
 
 // one block per film of the list
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_film_contour_b(const FilmDev<T>* __restrict__ Fs, const int* __restrict__ films) {
-  film_contour_body<T>(Fs[films[blockIdx.x]], 0, 1);
+  const FilmDev<T> F = Fs[films[blockIdx.x]];
+  film_contour_body<T>(F, 0, 1);
 }

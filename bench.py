@@ -230,6 +230,111 @@ def run_reference(args):
     return 0
 
 
+# --------------------------------------------------------------------------
+# batch workloads (reported beside the headline): C2 films and C5 bulk scan
+# --------------------------------------------------------------------------
+def c2_films(A, n=4096, seed=2, prec=None):
+    """4096 symmetric diblock films: nz ~ U{64..192} tanh-clustered (2.0),
+    D ~ U[2, 8], f = 0.5, chiN = 20, kappa = 25, h_A ~ U[-1, 1] as the
+    amplitude of the wall potential on A, Ns ~ U{100..300} end-refined
+    (half-cosine) steps, fields N(0, 0.05^2); the grand-canonical ensemble,
+    mu = 2.55 and lambda mixing 0.2 of the reference's Film_1D deck; split
+    precision."""
+    from adscf_gb300 import mesh
+    rng = np.random.default_rng(seed)
+    inst, fields = [], []
+    for _ in range(n):
+        gz = int(rng.integers(64, 193))
+        D = float(rng.uniform(2.0, 8.0))
+        dz, zr = mesh.tanh_mesh(gz, D, 2.0)
+        ns = int(rng.integers(100, 301))
+        ns += ns % 2
+        dss = mesh.contour_steps(ns, ds_scheme=1)
+        h = float(rng.uniform(-1.0, 1.0))
+        ext = mesh.wall_potential(zr, D, 0.4, (h, 0.0))
+        inst.append(dict(geometry=A.FILM_1D, grid=(1, 1, gz), size=(1.0, 1.0, D), dz=dz, dss=dss,
+                         n_a=ns // 2, block_length=(0.5, 0.5), chi=20.0, kappa=25.0,
+                         ext_potential=ext, int_scheme=1, int_span=1, ensemble=2, mu=2.55,
+                         precision=A.SPLIT if prec is None else prec,
+                         mixing_type=A.MIX_LAMBDA, lam=0.2))
+        w = rng.normal(0.0, 0.05, (2, gz + 1))
+        w[:, 0] = w[:, -1] = 0.0
+        fields.append(w.reshape(2, gz + 1, 1, 1))
+    return inst, fields
+
+
+def c5_bulk(A, n=256, seed=5, prec=None):
+    """256 diblock melts: cubic grids from {24, 32, 40, 48, 64}^3, f_A ~
+    U[0.25, 0.45], chiN ~ U[15, 30], L ~ U[3, 5], Ns ~ U{100..200} (ds =
+    1/Ns), fields +-0.5 chiN (0.5 - f_A) cos(2 pi x / L) + N(0, 0.1^2);
+    Anderson m = 10 after 10 lambda = 0.1 steps; split precision."""
+    rng = np.random.default_rng(seed)
+    inst, fields = [], []
+    for _ in range(n):
+        g = int(rng.choice([24, 32, 40, 48, 64]))
+        f = float(rng.uniform(0.25, 0.45))
+        chi = float(rng.uniform(15.0, 30.0))
+        L_ = float(rng.uniform(3.0, 5.0))
+        ns = int(rng.integers(100, 201))
+        inst.append(dict(geometry=A.BULK, grid=(g, g, g), size=(L_, L_, L_), ds=1.0 / ns,
+                         block_length=(round(f * ns) / ns, 1.0 - round(f * ns) / ns), chi=chi,
+                         kappa=25.0, precision=A.SPLIT if prec is None else prec,
+                         mixing_type=A.MIX_ANDERSON, mixing_dim=10, lam=0.1, lam_warm=0.1,
+                         warm_iters=10))
+        x = np.arange(g) * L_ / g
+        s = np.broadcast_to(np.cos(2 * np.pi * x / L_)[None, None, :], (g, g, g))
+        a = 0.5 * chi * (0.5 - f)
+        fields.append(np.stack([a * s, -a * s]) + rng.normal(0.0, 0.1, (2, g, g, g)))
+    return inst, fields
+
+
+def time_batch(torch, A, inst, fields, stream, steps, warmup):
+    """Batch iterations/s over `steps` graph replays after `warmup`."""
+    with A.Batch(inst) as b:
+        b.set_fields(fields)
+        b._ck(b.lib.adscf_batch_set_stream(b.h, stream.cuda_stream))
+        b._ck(b.lib.adscf_batch_enqueue(b.h, warmup))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b._ck(b.lib.adscf_batch_enqueue(b.h, steps))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res = (A._lib.IterResult * b.n)()
+        b.lib.adscf_batch_results(b.h, res)   # status per instance, read below
+        launches = b.lib.adscf_batch_launches(b.h)
+    ms = e0.elapsed_time(e1) / steps
+    bad = sum(1 for r in res if r.status != 0)
+    return ms, launches, bad
+
+
+def batch_legs(torch, A, stream, args):
+    out = {}
+    inst, fields = c2_films(A)
+    ms, launches, bad = time_batch(torch, A, inst, fields, stream, args.batch_steps, 3)
+    pts_steps = sum(2 * len(k["dss"]) * (k["grid"][2] + 1) for k in inst)   # both chains
+    out["film_batch"] = {
+        "workload": "C2: 4096 Film_1D diblock films, nz 64-192 tanh meshes, D 2-8, Ns 100-300 "
+                    "end-refined, h_A in [-1,1], grand canonical mu=2.55, split precision, "
+                    "lambda mixing 0.2",
+        "films": len(inst), "ms_per_iter": ms, "iter_s": 1000.0 / ms,
+        "film_iter_s": len(inst) * 1000.0 / ms,
+        "line_solves_s": 2 * len(inst) * sum(len(k["dss"]) - 1 for k in inst) / len(inst) * 1000.0 / ms,
+        "point_steps_s": pts_steps * 1000.0 / ms,
+        "launches_per_iter": launches, "nonfinite_instances": bad}
+    inst, fields = c5_bulk(A)
+    ms, launches, bad = time_batch(torch, A, inst, fields, stream, args.batch_steps, 3)
+    steps = sum(2 * round(1.0 / k["ds"]) for k in inst)
+    out["bulk_batch"] = {
+        "workload": "C5: 256 bulk diblock instances, grids {24,32,40,48,64}^3, f_A 0.25-0.45, "
+                    "chiN 15-30, L 3-5, Ns 100-200, split precision, Anderson m=10",
+        "instances": len(inst), "ms_per_iter": ms, "iter_s": 1000.0 / ms,
+        "instance_iter_s": len(inst) * 1000.0 / ms, "contour_steps_s": steps * 1000.0 / ms,
+        "launches_per_iter": launches, "nonfinite_instances": bad}
+    return out
+
+
 def run_profile():
     """One SCF iteration's stages at 128^3, ds = 0.05 (20 contour steps, 340 MB
     of slices) on the split path: the kernels of the bench, few launches."""
@@ -258,6 +363,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-batches", action="store_true", help="skip the C2 / C5 batch legs")
+    ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--saddle-iters", type=int, default=800,
                     help="split-path iterations toward the saddle for the converged parity")
     ap.add_argument("--profile", action="store_true",
@@ -410,6 +517,8 @@ def main():
                 "d2h_bytes_per_step": 2 * nv * 8 + 13 * 8,
                 "api": "adscf_scf_iteration (host field in/out, host density out)"},
     }
+    if not args.no_batches:
+        out.update(batch_legs(torch, A, stream, args))
     if rank == 0 and world == 1 and not args.no_cpu:
         t_iter, t_wall = cpu_sample(24, 1)
         out["cpu_baseline"] = {

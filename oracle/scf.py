@@ -45,7 +45,7 @@ def bulk_scf(field, n_iter, grid, size, ds, block_length, kappa, chi,
 
 def film_scf(field, n_iter, dz, dss, n_a, step, kappa, chi, surface, sizes,
              int_scheme=1, span="full", mixing_type=2, lam=0.1, m=2,
-             lam00=1.0e-3, warm=None, rho=1.0, density0=None, gram=True):
+             lam00=1.0e-3, warm=None, rho=1.0, density0=None, gram=True, ensemble=1, mu=0.0):
     """Film SCF loop, Film_CK_AD/Film_1D/Main_Diblock_Melt/main_diblock_melt.f90:
     155-169: densities (film Propagate_Diblock), Check_Accuracy over all
     planes, Calculate_Mean_Ext_Fields with the wall potential ``surface``
@@ -64,7 +64,8 @@ def film_scf(field, n_iter, dz, dss, n_a, step, kappa, chi, surface, sizes,
     hist = []
     for it in range(1, n_iter + 1):
         r = film.film_propagate_diblock(field, dz, dss, n_a, step, rho=rho, dx=dx, dy=dy,
-                                        int_scheme=int_scheme, span=span, sizes=sizes)
+                                        int_scheme=int_scheme, span=span, sizes=sizes,
+                                        ensemble=ensemble, mu=mu)
         newdensity = r["density"]
         acc = interactions.check_accuracy(density, newdensity)
         newfield = interactions.mean_fields(newdensity, kappa, chi, surface=surface[ext])
