@@ -1,6 +1,11 @@
 // bulk.cu -- plans, tables and launch sequences of the bulk propagator.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
 #include <vector>
 
 #include "internal.h"
@@ -183,6 +188,9 @@ int setup_tma(adscf_ctx* ctx, void* spec) {
 }
 
 template <typename T>
+int tune_t(adscf_ctx* ctx);
+
+template <typename T>
 int create_t(adscf_ctx* ctx) {
   BulkDev<T> I{};
   I.gx = ctx->gx; I.gy = ctx->gy; I.gz = ctx->gz;
@@ -292,70 +300,184 @@ int create_t(adscf_ctx* ctx) {
   CK(cudaMalloc(&ctx->d_inst, sizeof(BulkDev<T>)));
   CK(cudaMemcpy(ctx->d_inst, &I, sizeof(I), cudaMemcpyHostToDevice));
   hb<T>(ctx) = I;
+  // default plan: the most specialised kernel available for each pass
+  ctx->plan_y = ctx->plan_z = ctx->tma ? PK_TMA : ctx->pgrid_y ? PK_PERSISTENT : PK_PLAIN;
+  ctx->plan_x = ctx->pgrid_x ? PK_PERSISTENT : PK_PLAIN;
+  if (ctx->autotune) return tune_t<T>(ctx);
   return ADSCF_OK;
 }
 
+// One double step t: Yf, Z, Yi, X with the kernel the pass plan names for
+// each pass (PK_PLAIN: one CTA per tile; PK_PERSISTENT: resident grid with
+// register prefetch; PK_TMA: TMA-fed tiles, FP32 64/128).  Every choice does
+// the same arithmetic on the same natural-order spectrum.
 template <typename T>
-int chains_t(adscf_ctx* ctx) {
+int expfield_t(adscf_ctx* ctx, const double* d_w);
+
+template <typename T, int NN>
+void step_nn(adscf_ctx* ctx, int t) {
   const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
   const cplx<T>* tw = static_cast<const cplx<T>*>(ctx->d_tw);
   const T* fk = static_cast<const T*>(ctx->d_fk);
   const double2* tw64 = static_cast<const double2*>(ctx->d_tw64);
   const double* g64 = ctx->d_g64;
   cudaStream_t s = ctx->stream;
-  XAux none{nullptr, nullptr, nullptr};
-  launch_x<T>(ctx, 0, XM_INIT, none);
-  if constexpr (sizeof(T) == 4) {
-    if (ctx->tma) {
-      const BulkDev<float>* df = reinterpret_cast<const BulkDev<float>*>(ctx->d_inst);
-      const float2* twf = reinterpret_cast<const float2*>(tw);
-      const float* fkf = reinterpret_cast<const float*>(fk);
-      const double* g64 = ctx->d_g64;
-      const size_t sm = ctx->tma_smem;
-      const int gy_ = std::min(ctx->tma_grid, ctx->tma_tiles_y);
-      const int gz_ = std::min(ctx->tma_grid, ctx->tma_tiles_z);
-      // the x pass stays on the register-prefetch persistent kernel: its rows are
-      // contiguous, and a bulk-copy-fed variant measured slower (31 us vs 27 us at 128^3)
-#define ADSCF_TSTEP(NN)                                                                               \
-  for (int t = 1; t <= ctx->ns; ++t) {                                                                \
-    k_rs_tma<NN, 0><<<gy_, BULK_THREADS, sm, s>>>(df, ctx->tmap_y, ctx->tma_tiles_y, twf, fkf, g64, t, ctx->d_flags); \
-    k_rs_tma<NN, 2><<<gz_, BULK_THREADS, sm, s>>>(df, ctx->tmap_z, ctx->tma_tiles_z, twf, fkf, g64, t, ctx->d_flags); \
-    k_rs_tma<NN, 1><<<gy_, BULK_THREADS, sm, s>>>(df, ctx->tmap_y, ctx->tma_tiles_y, twf, fkf, g64, t, ctx->d_flags); \
-    k_rx_p<float, NN><<<ctx->pgrid_x, BULK_THREADS, ctx->smem_x, s>>>(df, ctx->n_work_x, twf, t);   \
-  }
-      if (ctx->tma == 64) { ADSCF_TSTEP(64) } else { ADSCF_TSTEP(128) }
-#undef ADSCF_TSTEP
-      CK(cudaGetLastError());
-      return ADSCF_OK;
+  const size_t sm = ctx->smem_x;
+  auto spass = [&](int kind) {
+    const int pk = kind == 2 ? ctx->plan_z : ctx->plan_y;
+    if constexpr (sizeof(T) == 4 && (NN == 64 || NN == 128)) {
+      if (pk == PK_TMA) {
+        const BulkDev<float>* df = reinterpret_cast<const BulkDev<float>*>(d);
+        const float2* twf = reinterpret_cast<const float2*>(tw);
+        const float* fkf = reinterpret_cast<const float*>(fk);
+        const bool z = kind == 2;
+        const int tiles = z ? ctx->tma_tiles_z : ctx->tma_tiles_y;
+        const int grid = std::min(ctx->tma_grid, tiles);
+        const CUtensorMap& map = z ? ctx->tmap_z : ctx->tmap_y;
+        if (kind == 0) k_rs_tma<NN, 0><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, ctx->d_flags);
+        else if (kind == 1) k_rs_tma<NN, 1><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, ctx->d_flags);
+        else k_rs_tma<NN, 2><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, ctx->d_flags);
+        return;
+      }
     }
-  }
-  if (ctx->pgrid_x) {
-    const double2* tw64 = static_cast<const double2*>(ctx->d_tw64);
-    const double* g64 = ctx->d_g64;
-    const size_t sm = ctx->smem_x;
-#define ADSCF_PSTEP(NN)                                                                          \
-  for (int t = 1; t <= ctx->ns; ++t) {                                                           \
-    k_rs_p<T, NN, 0><<<ctx->pgrid_y, BULK_THREADS, sm, s>>>(d, ctx->n_work_y, tw, fk, tw64, g64, t); \
-    k_rs_p<T, NN, 2><<<ctx->pgrid_z, BULK_THREADS, sm, s>>>(d, ctx->n_work_z, tw, fk, tw64, g64, t); \
-    k_rs_p<T, NN, 1><<<ctx->pgrid_y, BULK_THREADS, sm, s>>>(d, ctx->n_work_y, tw, fk, tw64, g64, t); \
-    k_rx_p<T, NN><<<ctx->pgrid_x, BULK_THREADS, sm, s>>>(d, ctx->n_work_x, tw, t);              \
-  }
-    switch (ctx->regx) {
-      case 32: ADSCF_PSTEP(32) break;
-      case 64: ADSCF_PSTEP(64) break;
-      case 128: ADSCF_PSTEP(128) break;
-      case 256: ADSCF_PSTEP(256) break;
+    if (pk == PK_PERSISTENT) {
+      if (kind == 0) k_rs_p<T, NN, 0><<<ctx->pgrid_y, BULK_THREADS, sm, s>>>(d, ctx->n_work_y, tw, fk, tw64, g64, t);
+      else if (kind == 1) k_rs_p<T, NN, 1><<<ctx->pgrid_y, BULK_THREADS, sm, s>>>(d, ctx->n_work_y, tw, fk, tw64, g64, t);
+      else k_rs_p<T, NN, 2><<<ctx->pgrid_z, BULK_THREADS, sm, s>>>(d, ctx->n_work_z, tw, fk, tw64, g64, t);
+      return;
     }
-#undef ADSCF_PSTEP
+    launch_s<T>(ctx, t, kind);
+  };
+  spass(0);
+  spass(2);
+  spass(1);
+  if (ctx->plan_x == PK_PERSISTENT) {
+    k_rx_p<T, NN><<<ctx->pgrid_x, BULK_THREADS, sm, s>>>(d, ctx->n_work_x, tw, t);
   } else {
-    for (int t = 1; t <= ctx->ns; ++t) {
+    const XAux none{nullptr, nullptr, nullptr};
+    launch_x<T>(ctx, t, XM_STEP, none);
+  }
+}
+
+template <typename T>
+void step_t(adscf_ctx* ctx, int t) {
+  // persistent and TMA passes need one register line length on all axes
+  const int nn = (ctx->regx && ctx->regx == ctx->regy && ctx->regx == ctx->regz) ? ctx->regx : 0;
+  switch (nn) {
+    case 32: step_nn<T, 32>(ctx, t); break;
+    case 64: step_nn<T, 64>(ctx, t); break;
+    case 128: step_nn<T, 128>(ctx, t); break;
+    case 256: step_nn<T, 256>(ctx, t); break;
+    default: {
+      const XAux none{nullptr, nullptr, nullptr};
       launch_s<T>(ctx, t, 0);
       launch_s<T>(ctx, t, 2);
       launch_s<T>(ctx, t, 1);
       launch_x<T>(ctx, t, XM_STEP, none);
     }
   }
+}
+
+template <typename T>
+int chains_t(adscf_ctx* ctx) {
+  const XAux none{nullptr, nullptr, nullptr};
+  launch_x<T>(ctx, 0, XM_INIT, none);
+  for (int t = 1; t <= ctx->ns; ++t) step_t<T>(ctx, t);
   CK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: time every available pass plan on this context's buffers and
+// keep the fastest.  Candidates per pass: Y and Z {plain, persistent, TMA},
+// X {plain, persistent}, as the shape and precision allow.  Each candidate
+// runs a few double steps (after two warm-up steps) on unit Boltzmann
+// factors, twice, timed with CUDA events on the context stream; the minimum
+// per-step time decides.  Plans are cached per (device, grid, precision), so
+// contexts of a shape already seen reuse the choice.
+// ---------------------------------------------------------------------------
+struct TuneKey {
+  int dev, gx, gy, gz, prec, avail;   // avail: bit set of the kernels this context can run
+  bool operator<(const TuneKey& o) const {
+    return std::tie(dev, gx, gy, gz, prec, avail) < std::tie(o.dev, o.gx, o.gy, o.gz, o.prec, o.avail);
+  }
+};
+struct TuneVal {
+  int y, z, x;
+  std::string report;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune;
+
+const char* pk_name(int k) { return k == PK_TMA ? "tma" : k == PK_PERSISTENT ? "persistent" : "plain"; }
+
+template <typename T>
+int tune_t(adscf_ctx* ctx) {
+  const int avail = (ctx->tma ? 1 : 0) | (ctx->pgrid_y ? 2 : 0) | (ctx->pgrid_x ? 4 : 0) |
+                    (ctx->use_generic ? 8 : 0);
+  const TuneKey key{ctx->dev, ctx->gx, ctx->gy, ctx->gz, ctx->prec, avail};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      ctx->plan_y = it->second.y; ctx->plan_z = it->second.z; ctx->plan_x = it->second.x;
+      ctx->tune_report = it->second.report + " (cached)";
+      return ADSCF_OK;
+    }
+  }
+  std::vector<int> ys = {PK_PLAIN}, xs = {PK_PLAIN};
+  if (ctx->pgrid_y) ys.push_back(PK_PERSISTENT);
+  if (ctx->tma) ys.push_back(PK_TMA);
+  if (ctx->pgrid_x) xs.push_back(PK_PERSISTENT);
+  const std::vector<int>& zs = ys;
+  if (ys.size() * xs.size() == 1) return ADSCF_OK;
+  // unit Boltzmann factors from a zero field; the slice buffer takes the steps
+  CK(cudaMemsetAsync(ctx->d_tmp, 0, 2 * (size_t)ctx->npts * sizeof(double), ctx->stream));
+  int rc = expfield_t<T>(ctx, ctx->d_tmp);
+  if (rc) return rc;
+  const XAux none{nullptr, nullptr, nullptr};
+  launch_x<T>(ctx, 0, XM_INIT, none);
+  const int steps = std::min(ctx->ns, 6);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  struct Cand { int y, z, x; float us; };
+  std::vector<Cand> cands;
+  for (int y : ys)
+    for (int z : zs)
+      for (int x : xs) cands.push_back({y, z, x, 1e30f});
+  for (int round = 0; round < 2; ++round) {
+    for (Cand& c : cands) {
+      ctx->plan_y = c.y; ctx->plan_z = c.z; ctx->plan_x = c.x;
+      step_t<T>(ctx, 1);
+      step_t<T>(ctx, 2 <= ctx->ns ? 2 : 1);
+      cudaEventRecord(e0, ctx->stream);
+      for (int t = 1; t <= steps; ++t) step_t<T>(ctx, t);
+      cudaEventRecord(e1, ctx->stream);
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      c.us = std::min(c.us, 1000.f * ms / steps);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaGetLastError());
+  const Cand* best = &cands[0];
+  for (const Cand& c : cands)
+    if (c.us < best->us) best = &c;
+  ctx->plan_y = best->y; ctx->plan_z = best->z; ctx->plan_x = best->x;
+  char line[160];
+  std::snprintf(line, sizeof(line), "y=%s z=%s x=%s %.2f us/double step;", pk_name(best->y),
+                pk_name(best->z), pk_name(best->x), best->us);
+  std::string rep = line;
+  for (const Cand& c : cands) {
+    std::snprintf(line, sizeof(line), " %s/%s/%s %.2f", pk_name(c.y), pk_name(c.z), pk_name(c.x), c.us);
+    rep += line;
+  }
+  ctx->tune_report = rep;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = TuneVal{best->y, best->z, best->x, rep};
   return ADSCF_OK;
 }
 

@@ -206,6 +206,10 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
   ctx->use_generic = std::getenv("ADSCF_GENERIC_FFT") != nullptr;
   ctx->no_persistent = std::getenv("ADSCF_NO_PERSISTENT") != nullptr;
   ctx->no_tma = std::getenv("ADSCF_NO_TMA") != nullptr;
+  {
+    const char* at = std::getenv("ADSCF_AUTOTUNE");
+    ctx->autotune = !(at && at[0] == '0');
+  }
   ctx->gx = p->gx; ctx->gy = p->gy; ctx->gz = p->gz;
   ctx->nplanes = p->geometry == ADSCF_BULK ? p->gz : p->gz + 1;
   ctx->npts = p->gx * p->gy * ctx->nplanes;
@@ -595,6 +599,29 @@ int adscf_set_stream(adscf_ctx* ctx, void* stream) {
   if (!ctx) return ADSCF_E_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return ADSCF_OK;
+}
+
+int adscf_tuning(const adscf_ctx* ctx, char* buf, int len) {
+  if (!ctx || !buf || len < 1) return ADSCF_E_ARG;
+  char plan[96];
+  std::snprintf(plan, sizeof(plan), "plan y=%d z=%d x=%d; ", ctx->plan_y, ctx->plan_z, ctx->plan_x);
+  const std::string s = std::string(plan) + (ctx->tune_report.empty() ? "not tuned" : ctx->tune_report);
+  std::snprintf(buf, (size_t)len, "%s", s.c_str());
+  return ADSCF_OK;
+}
+
+int adscf_set_pass_plan(adscf_ctx* ctx, int y, int z, int x) {
+  if (!ctx) return ADSCF_E_ARG;
+  if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "pass plans are for bulk contexts");
+  auto ok_yz = [&](int k) {
+    return k == ADSCF_PASS_PLAIN || (k == ADSCF_PASS_PERSISTENT && ctx->pgrid_y) || (k == ADSCF_PASS_TMA && ctx->tma);
+  };
+  const bool ok_x = x == ADSCF_PASS_PLAIN || (x == ADSCF_PASS_PERSISTENT && ctx->pgrid_x);
+  if (!ok_yz(y) || !ok_yz(z) || !ok_x) return set_err(ctx, ADSCF_E_ARG, "pass kernel not available for this shape");
+  ctx->plan_y = y; ctx->plan_z = z; ctx->plan_x = x;
+  if (ctx->g_iter) { cudaGraphExecDestroy(ctx->g_iter); ctx->g_iter = nullptr; }
+  if (ctx->g_prop) { cudaGraphExecDestroy(ctx->g_prop); ctx->g_prop = nullptr; }
   return ADSCF_OK;
 }
 

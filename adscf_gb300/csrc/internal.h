@@ -10,6 +10,8 @@
 #include "scf_kernels.cuh"
 
 struct FilmState;  // film / brush device state (film.cu)
+// pass kernels of a bulk double step
+enum { PK_PLAIN = 0, PK_PERSISTENT = 1, PK_TMA = 2 };
 struct AdjState;   // adjoint buffers and work lists (adjoint.cu)
 
 struct adscf_ctx {
@@ -50,6 +52,10 @@ struct adscf_ctx {
   int tma_tiles_y = 0, tma_tiles_z = 0, tma_grid = 0;
   size_t tma_smem = 0;
   int* d_flags = nullptr;             // device error flags (bounded-wait expiry)
+  // kernel per pass of a double step (PK_*), chosen by the autotuner
+  int plan_y = PK_PLAIN, plan_z = PK_PLAIN, plan_x = PK_PLAIN;
+  int autotune = 1;
+  std::string tune_report;
   int contour_blocks = 0;
 
   // ---- SCF state (FP64)

@@ -212,6 +212,17 @@ class Context:
         self._ck(self.lib.adscf_scf_run(self.h, int(n_iter), float(tol), C.byref(res)))
         return res
 
+    # -- pass-kernel autotuner (bulk) ---------------------------------------
+    def tuning(self):
+        """Chosen pass plan and the autotuner's per-candidate timings."""
+        buf = C.create_string_buffer(2048)
+        self._ck(self.lib.adscf_tuning(self.h, buf, len(buf)))
+        return buf.value.decode()
+
+    def set_pass_plan(self, y, z, x):
+        """Pin the kernel of the Y, Z and X passes (0 plain, 1 persistent, 2 TMA)."""
+        self._ck(self.lib.adscf_set_pass_plan(self.h, int(y), int(z), int(x)))
+
     # -- differentiation (FP64 bulk) ----------------------------------------
     def forward(self, field):
         """Free energy per chain at `field` [2][npts], no mixing; keeps the

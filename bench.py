@@ -443,6 +443,7 @@ def main():
         ms_total = float(t.item())
     ms_step = ms_total / args.steps
     launches_per_step = lib.adscf_stage_launches(ctx.h, L_.STAGE_ITERATION)
+    pass_plan = ctx.tuning()
 
     # ---- stage breakdown (CUDA events on the launching stream) ------------
     ns = ctx.ns
@@ -511,6 +512,7 @@ def main():
                                        "(--cache-control none; Boltzmann factors and spectrum "
                                        "stay in L2, only the slice store reaches DRAM)",
                      "contour_GBs": alg_contour / (t_cont * 1e-3) / 1e9},
+        "pass_plan": pass_plan,
         "clocks": clk,
         "gpu_launches": launches_per_step * args.steps,
         "e2e": {"value": world / e2e_s, "unit": "iter/s", "h2d_bytes_per_step": nv * 8,

@@ -225,3 +225,31 @@ def test_split_64cube_against_oracle(rng):
         dens, res = c.propagate_diblock(field)
     assert abs(np.log(res.Qsum) - np.log(ref["Qsum"])) < 1e-6
     assert np.max(np.abs(dens - ob.density_by_type(ref["density"]))) < 1e-5
+
+
+@pytest.mark.parametrize("n,prec", [(64, SPLIT), (128, SPLIT), (64, FP64), (32, FP64)])
+def test_every_pass_plan_gives_identical_results(n, prec, rng):
+    """The autotuner may pick any available kernel per pass (plain,
+    persistent, TMA); all compute the same arithmetic, bit for bit."""
+    from adscf_gb300 import AdscfError
+    grid, size, ds = (n, n, n), (3.8, 3.8, 3.8), 0.05
+    field = 0.5 * rng.standard_normal((2, n, n, n))
+    ref = None
+    tried = 0
+    with mkctx(grid, size, ds, prec, f=(0.4, 0.6)) as c:
+        assert "plan" in c.tuning()
+        for y in (0, 1, 2):
+            for z in (0, 1, 2):
+                for x in (0, 1):
+                    try:
+                        c.set_pass_plan(y, z, x)
+                    except AdscfError:
+                        continue
+                    d, r = c.propagate_diblock(field)
+                    tried += 1
+                    if ref is None:
+                        ref = (d, r.Qsum)
+                    else:
+                        assert r.Qsum == ref[1], (y, z, x)
+                        assert np.array_equal(d, ref[0]), (y, z, x)
+    assert tried >= 4
