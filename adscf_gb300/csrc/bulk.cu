@@ -176,9 +176,15 @@ int setup_tma(adscf_ctx* ctx, void* spec) {
   int nsm = 0, occ = 0;
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rs_tma<NN, 2>, BULK_THREADS, LY::bytes));
+  using LXY = tmak::XYLayout<NN>;
+  CK(cudaFuncSetAttribute(k_xy_tma<NN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LXY::bytes));
+  int occ_xy = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_xy, k_xy_tma<NN>, LXY::THREADS, LXY::bytes));
+  ctx->xy_smem = LXY::bytes;
   ctx->tma_tiles_y = ctx->gx * ctx->gz / LY::LPC;
   ctx->tma_tiles_z = ctx->gx * ctx->gy / LY::LPC;
   ctx->tma_grid = nsm * std::max(1, occ);
+  ctx->xy_grid = std::min(ctx->gz, nsm * std::max(1, occ_xy));
   if (!ctx->d_flags) {
     CK(cudaMalloc(&ctx->d_flags, sizeof(int)));
     CK(cudaMemset(ctx->d_flags, 0, sizeof(int)));
@@ -314,6 +320,15 @@ int create_t(adscf_ctx* ctx) {
 template <typename T>
 int expfield_t(adscf_ctx* ctx, const double* d_w);
 
+// fused XY plane pass of step t (t = 0: the initial plane)
+template <int NN>
+void xy_pass(adscf_ctx* ctx, int t) {
+  const BulkDev<float>* df = static_cast<const BulkDev<float>*>(ctx->d_inst);
+  const float2* twf = static_cast<const float2*>(ctx->d_tw);
+  k_xy_tma<NN><<<ctx->xy_grid, tmak::XYLayout<NN>::THREADS, ctx->xy_smem, ctx->stream>>>(
+      df, ctx->tmap_y, twf, t, ctx->d_flags);
+}
+
 template <typename T, int NN>
 void step_nn(adscf_ctx* ctx, int t) {
   const BulkDev<T>* d = static_cast<const BulkDev<T>*>(ctx->d_inst);
@@ -348,6 +363,13 @@ void step_nn(adscf_ctx* ctx, int t) {
     }
     launch_s<T>(ctx, t, kind);
   };
+  if constexpr (sizeof(T) == 4 && (NN == 64 || NN == 128)) {
+    if (ctx->plan_x == PK_FUSED) {   // Z, then Yi + X + Yf of the next step in one plane pass
+      spass(2);
+      xy_pass<NN>(ctx, t);
+      return;
+    }
+  }
   spass(0);
   spass(2);
   spass(1);
@@ -381,7 +403,13 @@ void step_t(adscf_ctx* ctx, int t) {
 template <typename T>
 int chains_t(adscf_ctx* ctx) {
   const XAux none{nullptr, nullptr, nullptr};
-  launch_x<T>(ctx, 0, XM_INIT, none);
+  if (sizeof(T) == 4 && ctx->plan_x == PK_FUSED) {
+    // the initial plane pass also does Yf of step 1
+    if (ctx->tma == 64) xy_pass<64>(ctx, 0);
+    else xy_pass<128>(ctx, 0);
+  } else {
+    launch_x<T>(ctx, 0, XM_INIT, none);
+  }
   for (int t = 1; t <= ctx->ns; ++t) step_t<T>(ctx, t);
   CK(cudaGetLastError());
   return ADSCF_OK;
@@ -409,7 +437,9 @@ struct TuneVal {
 std::mutex g_tune_mu;
 std::map<TuneKey, TuneVal> g_tune;
 
-const char* pk_name(int k) { return k == PK_TMA ? "tma" : k == PK_PERSISTENT ? "persistent" : "plain"; }
+const char* pk_name(int k) {
+  return k == PK_FUSED ? "fused-xy" : k == PK_TMA ? "tma" : k == PK_PERSISTENT ? "persistent" : "plain";
+}
 
 template <typename T>
 int tune_t(adscf_ctx* ctx) {
@@ -429,6 +459,7 @@ int tune_t(adscf_ctx* ctx) {
   if (ctx->pgrid_y) ys.push_back(PK_PERSISTENT);
   if (ctx->tma) ys.push_back(PK_TMA);
   if (ctx->pgrid_x) xs.push_back(PK_PERSISTENT);
+  if (ctx->tma && ctx->xy_grid) xs.push_back(PK_FUSED);
   const std::vector<int>& zs = ys;
   if (ys.size() * xs.size() == 1) return ADSCF_OK;
   // unit Boltzmann factors from a zero field; the slice buffer takes the steps
@@ -443,9 +474,12 @@ int tune_t(adscf_ctx* ctx) {
   CK(cudaEventCreate(&e1));
   struct Cand { int y, z, x; float us; };
   std::vector<Cand> cands;
-  for (int y : ys)
+  for (int x : xs)
     for (int z : zs)
-      for (int x : xs) cands.push_back({y, z, x, 1e30f});
+      for (int y : ys) {
+        if (x == PK_FUSED && y != ys[0]) continue;   // the fused pass has no separate Y
+        cands.push_back({x == PK_FUSED ? ys.back() : y, z, x, 1e30f});
+      }
   for (int round = 0; round < 2; ++round) {
     for (Cand& c : cands) {
       ctx->plan_y = c.y; ctx->plan_z = c.z; ctx->plan_x = c.x;

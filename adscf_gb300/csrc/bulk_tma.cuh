@@ -242,3 +242,178 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
     tmak::bulk_wait0();
   }
 }
+
+// ---------------------------------------------------------------------------
+// Fused XY pass: one z-plane per CTA, whole plane in shared memory.
+//
+// A 128 x 128 FP32 plane is 128 KB, so the three passes that run inside one
+// plane -- inverse y (Yi of step t), the x pass of step t, and forward y (Yf
+// of step t+1) -- fuse into one kernel: the plane arrives by TMA as N/16
+// swizzled 16-column boxes (the Y pass's tensor map), is transformed in
+// place, and leaves by TMA.  A double step becomes two launches, Z and XY,
+// and the spectrum crosses L2 twice per step instead of four times.
+//   phase 1: inverse y on the N columns (lines of D_out -> D_in)
+//   phase 2: inverse x on the N rows, q_t = E(t) z, slice store,
+//            z = E(t+1) q_t, forward x
+//   phase 3: forward y on the columns
+// t = 0 (initial): slice 0 = (1, 1), z = E(1), forward x, forward y.
+// t = Ns: phase 2 stores the last slice only.  Same arithmetic, element for
+// element, as the separate passes.  The mbarrier wait is bounded (error flag
+// 8); a CTA that gives up drains its copy before returning.
+// ---------------------------------------------------------------------------
+namespace tmak {
+
+template <int N>
+struct XYLayout {
+  using F = RegFFT<float, regk::Cfg<N>::R1, regk::Cfg<N>::TPL>;
+  static constexpr int THREADS = 512;
+  static constexpr int LINES = THREADS / F::TPL;            // lines per round
+  static constexpr int NB = N / kBoxCols;                   // boxes per plane
+  static constexpr int box_elems = N * kBoxCols;
+  static constexpr uint32_t plane_bytes = (uint32_t)N * N * 8;
+  static constexpr size_t sc_off = plane_bytes;             // plane at 0 (1024-aligned)
+  static constexpr size_t tw_off = sc_off + (size_t)LINES * F::LS * sizeof(float2);
+  static constexpr size_t bar_off = ((tw_off + N * sizeof(float2) + 15) / 16) * 16;
+  static constexpr size_t bytes = bar_off + sizeof(uint64_t) + 1024;   // + alignment slack
+  static_assert(N % LINES == 0 || LINES % N == 0, "rounds of whole lines");
+};
+
+// element (row j, column x) of a plane held as N/16 swizzled 16-column boxes
+template <int N>
+__device__ __forceinline__ int plane_at(int j, int x) {
+  return (x >> 4) * (N * kBoxCols) + swz(j, x & 15);
+}
+
+}  // namespace tmak
+
+template <int N>
+__global__ void __launch_bounds__(512, 1)
+k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUtensorMap tmap,
+         const float2* __restrict__ gtw, int t, int* __restrict__ err) {
+  using LY = tmak::XYLayout<N>;
+  using F = typename LY::F;
+  constexpr int R1 = F::R1, TPL = F::TPL, LINES = LY::LINES;
+  extern __shared__ __align__(1024) unsigned char smraw_[];
+  unsigned char* smraw = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smraw_) + 1023) & ~uintptr_t(1023));
+  float2* plane = reinterpret_cast<float2*>(smraw);
+  float2* scr = reinterpret_cast<float2*>(smraw + LY::sc_off);
+  float2* tw = reinterpret_cast<float2*>(smraw + LY::tw_off);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smraw + LY::bar_off);
+  const BulkDev<float>& I = insts[0];
+  if (t > I.ns) return;
+  const bool init = t == 0;
+  const bool more = init || t < I.ns;
+  const int gz = I.gz;
+  if (threadIdx.x == 0) {
+    tmak::mbar_init(bar, 1);
+    tmak::fence_mbar_init();
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[I.px.tw_off + i];
+  __syncthreads();
+  const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
+  const bool active = line < N;          // N = 64 leaves no idle line; kept for clarity
+  float2* sc = scr + line * F::LS;
+  // Boltzmann factor choice: node t of each chain, then node t+1
+  const int tt = init ? 1 : t;
+  const bool fA = tt <= I.na, bA = tt > I.nb;
+  const bool fA2 = (t + 1) <= I.na, bA2 = (t + 1) > I.nb;
+  float2* sl = I.slices + (size_t)t * I.npts;
+  int it = 0, issued = 0, done = 0;
+  for (int z = blockIdx.x; z < gz; z += gridDim.x, ++it) {
+    const size_t pbase = (size_t)z * N * N;
+    if (!init) {
+      if (threadIdx.x == 0) {
+        tmak::bulk_wait_read0();          // the previous plane's stores have read the buffer
+        tmak::mbar_expect_tx(bar, LY::plane_bytes);
+        for (int b = 0; b < LY::NB; ++b)
+          tmak::tma_load_3d(plane + b * LY::box_elems, &tmap, bar, b * tmak::kBoxCols, 0, z);
+        ++issued;
+      }
+      const bool got = tmak::mbar_wait_bounded(bar, (uint32_t)(it & 1), tmak::kWaitPolls);
+      if (!__syncthreads_and(got)) {
+        if (threadIdx.x == 0) atomicOr(err, 8);
+        break;
+      }
+      ++done;
+      // phase 1: inverse y, columns x
+      for (int c0 = 0; c0 < N; c0 += LINES) {
+        const int x = c0 + line;
+        if (active && x < N) {
+          float2 v[R1];
+#pragma unroll
+          for (int r = 0; r < R1; ++r) v[r] = plane[tmak::plane_at<N>(F::out_index(lt, r), x)];
+          F::inverse(v, sc, tw, lt);
+#pragma unroll
+          for (int r = 0; r < R1; ++r) plane[tmak::plane_at<N>(F::in_index(lt, r), x)] = v[r];
+        }
+      }
+      __syncthreads();
+    } else {
+      if (threadIdx.x == 0) tmak::bulk_wait_read0();
+      __syncthreads();
+    }
+    // phase 2: rows j
+    for (int r0 = 0; r0 < N; r0 += LINES) {
+      const int j = r0 + line;
+      if (!(active && j < N)) continue;
+      const size_t rbase = pbase + (size_t)j * N;
+      float2 v[R1];
+      if (!init) {
+#pragma unroll
+        for (int r = 0; r < R1; ++r) v[r] = plane[tmak::plane_at<N>(j, F::out_index(lt, r))];
+        F::inverse(v, sc, tw, lt);
+#pragma unroll
+        for (int m = 0; m < R1; ++m) {
+          const size_t g = rbase + F::in_index(lt, m);
+          const EPt<float> ev = load_ept(I.E, g);
+          const float2 q = make_float2(emul(v[m].x, fA ? ev.a : ev.b, fA ? ev.al : ev.bl),
+                                       emul(v[m].y, bA ? ev.a : ev.b, bA ? ev.al : ev.bl));
+          sl[g] = q;
+          if (more)
+            v[m] = make_float2(emul(q.x, fA2 ? ev.a : ev.b, fA2 ? ev.al : ev.bl),
+                               emul(q.y, bA2 ? ev.a : ev.b, bA2 ? ev.al : ev.bl));
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < R1; ++m) {
+          const size_t g = rbase + F::in_index(lt, m);
+          const EPt<float> ev = load_ept(I.E, g);
+          v[m] = make_float2(fA ? ev.a : ev.b, bA ? ev.a : ev.b);
+          sl[g] = make_float2(1.f, 1.f);
+        }
+      }
+      if (more) {
+        F::forward(v, sc, tw, lt);
+#pragma unroll
+        for (int r = 0; r < R1; ++r) plane[tmak::plane_at<N>(j, F::out_index(lt, r))] = v[r];
+      }
+    }
+    __syncthreads();
+    if (!more) continue;                  // last step: nothing goes back to the spectrum
+    // phase 3: forward y, columns x
+    for (int c0 = 0; c0 < N; c0 += LINES) {
+      const int x = c0 + line;
+      if (active && x < N) {
+        float2 v[R1];
+#pragma unroll
+        for (int r = 0; r < R1; ++r) v[r] = plane[tmak::plane_at<N>(F::in_index(lt, r), x)];
+        F::forward(v, sc, tw, lt);
+#pragma unroll
+        for (int r = 0; r < R1; ++r) plane[tmak::plane_at<N>(F::out_index(lt, r), x)] = v[r];
+      }
+    }
+    tmak::fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int b = 0; b < LY::NB; ++b)
+        tmak::tma_store_3d(&tmap, plane + b * LY::box_elems, b * tmak::kBoxCols, 0, z);
+      tmak::bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) {
+    // a load still in flight after an early exit lands before shared memory is released
+    for (int k = done; k < issued; ++k) tmak::mbar_wait_bounded(bar, (uint32_t)(k & 1), tmak::kWaitPolls);
+    tmak::bulk_wait0();
+  }
+}

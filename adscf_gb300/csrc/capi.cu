@@ -617,7 +617,8 @@ int adscf_set_pass_plan(adscf_ctx* ctx, int y, int z, int x) {
   auto ok_yz = [&](int k) {
     return k == ADSCF_PASS_PLAIN || (k == ADSCF_PASS_PERSISTENT && ctx->pgrid_y) || (k == ADSCF_PASS_TMA && ctx->tma);
   };
-  const bool ok_x = x == ADSCF_PASS_PLAIN || (x == ADSCF_PASS_PERSISTENT && ctx->pgrid_x);
+  const bool ok_x = x == ADSCF_PASS_PLAIN || (x == ADSCF_PASS_PERSISTENT && ctx->pgrid_x) ||
+                    (x == ADSCF_PASS_FUSED && ctx->tma && ctx->xy_grid);
   if (!ok_yz(y) || !ok_yz(z) || !ok_x) return set_err(ctx, ADSCF_E_ARG, "pass kernel not available for this shape");
   ctx->plan_y = y; ctx->plan_z = z; ctx->plan_x = x;
   if (ctx->g_iter) { cudaGraphExecDestroy(ctx->g_iter); ctx->g_iter = nullptr; }
@@ -628,7 +629,7 @@ int adscf_set_pass_plan(adscf_ctx* ctx, int y, int z, int x) {
 int adscf_stage_launches(const adscf_ctx* ctx, int stage) {
   if (!ctx) return -1;
   int prop, contour = 1, update = 3;
-  if (ctx->geometry == ADSCF_BULK) prop = 1 + 4 * ctx->ns;
+  if (ctx->geometry == ADSCF_BULK) prop = 1 + (ctx->plan_x == PK_FUSED ? 2 : 4) * ctx->ns;
   else prop = ctx->film_launches;
   if (ctx->geometry != ADSCF_BULK) contour = ctx->film_contour_launches;
   switch (stage) {

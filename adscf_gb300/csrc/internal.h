@@ -11,7 +11,7 @@
 
 struct FilmState;  // film / brush device state (film.cu)
 // pass kernels of a bulk double step
-enum { PK_PLAIN = 0, PK_PERSISTENT = 1, PK_TMA = 2 };
+enum { PK_PLAIN = 0, PK_PERSISTENT = 1, PK_TMA = 2, PK_FUSED = 3 };
 struct AdjState;   // adjoint buffers and work lists (adjoint.cu)
 
 struct adscf_ctx {
@@ -51,6 +51,8 @@ struct adscf_ctx {
   CUtensorMap tmap_y{}, tmap_z{};
   int tma_tiles_y = 0, tma_tiles_z = 0, tma_grid = 0;
   size_t tma_smem = 0;
+  size_t xy_smem = 0;                 // fused XY plane pass (FP32, gx = gy = 64/128)
+  int xy_grid = 0;
   int* d_flags = nullptr;             // device error flags (bounded-wait expiry)
   // kernel per pass of a double step (PK_*), chosen by the autotuner
   int plan_y = PK_PLAIN, plan_z = PK_PLAIN, plan_x = PK_PLAIN;

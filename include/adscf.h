@@ -218,13 +218,15 @@ ADSCF_API int adscf_stage_launches(const adscf_ctx *ctx, int stage);
 /* ---- pass-kernel autotuner (bulk) ----------------------------------------
  * No reference counterpart.  At context creation every available kernel for
  * each line pass of the double step -- Y and Z: plain, persistent or
- * TMA-fed; X: plain or persistent -- is timed on the context's own buffers
+ * TMA-fed; X: plain, persistent, or the fused plane pass that also does Yi
+ * and Yf (then the Y choice is moot) -- is timed on the context's own buffers
  * and the fastest plan kept (cached per device, grid and precision; the
  * environment variable ADSCF_AUTOTUNE=0 keeps the default plan instead).
  * All plans compute the same arithmetic: results do not depend on the choice.
  * adscf_tuning writes the plan and the per-candidate timings as text;
  * adscf_set_pass_plan pins a plan (ADSCF_E_ARG if unavailable).           */
-enum { ADSCF_PASS_PLAIN = 0, ADSCF_PASS_PERSISTENT = 1, ADSCF_PASS_TMA = 2 };
+enum { ADSCF_PASS_PLAIN = 0, ADSCF_PASS_PERSISTENT = 1, ADSCF_PASS_TMA = 2,
+       ADSCF_PASS_FUSED = 3 /* x only: one plane pass for Yi + X + Yf */ };
 ADSCF_API int adscf_tuning(const adscf_ctx *ctx, char *buf, int len);
 ADSCF_API int adscf_set_pass_plan(adscf_ctx *ctx, int y, int z, int x);
 

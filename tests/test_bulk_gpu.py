@@ -240,7 +240,7 @@ def test_every_pass_plan_gives_identical_results(n, prec, rng):
         assert "plan" in c.tuning()
         for y in (0, 1, 2):
             for z in (0, 1, 2):
-                for x in (0, 1):
+                for x in (0, 1, 3):
                     try:
                         c.set_pass_plan(y, z, x)
                     except AdscfError:
