@@ -438,9 +438,8 @@ def main():
     ms_total = e0.elapsed_time(e1)
     clk = clocks.stop()
     if dist:
-        t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
+        from adscf_gb300.parallel import max_over_ranks
+        ms_total = max_over_ranks(ms_total, device="cuda")
     ms_step = ms_total / args.steps
     launches_per_step = lib.adscf_stage_launches(ctx.h, L_.STAGE_ITERATION)
     pass_plan = ctx.tuning()
@@ -473,7 +472,7 @@ def main():
     # error drops out to first order there; converge the split path, then
     # evaluate both precisions at the same field
     ctx.set_field(xh)
-    conv = ctx.scf_run(args.saddle_iters, tol=1e-12)
+    conv = ctx.scf_run(args.saddle_iters if world == 1 else 0, tol=1e-12)
     ws = ctx.get_field()
     _x, ds_, rs = ctx.scf_iteration(ws.copy())
     with make_ctx(A, A.FP64, stream) as c64:
@@ -519,7 +518,7 @@ def main():
                 "d2h_bytes_per_step": 2 * nv * 8 + 13 * 8,
                 "api": "adscf_scf_iteration (host field in/out, host density out)"},
     }
-    if not args.no_batches:
+    if not args.no_batches and world == 1:
         out.update(batch_legs(torch, A, stream, args))
     if rank == 0 and world == 1 and not args.no_cpu:
         t_iter, t_wall = cpu_sample(24, 1)
