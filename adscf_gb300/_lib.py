@@ -104,6 +104,8 @@ SIGNATURES = {
     "adscf_set_pass_plan": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "adscf_forward": (C.c_int, [C.c_void_p, _dp, _dp]),
     "adscf_backward": (C.c_int, [C.c_void_p, _dp]),
+    "adscf_forward_dev": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),
+    "adscf_free_energy_fp64": (C.c_int, [C.c_void_p, C.POINTER(IterResult)]),
     "adscf_batch_create": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p)]),
     "adscf_batch_destroy": (C.c_int, [C.c_void_p]),
     "adscf_batch_last_error": (C.c_char_p, [C.c_void_p]),

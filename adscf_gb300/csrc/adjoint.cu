@@ -126,16 +126,11 @@ void adj_destroy(adscf_ctx* ctx) {
   ctx->adj = nullptr;
 }
 
-extern "C" {
-
-int adscf_forward(adscf_ctx* ctx, const double* field, double* free_energy) {
-  if (!ctx || !field) return ADSCF_E_ARG;
+namespace {
+// the forward pass from the fields already in the adjoint buffer
+int forward_core(adscf_ctx* ctx, double* free_energy, double* sc_out) {
   int rc;
-  if ((rc = check_ctx(ctx)) || (rc = adj_setup(ctx))) return rc;
   AdjState* s = ctx->adj;
-  const size_t nv = 2 * (size_t)ctx->npts;
-  std::vector<double> tmp(field, field + nv);
-  CK(cudaMemcpyAsync(s->d_w, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if ((rc = bulk_enqueue_expfield(ctx, s->d_w))) return rc;
   if ((rc = bulk_enqueue_propagate(ctx))) return rc;
   k_adj_closure<<<s->A.nclos, BULK_THREADS, 0, ctx->stream>>>(s->A);
@@ -147,6 +142,66 @@ int adscf_forward(adscf_ctx* ctx, const double* field, double* free_energy) {
     return set_err(ctx, ADSCF_E_NONFINITE, "non-finite or non-positive Q in the forward pass");
   s->gen = ++ctx->prop_gen;
   if (free_energy) *free_energy = sc[ADJ_F];
+  if (sc_out) std::memcpy(sc_out, sc, sizeof(sc));
+  return ADSCF_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int adscf_forward(adscf_ctx* ctx, const double* field, double* free_energy) {
+  if (!ctx || !field) return ADSCF_E_ARG;
+  int rc;
+  if ((rc = check_ctx(ctx)) || (rc = adj_setup(ctx))) return rc;
+  const size_t nv = 2 * (size_t)ctx->npts;
+  std::vector<double> tmp(field, field + nv);
+  CK(cudaMemcpyAsync(ctx->adj->d_w, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  return forward_core(ctx, free_energy, nullptr);
+}
+
+int adscf_forward_dev(adscf_ctx* ctx, const double* d_field, double* free_energy) {
+  if (!ctx || !d_field) return ADSCF_E_ARG;
+  int rc;
+  if ((rc = check_ctx(ctx)) || (rc = adj_setup(ctx))) return rc;
+  const size_t nv = 2 * (size_t)ctx->npts;
+  CK(cudaMemcpyAsync(ctx->adj->d_w, d_field, nv * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  return forward_core(ctx, free_energy, nullptr);
+}
+
+// FP64 free energy at the context's current (device-resident) SCF field.  A
+// split context evaluates it on an FP64 sibling context created on first use.
+int adscf_free_energy_fp64(adscf_ctx* ctx, adscf_iter_result* out) {
+  if (!ctx || !out) return ADSCF_E_ARG;
+  if (ctx->geometry != ADSCF_BULK || ctx->p.ensemble != 1)
+    return set_err(ctx, ADSCF_E_STATE, "FP64 free energy: bulk contexts, canonical ensemble");
+  adscf_ctx* c64 = ctx;
+  int rc;
+  if (ctx->prec != ADSCF_FP64) {
+    if (!ctx->sib64) {
+      adscf_params q = ctx->p;
+      q.precision = ADSCF_FP64;
+      if ((rc = adscf_ctx_create(&q, &ctx->sib64))) return set_err(ctx, rc, "FP64 sibling context");
+    }
+    c64 = ctx->sib64;
+    if ((rc = adscf_set_stream(c64, ctx->stream))) return set_err(ctx, rc, c64->err);
+  }
+  int k = 0;
+  CK(cudaMemcpyAsync(&k, ctx->d_iter, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const double* field = ctx->d_hx + (size_t)(k % ctx->hist_slots) * 2 * (size_t)ctx->npts;
+  if ((rc = check_ctx(c64)) || (rc = adj_setup(c64))) return set_err(ctx, rc, c64->err);
+  const size_t nv = 2 * (size_t)ctx->npts;
+  CK(cudaMemcpyAsync(c64->adj->d_w, field, nv * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  double sc[ADJ_NSC];
+  double F = 0.0;
+  if ((rc = forward_core(c64, &F, sc))) return set_err(ctx, rc, c64->err);
+  *out = adscf_iter_result{};
+  out->free_energy = F;
+  out->Qsum = c64->dvol * sc[ADJ_S];
+  out->logQ = std::log(out->Qsum);
+  out->rho = ctx->p.rho;
+  out->mu = std::log(ctx->p.rho * ctx->volume / out->Qsum);
+  out->iter = k;
   return ADSCF_OK;
 }
 

@@ -319,6 +319,7 @@ int adscf_ctx_destroy(adscf_ctx* ctx) {
   if (ctx->g_iter) cudaGraphExecDestroy(ctx->g_iter);
   if (ctx->g_prop) cudaGraphExecDestroy(ctx->g_prop);
   adj_destroy(ctx);
+  if (ctx->sib64) adscf_ctx_destroy(ctx->sib64);
   if (ctx->geometry == ADSCF_BULK) bulk_destroy(ctx);
   else film_destroy(ctx);
   cudaFree(ctx->d_dist); cudaFree(ctx->d_dens); cudaFree(ctx->d_tmp);

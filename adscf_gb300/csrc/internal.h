@@ -91,6 +91,7 @@ struct adscf_ctx {
   // every propagating entry point advances so a stale forward is detected
   AdjState* adj = nullptr;
   long long prop_gen = 0;
+  adscf_ctx* sib64 = nullptr;   // FP64 sibling of a split context (adscf_free_energy_fp64)
 };
 
 // errors

@@ -232,6 +232,13 @@ class Context:
         self._ck(self.lib.adscf_forward(self.h, L.dptr(w), C.byref(out)))
         return out.value
 
+    def free_energy_fp64(self):
+        """FP64 free energy at the current SCF field (IterResult); on a split
+        context this is the polished value at a converged field."""
+        res = L.IterResult()
+        self._ck(self.lib.adscf_free_energy_fp64(self.h, C.byref(res)))
+        return res
+
     def backward(self):
         """(dF/dL_x, dF/dL_y, dF/dL_z, dF/dchi) at the fields of the last
         ``forward`` (reverse-mode adjoint of the discrete chain)."""

@@ -288,6 +288,37 @@ def c5_bulk(A, n=256, seed=5, prec=None):
     return inst, fields
 
 
+def c1_parity(A):
+    """C1 (the reference's CPU-runnable case: 32^3, L = 4.0, f_A = 0.30, chiN =
+    kappa = 25, ds = 0.01, Anderson m = 10 after 20 lambda = 0.1 steps; start
+    w = +-chiN (phi_A0 - f_A) + N(0, 0.1^2), phi_A0 = f_A + 0.1 cos(2 pi x/L),
+    seed 1) converged in FP64 and in split precision on the GPU: the split
+    path's own F and its FP64 evaluation at the split-converged field, each
+    against the FP64 saddle."""
+    n, l, f, chi = 32, 4.0, 0.30, 25.0
+    rng = np.random.default_rng(1)
+    x = np.arange(n) * l / n
+    phi0 = f + 0.1 * np.broadcast_to(np.cos(2 * np.pi * x / l)[None, None, :], (n, n, n))
+    w = np.stack([chi * (phi0 - f) + rng.normal(0.0, 0.1, (n, n, n)),
+                  -chi * (phi0 - f) + rng.normal(0.0, 0.1, (n, n, n))])
+    kw = dict(grid=(n, n, n), size=(l, l, l), ds=0.01, block_length=(f, 1 - f), kappa=25.0,
+              chi=chi, mixing_type=A.MIX_ANDERSON, mixing_dim=10, lam=0.1, lam_warm=0.1,
+              warm_iters=20)
+    with A.Context(A.BULK, precision=A.FP64, **kw) as c:
+        c.set_field(w)
+        r64 = c.scf_run(3000, tol=1e-16)
+    with A.Context(A.BULK, precision=A.SPLIT, **kw) as c:
+        c.set_field(w)
+        rs = c.scf_run(3000, tol=1e-8)
+        pol = c.free_energy_fp64()
+    return {"workload": "C1 32^3 diblock melt, converged", "fp64_iterations": r64.iter,
+            "fp64_accuracy": r64.accuracy, "split_iterations": rs.iter,
+            "split_accuracy": rs.accuracy,
+            "dF_per_chain_split": abs(rs.free_energy - r64.free_energy),
+            "dF_per_chain_split_fp64_at_split_saddle": abs(pol.free_energy - r64.free_energy),
+            "vs": "FP64 GPU path converged to accuracy 1e-16"}
+
+
 def time_batch(torch, A, inst, fields, stream, steps, warmup):
     """Batch iterations/s over `steps` graph replays after `warmup`."""
     with A.Batch(inst) as b:
@@ -518,6 +549,8 @@ def main():
                 "d2h_bytes_per_step": 2 * nv * 8 + 13 * 8,
                 "api": "adscf_scf_iteration (host field in/out, host density out)"},
     }
+    if world == 1:
+        out["parity_c1"] = c1_parity(A)
     if not args.no_batches and world == 1:
         out.update(batch_legs(torch, A, stream, args))
     if rank == 0 and world == 1 and not args.no_cpu:

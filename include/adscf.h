@@ -246,7 +246,17 @@ ADSCF_API int adscf_set_pass_plan(adscf_ctx *ctx, int y, int z, int x);
  * derivatives of the equilibrium free energy.  Any other propagating call
  * on the context between the two returns ADSCF_E_STATE.                  */
 ADSCF_API int adscf_forward(adscf_ctx *ctx, const double *field, double *free_energy);
+ADSCF_API int adscf_forward_dev(adscf_ctx *ctx, const double *d_field, double *free_energy);
 ADSCF_API int adscf_backward(adscf_ctx *ctx, double *grad);
+
+/* FP64 free energy per chain at the context's current device-resident SCF
+ * field (bulk, canonical).  A split context iterates in FP32/FP64-split
+ * precision; at a converged field F is stationary in the densities, so one
+ * FP64 evaluation there (on an FP64 sibling context, created on first use)
+ * gives the saddle free energy to second order in the remaining field
+ * error.  Fills free_energy, Qsum, logQ, mu, rho and iter of `out`.  No
+ * reference counterpart (the reference is FP64 throughout).               */
+ADSCF_API int adscf_free_energy_fp64(adscf_ctx *ctx, adscf_iter_result *out);
 
 /* ---- batches of independent bulk instances ------------------------------
  * No single reference counterpart: the reference runs a phase-diagram or

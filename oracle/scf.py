@@ -17,7 +17,7 @@ from . import bulk, interactions, iterate
 def bulk_scf(field, n_iter, grid, size, ds, block_length, kappa, chi,
              mixing_type=2, lam=0.1, m=2, lam00=1.0e-3, warm=None,
              ensemble=1, rho=1.0, mu=0.0, density0=None, vol=(1.0, 1.0),
-             gram=False):
+             gram=False, stop_accuracy=None):
     field = np.array(field, dtype=np.float64, copy=True)
     density = np.zeros_like(field) if density0 is None else np.array(density0, dtype=np.float64)
     mixer = iterate.Mixer(field.size, mixing_type, lam, m=m, lam00=lam00, warm=warm,
@@ -40,6 +40,8 @@ def bulk_scf(field, n_iter, grid, size, ds, block_length, kappa, chi,
         dfield = newfield - field
         field = mixer(field, dfield, it)
         density = newdensity
+        if stop_accuracy is not None and not acc > stop_accuracy:
+            break
     return field, hist
 
 
