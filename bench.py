@@ -319,6 +319,62 @@ def c1_parity(A):
             "vs": "FP64 GPU path converged to accuracy 1e-16"}
 
 
+def c4_film3d(A, seed=4):
+    """C4: AB diblock film f_A = 0.25, chiN = 30, kappa = 25, lateral 64 x 64
+    periodic (L_x = L_y = 6.0), 64-interval tanh z mesh (2.0), D = 3.0, wall
+    field h_A = -0.5 at the bottom wall and +0.5 at the top, Ns = 150
+    end-refined contour steps; start fields a hexagonal pattern of amplitude
+    0.5 plus N(0, 0.05^2); the grand-canonical ensemble, mu = 2.25 and lambda
+    mixing 0.2 of the reference's Film_3D deck; Douglas ADI, split precision."""
+    from adscf_gb300 import mesh
+    gx = gy = 64
+    gz, D, Lxy = 64, 3.0, 6.0
+    dz, zr = mesh.tanh_mesh(gz, D, 2.0)
+    dss = mesh.contour_steps(150, ds_scheme=1)
+    lo = mesh.wall_potential(zr, D, 0.4, (1.0,), walls=(True, False))[0]
+    hi = mesh.wall_potential(zr, D, 0.4, (1.0,), walls=(False, True))[0]
+    ext = np.stack([-0.5 * lo + 0.5 * hi, np.zeros(gz + 1)])
+    rng = np.random.default_rng(seed)
+    x = np.arange(gx) * Lxy / gx
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    k = 4 * np.pi / (np.sqrt(3.0) * Lxy / 2)
+    hexp = sum(np.cos(k * (np.cos(a) * X + np.sin(a) * Y)) for a in (0.0, 2 * np.pi / 3, 4 * np.pi / 3)) / 3
+    pat = np.broadcast_to(hexp[None, :, :], (gz + 1, gy, gx))
+    w = np.stack([0.5 * pat, -0.5 * pat]) + rng.normal(0.0, 0.05, (2, gz + 1, gy, gx))
+    w[:, 0] = w[:, -1] = 0.0
+    kw = dict(grid=(gx, gy, gz), size=(Lxy, Lxy, D), dz=dz, dss=dss, n_a=int(round(0.25 * 150)),
+              block_length=(0.25, 0.75), chi=30.0, kappa=25.0, ext_potential=ext,
+              int_scheme=1, int_span=0, ensemble=2, mu=2.25, precision=A.SPLIT,
+              mixing_type=A.MIX_LAMBDA, lam=0.2)
+    return kw, w
+
+
+def film3d_leg(torch, A, stream, steps):
+    kw, w = c4_film3d(A)
+    with A.Context(A.FILM_3D, **kw) as c:
+        A._lib.check(c.lib, c.h, c.lib.adscf_set_stream(c.h, stream.cuda_stream))
+        c.set_field(w)
+        c._ck(c.lib.adscf_enqueue(c.h, 0, 3))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        c._ck(c.lib.adscf_enqueue(c.h, 0, steps))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        res = c.scf_run(0)
+        launches = c.lib.adscf_stage_launches(c.h, 0)
+    ns = len(kw["dss"]) - 1
+    lines = 2 * ns * (64 * 63 + 64 * 63 + 64 * 64)   # x, y and z line solves, both chains
+    return {"workload": "C4: Film_3D diblock, 64x64 lateral L=6, 64-interval tanh z mesh, D=3, "
+                        "h_A -0.5/+0.5, Ns=150 end-refined, f_A=0.25, chiN=30, grand canonical mu=2.25, "
+                        "ADI, split",
+            "ms_per_iter": ms, "iter_s": 1000.0 / ms, "line_solves_s": lines * 1000.0 / ms,
+            "contour_steps_s": 2 * ns * 1000.0 / ms, "launches_per_iter": launches,
+            "accuracy": res.accuracy, "status": res.status}
+
+
 def time_batch(torch, A, inst, fields, stream, steps, warmup):
     """Batch iterations/s over `steps` graph replays after `warmup`."""
     with A.Batch(inst) as b:
@@ -552,6 +608,7 @@ def main():
     if world == 1:
         out["parity_c1"] = c1_parity(A)
     if not args.no_batches and world == 1:
+        out["film3d"] = film3d_leg(torch, A, stream, args.batch_steps)
         out.update(batch_legs(torch, A, stream, args))
     if rank == 0 and world == 1 and not args.no_cpu:
         t_iter, t_wall = cpu_sample(24, 1)
