@@ -116,6 +116,14 @@ int read_scalars(adscf_ctx* ctx, double* sc) {
 
 }  // namespace
 
+void adj_set_box(adscf_ctx* ctx) {
+  if (!ctx->adj) return;
+  ctx->adj->A.lx = ctx->p.sizex;
+  ctx->adj->A.ly = ctx->p.sizey;
+  ctx->adj->A.lz = ctx->p.sizez;
+  ctx->adj->gen = -1;          // a forward at the old box no longer matches
+}
+
 void adj_destroy(adscf_ctx* ctx) {
   AdjState* s = ctx->adj;
   if (!s) return;

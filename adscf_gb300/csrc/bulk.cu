@@ -653,7 +653,26 @@ int mix_e_t(adscf_ctx* ctx) {
   return ADSCF_OK;
 }
 
+// new box side lengths: recompute the k-space tables in place (same sizes,
+// same device buffers, so captured kernels keep valid pointers)
+template <typename T>
+int set_box_t(adscf_ctx* ctx) {
+  std::vector<T> fk;
+  std::vector<double> g64;
+  int gxy_off = 0, gz_off = 0, g64_off = 0;
+  bulkhost::append_tables<T>(ctx->gx, ctx->gy, ctx->gz, ctx->p.sizex, ctx->p.sizey, ctx->p.sizez,
+                             ctx->p.ds, fk, g64, gxy_off, gz_off, g64_off);
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(ctx->d_fk, fk.data(), fk.size() * sizeof(T), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_g64, g64.data(), g64.size() * sizeof(double), cudaMemcpyHostToDevice));
+  return ADSCF_OK;
+}
+
 }  // namespace
+
+int bulk_set_box(adscf_ctx* ctx) {
+  return ctx->prec == ADSCF_SPLIT ? set_box_t<float>(ctx) : set_box_t<double>(ctx);
+}
 
 int bulk_create(adscf_ctx* ctx) {
   return ctx->prec == ADSCF_SPLIT ? create_t<float>(ctx) : create_t<double>(ctx);

@@ -603,6 +603,26 @@ int adscf_set_stream(adscf_ctx* ctx, void* stream) {
   return ADSCF_OK;
 }
 
+int adscf_set_box(adscf_ctx* ctx, double sizex, double sizey, double sizez) {
+  if (!ctx || !(sizex > 0 && sizey > 0 && sizez > 0)) return ADSCF_E_ARG;
+  if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "box updates are for bulk contexts");
+  ++ctx->prop_gen;
+  ctx->p.sizex = sizex; ctx->p.sizey = sizey; ctx->p.sizez = sizez;
+  ctx->volume = sizex * sizey * sizez;
+  ctx->dvol = ctx->volume / ((double)ctx->gx * ctx->gy * ctx->gz);
+  ctx->S.volume = ctx->volume;
+  ctx->S.dvol = ctx->dvol;
+  ctx->S.qscale = ctx->dvol;
+  int rc = bulk_set_box(ctx);
+  if (rc) return rc;
+  adj_set_box(ctx);
+  // graphs hold the closure parameters by value: capture again on next use
+  if (ctx->g_iter) { cudaGraphExecDestroy(ctx->g_iter); ctx->g_iter = nullptr; }
+  if (ctx->g_prop) { cudaGraphExecDestroy(ctx->g_prop); ctx->g_prop = nullptr; }
+  if (ctx->sib64) { adscf_ctx_destroy(ctx->sib64); ctx->sib64 = nullptr; }
+  return ADSCF_OK;
+}
+
 int adscf_tuning(const adscf_ctx* ctx, char* buf, int len) {
   if (!ctx || !buf || len < 1) return ADSCF_E_ARG;
   char plan[96];

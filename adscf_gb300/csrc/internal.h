@@ -114,6 +114,8 @@ int bulk_step_single(adscf_ctx* ctx, double* d_prop, const double* d_e);
 int bulk_r2c(adscf_ctx* ctx, const double* d_prop, double* h_half);
 int bulk_c2r(adscf_ctx* ctx, const double* h_half, double* d_prop);
 int bulk_mix_e(adscf_ctx* ctx);                 // k_mix with E update
+int bulk_set_box(adscf_ctx* ctx);               // k-space tables for new side lengths
+void adj_set_box(adscf_ctx* ctx);               // adjoint's copy of the side lengths
 // adjoint (adjoint.cu)
 void adj_destroy(adscf_ctx* ctx);
 // films (film.cu)

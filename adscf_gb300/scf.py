@@ -232,6 +232,11 @@ class Context:
         self._ck(self.lib.adscf_forward(self.h, L.dptr(w), C.byref(out)))
         return out.value
 
+    def set_box(self, size):
+        """New box side lengths (bulk); fields and mixing history are kept."""
+        self._ck(self.lib.adscf_set_box(self.h, *map(float, size)))
+        self.params.sizex, self.params.sizey, self.params.sizez = size
+
     def free_energy_fp64(self):
         """FP64 free energy at the current SCF field (IterResult); on a split
         context this is the polished value at a converged field."""

@@ -249,6 +249,13 @@ ADSCF_API int adscf_forward(adscf_ctx *ctx, const double *field, double *free_en
 ADSCF_API int adscf_forward_dev(adscf_ctx *ctx, const double *d_field, double *free_energy);
 ADSCF_API int adscf_backward(adscf_ctx *ctx, double *grad);
 
+/* New box side lengths for a bulk context (unit-cell relaxation): the
+ * k-space factors of Calculate_Laplace (mod_fourier.f90:165-198) and the
+ * volume terms are recomputed in place; fields, densities and the mixing
+ * history are kept.  No reference counterpart: the reference fixes the box
+ * at start-up.                                                            */
+ADSCF_API int adscf_set_box(adscf_ctx *ctx, double sizex, double sizey, double sizez);
+
 /* FP64 free energy per chain at the context's current device-resident SCF
  * field (bulk, canonical).  A split context iterates in FP32/FP64-split
  * precision; at a converged field F is stationary in the densities, so one

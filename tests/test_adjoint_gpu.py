@@ -22,9 +22,21 @@ def oracle_free_energy(w, grid, size, ds, chi=CHI):
     return (r["energy"] - phiw + eint) / (r["rho"] * r["volume"])
 
 
-def ctx(grid, size, ds, prec=FP64, chi=CHI, **kw):
+def ctx(grid, size, ds, prec=FP64, chi=CHI, kappa=KAPPA, **kw):
     return Context(BULK, grid=grid, size=size, ds=ds, block_length=(F_A, 1.0 - F_A),
-                   kappa=KAPPA, chi=chi, precision=prec, **kw)
+                   kappa=kappa, chi=chi, precision=prec, **kw)
+
+
+# an ordered lamellar phase along x: chiN = 25, kappa = 25 at f_A = 0.4
+# (the free energy of converged lamellae has its minimum near L_x = 4.1)
+LAM = dict(chi=25.0, kappa=25.0, mixing_type=MIX_ANDERSON, mixing_dim=10, lam=0.1, lam_warm=0.1,
+           warm_iters=10)
+
+
+def lamellar_start(grid, size, rng, amp=5.0):
+    x = np.arange(grid[0]) * size[0] / grid[0]
+    s = np.broadcast_to(np.cos(2 * np.pi * x / size[0])[None, None, :], grid[::-1])
+    return np.stack([amp * s, -amp * s]) + 0.01 * rng.standard_normal((2,) + grid[::-1])
 
 
 def fields(grid, size, rng, amp=1.0, noise=0.3):
@@ -110,28 +122,55 @@ def test_backward_state_errors(rng):
 
 
 def test_stress_at_saddle_matches_neighbouring_box_free_energies(rng):
-    """At a converged saddle point dF/dL_x equals the slope of the
+    """At a converged (ordered) saddle point dF/dL_x equals the slope of the
     equilibrium free energy between neighbouring box sizes."""
-    grid, ds = (32, 8, 8), 0.05
-    size = (4.2, 2.0, 2.0)
-    x = np.arange(grid[0]) * size[0] / grid[0]
-    s = np.broadcast_to(np.cos(2 * np.pi * x / size[0])[None, None, :], grid[::-1])
-    w0 = np.stack([2.0 * s, -2.0 * s]) + 0.01 * rng.standard_normal((2,) + grid[::-1])
+    grid, ds = (32, 8, 8), 0.02
+    size = (3.8, 2.0, 2.0)
+    w0 = lamellar_start(grid, size, rng)
 
     def converge(sz, start):
-        with ctx(grid, sz, ds, mixing_type=MIX_ANDERSON, mixing_dim=10, lam=0.1,
-                 lam_warm=0.1, warm_iters=10) as c:
+        with ctx(grid, sz, ds, **LAM) as c:
             c.set_field(start)
             res = c.scf_run(3000, tol=1e-26)
             wf = c.get_field().reshape(start.shape)
             F = c.forward(wf)
             g = c.backward()
-        return wf, F, g, res
+            dens = c.get_density()
+        return wf, F, g, res, dens
 
-    wc, Fc, gc, res = converge(size, w0)
+    wc, Fc, gc, res, dens = converge(size, w0)
     assert res.accuracy < 1e-18
+    assert np.ptp(dens[: dens.size // 2]) > 0.5          # lamellae, not the disordered melt
     d = 2e-3
-    _, Fp, _, _ = converge((size[0] + d,) + size[1:], wc)
-    _, Fm, _, _ = converge((size[0] - d,) + size[1:], wc)
+    _, Fp, _, _, _ = converge((size[0] + d,) + size[1:], wc)
+    _, Fm, _, _, _ = converge((size[0] - d,) + size[1:], wc)
     slope = (Fp - Fm) / (2 * d)
-    assert abs(gc[0] - slope) < 1e-5 * max(1e-2, abs(slope)) + 1e-8, (gc[0], slope)
+    assert abs(slope) > 1e-2                              # a real stress at L = 3.8
+    assert abs(gc[0] - slope) < 1e-5 * abs(slope), (gc[0], slope)
+
+
+def test_unit_cell_relaxation_reaches_zero_stress(rng):
+    """Lamellae along x: relax L_x from 3.6 with the adjoint stress to
+    |dF/dL_x| < 1e-6; the converged free energy there is below its
+    neighbours', and the lamellae persist."""
+    from adscf_gb300.relax import relax_box
+    grid, ds = (32, 8, 8), 0.02
+    size = (3.6, 2.0, 2.0)
+    w0 = lamellar_start(grid, size, rng)
+    with ctx(grid, size, ds, **LAM) as c:
+        L, F, g, hist = relax_box(c, w0, axes=(0,), tol=1e-6)
+        dens = c.get_density()
+    print("relaxation:", [(round(h[0][0], 6), h[1], h[2][0]) for h in hist])
+    assert abs(g[0]) < 1e-6, hist
+    assert len(hist) < 25
+    assert 3.9 < L[0] < 4.4
+    assert np.ptp(dens[: dens.size // 2]) > 0.5
+
+    def converged_F(lx):
+        with ctx(grid, (lx,) + size[1:], ds, **LAM) as c2:
+            c2.set_field(lamellar_start(grid, (lx,) + size[1:], rng))
+            c2.scf_run(3000, tol=1e-16)
+            return c2.forward(c2.get_field())
+
+    d = 0.01
+    assert converged_F(L[0] - d) > F and converged_F(L[0] + d) > F
