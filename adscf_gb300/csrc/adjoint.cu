@@ -160,6 +160,13 @@ extern "C" {
 int adscf_forward(adscf_ctx* ctx, const double* field, double* free_energy) {
   if (!ctx || !field) return ADSCF_E_ARG;
   int rc;
+  if (ctx->geometry != ADSCF_BULK) {   // films and brushes: F and its wall-potential gradient
+    double* d = film_fe_field(ctx);
+    if (!d) return set_err(ctx, ADSCF_E_OOM, "film forward buffer");
+    const size_t nvf = (size_t)ctx->ntypes * ctx->npts;
+    CK(cudaMemcpyAsync(d, field, nvf * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    return film_forward(ctx, free_energy);
+  }
   if ((rc = check_ctx(ctx)) || (rc = adj_setup(ctx))) return rc;
   const size_t nv = 2 * (size_t)ctx->npts;
   std::vector<double> tmp(field, field + nv);
@@ -213,8 +220,16 @@ int adscf_free_energy_fp64(adscf_ctx* ctx, adscf_iter_result* out) {
   return ADSCF_OK;
 }
 
+int adscf_backward_surface(adscf_ctx* ctx, double* dF_dchi, double* dF_dU) {
+  if (!ctx) return ADSCF_E_ARG;
+  if (ctx->geometry == ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "wall-potential gradients are for films and brushes");
+  return film_backward(ctx, dF_dchi, dF_dU);
+}
+
 int adscf_backward(adscf_ctx* ctx, double* grad) {
   if (!ctx || !grad) return ADSCF_E_ARG;
+  if (ctx->geometry != ADSCF_BULK)
+    return set_err(ctx, ADSCF_E_STATE, "films and brushes: use adscf_backward_surface");
   int rc;
   if ((rc = check_ctx(ctx))) return rc;
   AdjState* s = ctx->adj;

@@ -25,6 +25,11 @@ struct FilmState {
   void* d_w1 = nullptr;
   int* d_err = nullptr;
   double max_ratio = 1.0;       // largest neighbour spacing ratio of the mesh
+  // free energy at fixed fields and its wall-potential gradient
+  double* d_fe_w = nullptr;     // [ntypes][npts] field copy
+  double* d_fe_part = nullptr;  // [nplanes][FE_N]
+  double* d_fe_out = nullptr;   // [2 + ntypes*nplanes]
+  long long fe_gen = -1;
 };
 
 namespace {
@@ -220,9 +225,55 @@ int film_create(adscf_ctx* ctx, const adscf_params* p) {
   return ADSCF_OK;
 }
 
+// F at the fields in d_fe_w (copied there by the caller) and its gradient
+int film_forward(adscf_ctx* ctx, double* out_F) {
+  FilmState* F = ctx->film;
+  const size_t nv = (size_t)ctx->ntypes * ctx->npts;
+  if (!F->d_fe_part) {
+    CK(cudaMalloc(&F->d_fe_part, (size_t)ctx->nplanes * FE_N * sizeof(double)));
+    CK(cudaMalloc(&F->d_fe_out, (2 + (size_t)ctx->ntypes * ctx->nplanes) * sizeof(double)));
+  }
+  int rc = film_enqueue_propagate(ctx, F->d_fe_w);
+  if (rc) return rc;
+  if ((rc = film_check_pivot(ctx))) return rc;
+  k_film_fe<<<ctx->nplanes, 256, 0, ctx->stream>>>(ctx->S, F->d_fe_w, F->d_fe_part);
+  k_film_fe_sc<<<1, 32, 0, ctx->stream>>>(ctx->S, F->d_fe_part, F->d_fe_out);
+  CK(cudaGetLastError());
+  double f = 0.0;
+  CK(cudaMemcpyAsync(&f, F->d_fe_out, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (!std::isfinite(f)) return set_err(ctx, ADSCF_E_NONFINITE, "non-finite free energy");
+  F->fe_gen = ++ctx->prop_gen;
+  if (out_F) *out_F = f;
+  return ADSCF_OK;
+}
+
+double* film_fe_field(adscf_ctx* ctx) {
+  FilmState* F = ctx->film;
+  if (!F->d_fe_w && cudaMalloc(&F->d_fe_w, (size_t)ctx->ntypes * ctx->npts * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return F->d_fe_w;
+}
+
+int film_backward(adscf_ctx* ctx, double* dF_dchi, double* dF_dU) {
+  FilmState* F = ctx->film;
+  if (F->fe_gen != ctx->prop_gen || !F->d_fe_out)
+    return set_err(ctx, ADSCF_E_STATE, "the film gradient needs the state of an immediately preceding adscf_forward");
+  const size_t n = 2 + (size_t)ctx->ntypes * ctx->nplanes;
+  std::vector<double> h(n);
+  CK(cudaMemcpyAsync(h.data(), F->d_fe_out, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (dF_dchi) *dF_dchi = h[1];
+  if (dF_dU) std::memcpy(dF_dU, h.data() + 2, (n - 2) * sizeof(double));
+  return ADSCF_OK;
+}
+
 void film_destroy(adscf_ctx* ctx) {
   FilmState* F = ctx->film;
   if (!F) return;
+  cudaFree(F->d_fe_w); cudaFree(F->d_fe_part); cudaFree(F->d_fe_out);
   cudaFree(F->d_alpha); cudaFree(F->d_beta); cudaFree(F->d_gamma);
   cudaFree(F->d_dss); cudaFree(F->d_wA); cudaFree(F->d_wB); cudaFree(F->d_graft);
   cudaFree(F->d_q); cudaFree(F->d_qd); cudaFree(F->d_gam); cudaFree(F->d_w1);

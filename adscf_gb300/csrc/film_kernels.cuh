@@ -366,3 +366,74 @@ k_film_contour_b(const FilmDev<T>* __restrict__ Fs, const int* __restrict__ film
   const FilmDev<T> F = Fs[films[blockIdx.x]];
   film_contour_body<T>(F, 0, 1);
 }
+
+// ---------------------------------------------------------------------------
+// Free energy of a film or brush at fixed fields and its gradient with
+// respect to the wall potential U_c(z), chi (diblock) or ww (brush).  At fixed
+// w the densities do not depend on U, so dF/dU_c(z) = w_z sum_xy v_c phi_c /
+// (rho V); the energy terms follow Calculate_Energy with the external term
+// (Film_CK_AD/Film_1D/Main_Diblock_Melt/main_diblock_melt.f90).  One block
+// per plane sums its lines; a one-thread kernel combines the planes.
+// ---------------------------------------------------------------------------
+enum { FE_S0 = 0, FE_S1, FE_PHIW, FE_EINT, FE_EEXT, FE_X01, FE_RHO, FE_N };
+
+static __global__ void __launch_bounds__(256) k_film_fe(ScfDev S, const double* __restrict__ w,
+                                                 double* __restrict__ part) {
+  __shared__ double red[FE_N * 32];
+  const double Q = q_total(S);
+  const double scale = density_scale(S, Q);
+  const int z = blockIdx.x;
+  double acc[FE_N];
+#pragma unroll
+  for (int k = 0; k < FE_N; ++k) acc[k] = 0.0;
+  for (int l = threadIdx.x; l < S.plane; l += blockDim.x) {
+    const int p = z * S.plane + l;
+    const double phi0 = scale * S.dist[p];
+    if (S.homopolymer) {
+      const double u = S.ext ? S.ext[z] : 0.0;
+      acc[FE_S0] += phi0;
+      acc[FE_PHIW] += phi0 * w[p];
+      acc[FE_EINT] += 0.5 * S.ww * phi0 * phi0;
+      acc[FE_EEXT] += u * phi0;
+      acc[FE_X01] += 0.5 * phi0 * phi0;
+      acc[FE_RHO] += phi0;
+    } else {
+      const double phi1 = scale * S.dist[S.npts + p];
+      const double f0 = S.v0 * phi0, f1 = S.v1 * phi1, tot = f0 + f1;
+      const double u0 = S.ext ? S.ext[z] : 0.0, u1 = S.ext ? S.ext[S.nplanes + z] : 0.0;
+      acc[FE_S0] += f0;
+      acc[FE_S1] += f1;
+      acc[FE_PHIW] += phi0 * w[p] + phi1 * w[S.npts + p];
+      acc[FE_EINT] += 0.5 * S.kappa * (tot - 1.0) * (tot - 1.0) + S.chi * f0 * f1;
+      acc[FE_EEXT] += u0 * f0 + u1 * f1;
+      acc[FE_X01] += f0 * f1;
+      acc[FE_RHO] += phi0 + phi1;
+    }
+  }
+  const double r = block_reduce_k<FE_N>(acc, red);
+  if (threadIdx.x < FE_N) part[z * FE_N + threadIdx.x] = r;
+}
+
+// out: [0] F, [1] dF/dchi (brush: dF/dww), [2 + c*nplanes + z] dF/dU_c(z)
+static __global__ void k_film_fe_sc(ScfDev S, const double* __restrict__ part, double* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double Q = q_total(S);
+  double t[FE_N] = {0, 0, 0, 0, 0, 0, 0};
+  for (int z = 0; z < S.nplanes; ++z)
+    for (int k = 0; k < FE_N; ++k) t[k] += S.wz[z] * part[z * FE_N + k];
+  double rho, energy;
+  if (S.ensemble == 1) {
+    rho = S.rho;
+    energy = S.rho * S.volume * (log(S.rho * S.volume / Q) - 1.0);
+  } else {
+    rho = t[FE_RHO] / S.volume / S.chain_len;
+    energy = -rho * S.volume;
+  }
+  const double rv = rho * S.volume;
+  out[0] = (energy - t[FE_PHIW] + t[FE_EINT] + t[FE_EEXT]) / rv;
+  out[1] = t[FE_X01] / rv;
+  for (int z = 0; z < S.nplanes; ++z) {
+    out[2 + z] = S.wz[z] * part[z * FE_N + FE_S0] / rv;
+    if (S.ntypes == 2) out[2 + S.nplanes + z] = S.wz[z] * part[z * FE_N + FE_S1] / rv;
+  }
+}

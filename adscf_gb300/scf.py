@@ -225,9 +225,9 @@ class Context:
 
     # -- differentiation (FP64 bulk) ----------------------------------------
     def forward(self, field):
-        """Free energy per chain at `field` [2][npts], no mixing; keeps the
-        propagator slices for ``backward``."""
-        w = _f64(field, 2 * self.npts)
+        """Free energy per chain at `field` [ntypes][npts], no mixing; keeps
+        the propagator state for ``backward`` / ``backward_surface``."""
+        w = _f64(field, self.ntypes * self.npts)
         out = C.c_double()
         self._ck(self.lib.adscf_forward(self.h, L.dptr(w), C.byref(out)))
         return out.value
@@ -243,6 +243,15 @@ class Context:
         res = L.IterResult()
         self._ck(self.lib.adscf_free_energy_fp64(self.h, C.byref(res)))
         return res
+
+    def backward_surface(self):
+        """Films / brushes: (dF/dchi or dF/dww, dF/dU [ntypes][gz+1]) at the
+        fields of the last ``forward``."""
+        nplanes = self.npts // (self.params.gx * self.params.gy)
+        g = np.empty(self.ntypes * nplanes)
+        dchi = C.c_double()
+        self._ck(self.lib.adscf_backward_surface(self.h, C.byref(dchi), L.dptr(g)))
+        return dchi.value, g.reshape(self.ntypes, nplanes)
 
     def backward(self):
         """(dF/dL_x, dF/dL_y, dF/dL_z, dF/dchi) at the fields of the last

@@ -248,6 +248,14 @@ ADSCF_API int adscf_set_pass_plan(adscf_ctx *ctx, int y, int z, int x);
 ADSCF_API int adscf_forward(adscf_ctx *ctx, const double *field, double *free_energy);
 ADSCF_API int adscf_forward_dev(adscf_ctx *ctx, const double *d_field, double *free_energy);
 ADSCF_API int adscf_backward(adscf_ctx *ctx, double *grad);
+/* Films and brushes (any precision): adscf_forward gives the free energy
+ * per chain at the host fields (the film Calculate_Energy with the external
+ * term); adscf_backward_surface then gives dF/dchi (brush: dF/dww) and the
+ * gradient with respect to the wall potential, dF_dU[c][z] for every type c
+ * and plane z = 0..gz (the ext_potential array of adscf_params).  At fixed
+ * fields the densities do not depend on U, so the gradient is the
+ * plane-weighted density over rho V.                                      */
+ADSCF_API int adscf_backward_surface(adscf_ctx *ctx, double *dF_dchi, double *dF_dU);
 
 /* New box side lengths for a bulk context (unit-cell relaxation): the
  * k-space factors of Calculate_Laplace (mod_fourier.f90:165-198) and the

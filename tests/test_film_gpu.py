@@ -159,3 +159,73 @@ def test_zero_pivot_returns_status():
         with pytest.raises(AdscfError) as e:
             c.propagate_step(np.ones(gz + 1), w, 0.25)
     assert e.value.code == 3
+
+
+def _film_kw(gz, D, dz, ext, ensemble=1, chi=15.0, **kw):
+    return dict(grid=(1, 1, gz), size=(1.0, 1.0, D), ds=0.02, block_length=(0.5, 0.5), dz=dz,
+                kappa=25.0, chi=chi, ext_potential=ext, int_scheme=1, int_span=1,
+                ensemble=ensemble, mu=0.4, **kw)
+
+
+@pytest.mark.parametrize("ensemble", [1, 2])
+def test_film_free_energy_gradient_wrt_wall_potential(ensemble, rng):
+    """adscf_forward / adscf_backward_surface on a Film_1D context: F equals
+    the SCF loop's F of the same field, and dF/dU_c(z), dF/dchi match
+    central differences of F at fixed fields."""
+    gz, D = 40, 3.0
+    dz, zr = of.tanh_mesh(gz, D)
+    ext = np.stack([0.6 * oi.wall_potential_shape(zr, D, 0.4), -0.3 * oi.wall_potential_shape(zr, D, 0.4)])
+    z = zr / D
+    field = np.stack([1.5 * np.cos(2 * np.pi * z), -1.5 * np.cos(2 * np.pi * z)])
+    field += 0.1 * rng.standard_normal(field.shape)
+    field[:, 0] = field[:, -1] = 0.0
+    with Context(FILM_1D, **_film_kw(gz, D, dz, ext, ensemble)) as c:
+        F = c.forward(field)
+        dchi, dU = c.backward_surface()
+        c.set_field(field)
+        _x, _d, r = c.scf_iteration(field.copy())
+    assert abs(F - r.free_energy) < 1e-12 * max(1.0, abs(F))
+
+    def F_of(ext2, chi=15.0):
+        with Context(FILM_1D, **_film_kw(gz, D, dz, ext2, ensemble, chi)) as c2:
+            return c2.forward(field)
+
+    d = 1e-5
+    for ctype, zi in ((0, 1), (0, 5), (1, 3), (1, gz - 2), (0, gz // 2)):
+        ep, em = ext.copy(), ext.copy()
+        ep[ctype, zi] += d
+        em[ctype, zi] -= d
+        fd = (F_of(ep) - F_of(em)) / (2 * d)
+        assert abs(dU[ctype, zi] - fd) < 1e-7 * max(1e-3, abs(fd)), (ctype, zi, dU[ctype, zi], fd)
+    fd = (F_of(ext, 15.0 + 1e-4) - F_of(ext, 15.0 - 1e-4)) / 2e-4
+    assert abs(dchi - fd) < 1e-8 * max(1.0, abs(fd))
+
+
+def test_brush_gradient_wrt_wall_potential(rng):
+    gz, D = 50, 4.0
+    dz, zr = of.tanh_mesh(gz, D)
+    dss = of.contour_steps(60, ds_scheme=2)
+    graft = np.zeros(gz + 1)
+    graft[3] = 1.0
+    graft /= np.dot(of.integrator_weights(dz, 1, "interior"), graft)
+    ext = (0.4 * oi.wall_potential_shape(zr, D, 0.5))[None, :]
+    field = 0.3 * rng.standard_normal((1, gz + 1))
+
+    def make(ext2, ww=1.0):
+        return Context(BRUSH, grid=(1, 1, gz), size=(1.0, 1.0, D), dss=dss, dz=dz, graft=graft,
+                       rho=0.3, ww=ww, ext_potential=ext2, int_scheme=1, int_span=1)
+
+    with make(ext) as c:
+        F = c.forward(field)
+        dww, dU = c.backward_surface()
+    d = 1e-5
+    for zi in (2, 10, 25):
+        ep, em = ext.copy(), ext.copy()
+        ep[0, zi] += d
+        em[0, zi] -= d
+        with make(ep) as a, make(em) as b:
+            fd = (a.forward(field) - b.forward(field)) / (2 * d)
+        assert abs(dU[0, zi] - fd) < 1e-7 * max(1e-3, abs(fd)), (zi, dU[0, zi], fd)
+    with make(ext, 1.0 + 1e-4) as a, make(ext, 1.0 - 1e-4) as b:
+        fd = (a.forward(field) - b.forward(field)) / 2e-4
+    assert abs(dww - fd) < 1e-8 * max(1.0, abs(fd))
