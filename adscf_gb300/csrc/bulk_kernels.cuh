@@ -356,8 +356,9 @@ k_bulk_strided(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ wo
 // q_{N-s} qdag_s (node N-s).  Trapezoid weights per block: 1/2 at the block
 // ends, 1 inside (times ds, applied at the end).
 //   FP32 slices: each product is split exactly (TwoProd via FMA) and summed
-//   with a compensated (Kahan/TwoSum) float pair, flushed every CHUNK pairs
-//   into FP64 accumulators.
+//   with a compensated (Kahan/TwoSum) float pair, ~48 bits over the whole
+//   contour, converted to FP64 once per point (conversions run on GB300's
+//   narrow FP64 pipe).
 //   FP64 slices: plain FP64 accumulation, as the reference.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float wA_of(int s, int na) {
@@ -395,7 +396,6 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
     double accA = 0.0, accB = 0.0;
     if constexpr (sizeof(T) == 4) {
       FF fa = {0.f, 0.f}, fb = {0.f, 0.f};
-      int cnt = 0;
       for (int s = 0; 2 * s <= N; ++s) {
         const int u = N - s;
         const cplx<T> a = sl[(size_t)s * np + p];
@@ -411,11 +411,6 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
           wa = wA_of(u, NA); wb = wB_of(u, NA, N);
           if (wa != 0.f) ff_add_prod(fa, x2, y2, wa);
           if (wb != 0.f) ff_add_prod(fb, x2, y2, wb);
-        }
-        if (++cnt == 16) {
-          accA += (double)fa.hi + (double)fa.lo; fa.hi = fa.lo = 0.f;
-          accB += (double)fb.hi + (double)fb.lo; fb.hi = fb.lo = 0.f;
-          cnt = 0;
         }
       }
       accA += (double)fa.hi + (double)fa.lo;
