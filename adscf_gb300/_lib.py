@@ -120,6 +120,8 @@ SIGNATURES = {
     "adscf_batch_enqueue": (C.c_int, [C.c_void_p, C.c_int]),
     "adscf_batch_results": (C.c_int, [C.c_void_p, C.POINTER(IterResult)]),
     "adscf_batch_launches": (C.c_int, [C.c_void_p]),
+    "adscf_batch_forward": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "adscf_batch_backward": (C.c_int, [C.c_void_p, _dp]),
     "adscf_propagate_step_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                                C.c_double, C.c_double, C.c_void_p, C.c_void_p,
                                                C.c_void_p]),

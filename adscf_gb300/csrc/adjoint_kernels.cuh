@@ -56,7 +56,7 @@ __device__ __forceinline__ double adj_k2(int i, int n, double len) {
 }
 
 // densities, mean-field residual and the cotangents of the contour integrals
-__global__ void __launch_bounds__(BULK_THREADS) k_adj_closure(AdjDev A) {
+__device__ __forceinline__ void adj_closure_body(const AdjDev& A, int bid, int nb) {
   __shared__ double red[4 * 32];
   __shared__ double sS;
   if (threadIdx.x == 0) {
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(BULK_THREADS) k_adj_closure(AdjDev A) {
   const size_t np = (size_t)A.I.npts;
   const double scale = A.rho * (double)np / S;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += (size_t)gridDim.x * blockDim.x) {
+  for (size_t p = (size_t)bid * blockDim.x + threadIdx.x; p < np; p += (size_t)nb * blockDim.x) {
     const double pa = scale * A.I.dist[p], pb = scale * A.I.dist[np + p];
     const double va = A.v0 * pa, vb = A.v1 * pb;
     const double tot = va + vb - 1.0;
@@ -84,10 +84,21 @@ __global__ void __launch_bounds__(BULK_THREADS) k_adj_closure(AdjDev A) {
     acc[3] += va * vb;
   }
   const double r = block_reduce_k<4>(acc, red);
-  if (threadIdx.x < 4) A.part[blockIdx.x * 4 + threadIdx.x] = r;
+  if (threadIdx.x < 4) A.part[bid * 4 + threadIdx.x] = r;
 }
 
-__global__ void k_adj_scalars(AdjDev A) {
+static __global__ void __launch_bounds__(BULK_THREADS) k_adj_closure(AdjDev A) {
+  adj_closure_body(A, blockIdx.x, gridDim.x);
+}
+
+// batch: instance blockIdx.y, A.nclos blocks each
+static __global__ void __launch_bounds__(BULK_THREADS) k_adj_closure_b(const AdjDev* __restrict__ As) {
+  const AdjDev& A = As[blockIdx.y];
+  if ((int)blockIdx.x >= A.nclos) return;
+  adj_closure_body(A, blockIdx.x, A.nclos);
+}
+
+__device__ __forceinline__ void adj_scalars_body(const AdjDev& A) {
   if (threadIdx.x != 0) return;
   double S = 0.0, p[4] = {0.0, 0.0, 0.0, 0.0};
   for (int i = 0; i < A.nqpart; ++i) S += A.I.qpart[i];
@@ -100,9 +111,11 @@ __global__ void k_adj_scalars(AdjDev A) {
   A.sc[ADJ_DCHI] = p[3] / rm;
 }
 
-// adjoint x pass of step t (see the file comment); work.y = row tile
-__global__ void __launch_bounds__(BULK_THREADS)
-k_adj_x(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw, int t) {
+static __global__ void k_adj_scalars(AdjDev A) { adj_scalars_body(A); }
+static __global__ void k_adj_scalars_b(const AdjDev* __restrict__ As) { adj_scalars_body(As[blockIdx.x]); }
+
+// adjoint x pass of step t (see the file comment) on row tile `tile`
+__device__ __forceinline__ void adj_x_body(const AdjDev& A, int tile, const double2* __restrict__ gtw, int t) {
   extern __shared__ __align__(16) unsigned char smraw[];
   const BulkDev<double>& I = A.I;
   const Plan1D P = I.px;
@@ -111,7 +124,7 @@ k_adj_x(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw
   load_twiddles<double>(tw, gtw, P);
   const int N = P.n, LPC = P.lpc;
   const int nrows = I.gy * I.gz;
-  const int row0 = work[blockIdx.x].y * LPC;
+  const int row0 = tile * LPC;
   const int nl = min(LPC, nrows - row0);
   const size_t base = (size_t)row0 * N;
   const int tot = nl * N;
@@ -173,11 +186,23 @@ k_adj_x(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw
   for (int e = threadIdx.x; e < tot; e += blockDim.x) A.sa[base + e] = r2[(e / N) * P.ld + (e % N)];
 }
 
+static __global__ void __launch_bounds__(BULK_THREADS)
+k_adj_x(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw, int t) {
+  adj_x_body(A, work[blockIdx.x].y, gtw, t);
+}
+
+// batch: work = (instance, row tile); every listed instance has t <= its Ns
+static __global__ void __launch_bounds__(BULK_THREADS)
+k_adj_x_b(const AdjDev* __restrict__ As, const int2* __restrict__ work, const double2* __restrict__ gtw, int t) {
+  const int2 w = work[blockIdx.x];
+  if (t > As[w.x].I.ns) return;
+  adj_x_body(As[w.x], w.y, gtw, t);
+}
+
 // adjoint z pass of step t: forward z of both spectra, stress partials,
 // factor G/M on the adjoint spectrum, inverse z.  Three line buffers.
-__global__ void __launch_bounds__(BULK_THREADS)
-k_adj_z(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw,
-        const double* __restrict__ fk) {
+__device__ __forceinline__ void adj_z_body(const AdjDev& A, int tile, const double2* __restrict__ gtw,
+                                           const double* __restrict__ fk) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ double red[3 * 32];
   const BulkDev<double>& I = A.I;
@@ -189,7 +214,7 @@ k_adj_z(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw
   const int N = P.n, LPC = P.lpc;
   const int gx = I.gx, gy = I.gy;
   const int nlines = gx * gy;
-  const int L0 = work[blockIdx.x].y * LPC;
+  const int L0 = tile * LPC;
   const int nl = min(LPC, nlines - L0);
   const size_t es = (size_t)gx * gy;
   const int tot = nl * N;
@@ -232,7 +257,7 @@ k_adj_z(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw
     a = make_double2(a.x * g, a.y * g);
   }
   const double s = block_reduce_k<3>(acc, red);
-  if (threadIdx.x < 3) A.gpart[blockIdx.x * 3 + threadIdx.x] += s;
+  if (threadIdx.x < 3) A.gpart[tile * 3 + threadIdx.x] += s;   // one tile per block: deterministic
   double2* o = (r == b0) ? b1 : b0;
   r = fft_lines<double>(r, o, tw, P, line, lt, active, -1);
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
@@ -242,7 +267,21 @@ k_adj_z(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw
   }
 }
 
-__global__ void k_adj_grad(AdjDev A) {
+static __global__ void __launch_bounds__(BULK_THREADS)
+k_adj_z(AdjDev A, const int2* __restrict__ work, const double2* __restrict__ gtw,
+        const double* __restrict__ fk) {
+  adj_z_body(A, work[blockIdx.x].y, gtw, fk);
+}
+
+static __global__ void __launch_bounds__(BULK_THREADS)
+k_adj_z_b(const AdjDev* __restrict__ As, const int2* __restrict__ work, const double2* __restrict__ gtw,
+          const double* __restrict__ fk, int t) {
+  const int2 w = work[blockIdx.x];
+  if (t > As[w.x].I.ns) return;
+  adj_z_body(As[w.x], w.y, gtw, fk);
+}
+
+__device__ __forceinline__ void adj_grad_body(const AdjDev& A) {
   if (threadIdx.x != 0) return;
   double g[3] = {0.0, 0.0, 0.0};
   for (int b = 0; b < A.nztiles; ++b)
@@ -251,3 +290,6 @@ __global__ void k_adj_grad(AdjDev A) {
   A.sc[ADJ_DLY] = 2.0 * A.ds * g[1] / A.ly;
   A.sc[ADJ_DLZ] = 2.0 * A.ds * g[2] / A.lz;
 }
+
+static __global__ void k_adj_grad(AdjDev A) { adj_grad_body(A); }
+static __global__ void k_adj_grad_b(const AdjDev* __restrict__ As) { adj_grad_body(As[blockIdx.x]); }

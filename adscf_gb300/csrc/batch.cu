@@ -35,6 +35,7 @@
 #include "bulk_reg.cuh"
 #include "film_host.h"
 #include "film_kernels.cuh"
+#include "adjoint_kernels.cuh"
 
 struct adscf_batch {
   int n = 0, prec = ADSCF_SPLIT;
@@ -76,6 +77,26 @@ struct adscf_batch {
   int* d_list64 = nullptr;
   int n32 = 0, n64 = 0;
   int* d_err = nullptr;                 // zero-pivot flag of the sweeps
+  // FP64 bulk batches: host copies of the instances and the adjoint state
+  std::vector<BulkDev<double>> hI64;
+  struct BatchAdj* adj = nullptr;
+  long long prop_gen = 0;
+};
+
+// forward/backward of every instance of an FP64 bulk batch (adjoint_kernels.cuh)
+struct BatchAdj {
+  AdjDev* d_adj = nullptr;              // [n]
+  BulkDev<double>* d_inst2 = nullptr;   // [2n]: (adjoint spectrum, forward-chain spectrum) per instance
+  void* pool = nullptr;
+  double* d_w = nullptr;                // packed fields
+  double* d_sc = nullptr;               // [n][ADJ_NSC]
+  int2 *wx = nullptr, *wy2 = nullptr, *wy1 = nullptr, *wz = nullptr;
+  std::vector<int> px, py2, py1, pz;    // tiles active at reverse step T
+  std::vector<size_t> gpart_off;
+  size_t gpart_bytes = 0;
+  size_t smx = 0, smy = 0, smz = 0;
+  int nclos_max = 1;
+  long long gen = -1;
 };
 
 namespace {
@@ -237,6 +258,7 @@ int build(adscf_batch* b) {
     S.mixE = d.E;
     S.mixds = q.ds;
   }
+  if constexpr (sizeof(T) == 8) b->hI64.assign(I.begin(), I.end());
   BK(cudaMalloc(&b->d_inst, n * sizeof(BulkDev<T>)));
   BK(cudaMemcpyAsync(b->d_inst, I.data(), n * sizeof(BulkDev<T>), cudaMemcpyHostToDevice, b->stream));
   BK(cudaMalloc(&b->d_S, n * sizeof(ScfDev)));
@@ -524,7 +546,7 @@ int enqueue_film(adscf_batch* b) {
 }
 
 template <typename T>
-int enqueue_iteration(adscf_batch* b) {
+int enqueue_propagation(adscf_batch* b) {
   const BulkDev<T>* d = static_cast<const BulkDev<T>*>(b->d_inst);
   const cplx<T>* tw = static_cast<const cplx<T>*>(b->d_tw);
   const T* fk = static_cast<const T*>(b->d_fk);
@@ -570,6 +592,15 @@ int enqueue_iteration(adscf_batch* b) {
     for (const auto& C : b->cls) xpass(C, C.px[t], t, XM_STEP);
   }
   k_bulk_contour<T><<<dim3(b->cont_blocks, b->n), BULK_THREADS, 0, s>>>(d);
+  BK(cudaGetLastError());
+  return ADSCF_OK;
+}
+
+template <typename T>
+int enqueue_iteration(adscf_batch* b) {
+  int rc = enqueue_propagation<T>(b);
+  if (rc) return rc;
+  cudaStream_t s = b->stream;
   k_closure_b<<<dim3(b->clos_grid, b->n), SCF_THREADS, 0, s>>>(b->d_S, CL_MEANFIELD | CL_MIXDOTS);
   k_solve_b<<<b->n, 64, 0, s>>>(b->d_S, 1, 1);
   k_mix_b<T><<<dim3(b->mix_grid, b->n), SCF_THREADS, 0, s>>>(b->d_S, b->mix_grid);
@@ -690,9 +721,201 @@ int get_t(adscf_batch* b, double* out, bool fields) {
   return ADSCF_OK;
 }
 
+size_t plan_bytes_d(const Plan1D& P, int nbuf) {
+  const size_t twn = (P.n + 1) & ~1;
+  return (twn + (size_t)nbuf * P.lpc * P.ld) * sizeof(double2);
+}
+
+int batch_adj_setup(adscf_batch* b) {
+  if (b->adj) return ADSCF_OK;
+  BatchAdj* a = new (std::nothrow) BatchAdj();
+  if (!a) return berr(b, ADSCF_E_OOM, "batch adjoint state");
+  b->adj = a;
+  const int n = b->n;
+  // pool: per instance forward-chain spectrum, seeds, closure and stress partials
+  Carve c;
+  struct Off { size_t sf, bb, part, gpart; };
+  std::vector<Off> o(n);
+  std::vector<int> nclos(n), nzt(n);
+  for (int i = 0; i < n; ++i) {
+    const BulkDev<double>& I = b->hI64[i];
+    const size_t np = I.npts;
+    nclos[i] = (int)std::min<size_t>((np + BULK_THREADS - 1) / BULK_THREADS, 128);
+    nzt[i] = (I.gx * I.gy + I.pz.lpc - 1) / I.pz.lpc;
+    a->nclos_max = std::max(a->nclos_max, nclos[i]);
+    o[i].sf = c.take(np * sizeof(double2));
+    o[i].bb = c.take(2 * np * sizeof(double));
+    o[i].part = c.take((size_t)nclos[i] * 4 * sizeof(double));
+    o[i].gpart = c.take((size_t)nzt[i] * 3 * sizeof(double));
+  }
+  const size_t o_sc = c.take((size_t)n * ADJ_NSC * sizeof(double));
+  const size_t o_w = c.take(b->foff[n] * sizeof(double));
+  if (cudaMalloc(&a->pool, c.off) != cudaSuccess) {
+    cudaGetLastError();
+    return berr(b, ADSCF_E_OOM, "batch adjoint pool");
+  }
+  unsigned char* base = static_cast<unsigned char*>(a->pool);
+  a->d_sc = reinterpret_cast<double*>(base + o_sc);
+  a->d_w = reinterpret_cast<double*>(base + o_w);
+  std::vector<AdjDev> h(n);
+  std::vector<BulkDev<double>> two(2 * n);
+  for (int i = 0; i < n; ++i) {
+    const adscf_params& q = b->p[i];
+    AdjDev& A = h[i];
+    A.I = b->hI64[i];
+    A.sa = A.I.spec;
+    A.sf = reinterpret_cast<double2*>(base + o[i].sf);
+    A.b = reinterpret_cast<double*>(base + o[i].bb);
+    A.w = a->d_w + b->foff[i];
+    A.part = reinterpret_cast<double*>(base + o[i].part);
+    A.gpart = reinterpret_cast<double*>(base + o[i].gpart);
+    A.sc = a->d_sc + (size_t)i * ADJ_NSC;
+    A.nqpart = b->cont_blocks;
+    A.nclos = nclos[i];
+    A.nztiles = nzt[i];
+    A.rho = q.rho; A.kappa = q.kappa; A.chi = q.chi;
+    A.v0 = q.monomer_volume[0] != 0 ? q.monomer_volume[0] : 1.0;
+    A.v1 = q.monomer_volume[1] != 0 ? q.monomer_volume[1] : 1.0;
+    A.ds = q.ds;
+    A.lx = q.sizex; A.ly = q.sizey; A.lz = q.sizez;
+    two[2 * i] = A.I;
+    two[2 * i + 1] = A.I;
+    two[2 * i + 1].spec = A.sf;
+    a->smx = std::max(a->smx, plan_bytes_d(A.I.px, 2));
+    a->smy = std::max(a->smy, plan_bytes_d(A.I.py, 2));
+    a->smz = std::max(a->smz, plan_bytes_d(A.I.pz, 3));
+  }
+  BK(cudaMalloc(&a->d_adj, n * sizeof(AdjDev)));
+  BK(cudaMemcpyAsync(a->d_adj, h.data(), n * sizeof(AdjDev), cudaMemcpyHostToDevice, b->stream));
+  BK(cudaMalloc(&a->d_inst2, 2 * n * sizeof(BulkDev<double>)));
+  BK(cudaMemcpyAsync(a->d_inst2, two.data(), 2 * n * sizeof(BulkDev<double>), cudaMemcpyHostToDevice, b->stream));
+  a->gpart_off.resize(n);
+  for (int i = 0; i < n; ++i) a->gpart_off[i] = o[i].gpart;
+  // generic-plan work lists by descending Ns: the instances still on their
+  // reverse sweep at step T are a prefix
+  std::vector<int> ord(n);
+  for (int i = 0; i < n; ++i) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return b->ns[x] > b->ns[y]; });
+  std::vector<int2> wx, wy2, wy1, wz;
+  std::vector<int> tx(n), ty(n), tz(n);
+  for (int i : ord) {
+    const BulkDev<double>& I = b->hI64[i];
+    tx[i] = (I.gy * I.gz + I.px.lpc - 1) / I.px.lpc;
+    ty[i] = (I.gx * I.gz + I.py.lpc - 1) / I.py.lpc;
+    tz[i] = nzt[i];
+    for (int k = 0; k < tx[i]; ++k) wx.push_back(make_int2(i, k));
+    for (int k = 0; k < ty[i]; ++k) { wy2.push_back(make_int2(2 * i, k)); wy2.push_back(make_int2(2 * i + 1, k)); }
+    for (int k = 0; k < ty[i]; ++k) wy1.push_back(make_int2(2 * i, k));
+    for (int k = 0; k < tz[i]; ++k) wz.push_back(make_int2(i, k));
+  }
+  a->px.assign(b->maxns + 1, 0); a->py2.assign(b->maxns + 1, 0);
+  a->py1.assign(b->maxns + 1, 0); a->pz.assign(b->maxns + 1, 0);
+  for (int T = 1; T <= b->maxns; ++T)
+    for (int i = 0; i < n; ++i)
+      if (b->ns[i] >= T) { a->px[T] += tx[i]; a->py2[T] += 2 * ty[i]; a->py1[T] += ty[i]; a->pz[T] += tz[i]; }
+  auto up = [&](const std::vector<int2>& v, int2*& d) -> int {
+    BK(cudaMalloc(&d, v.size() * sizeof(int2)));
+    BK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    return ADSCF_OK;
+  };
+  int rc;
+  if ((rc = up(wx, a->wx)) || (rc = up(wy2, a->wy2)) || (rc = up(wy1, a->wy1)) || (rc = up(wz, a->wz))) return rc;
+  a->gpart_bytes = c.off;   // the whole pool is cleared before a backward pass
+  int optin = 0;
+  BK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev));
+  if (a->smx > (size_t)optin || a->smy > (size_t)optin || a->smz + 3 * 32 * sizeof(double) > (size_t)optin)
+    return berr(b, ADSCF_E_ARG, "grid line too long for the adjoint passes");
+  BK(cudaFuncSetAttribute(k_adj_x_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a->smx));
+  BK(cudaFuncSetAttribute(k_adj_z_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a->smz));
+  BK(cudaStreamSynchronize(b->stream));
+  return ADSCF_OK;
+}
+
+void batch_adj_destroy(adscf_batch* b) {
+  BatchAdj* a = b->adj;
+  if (!a) return;
+  cudaFree(a->d_adj); cudaFree(a->d_inst2); cudaFree(a->pool);
+  cudaFree(a->wx); cudaFree(a->wy2); cudaFree(a->wy1); cudaFree(a->wz);
+  delete a;
+  b->adj = nullptr;
+}
+
+int batch_adj_check(adscf_batch* b) {
+  if (b->film || b->prec != ADSCF_FP64) return berr(b, ADSCF_E_STATE, "the batch adjoint needs an FP64 bulk batch");
+  for (const adscf_params& q : b->p)
+    if (q.ensemble != 1) return berr(b, ADSCF_E_STATE, "the batch adjoint covers the canonical ensemble");
+  return ADSCF_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int adscf_batch_forward(adscf_batch* b, const double* fields, double* free_energy) {
+  if (!b || !fields || !free_energy) return ADSCF_E_ARG;
+  int rc;
+  if ((rc = batch_adj_check(b)) || (rc = batch_adj_setup(b))) return rc;
+  BatchAdj* a = b->adj;
+  const int n = b->n;
+  BK(cudaMemcpyAsync(a->d_w, fields, b->foff[n] * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  for (int i = 0; i < n; ++i) {
+    const size_t np = b->npts[i];
+    const int gb = (int)std::min<size_t>((2 * np + 255) / 256, 152 * 8);
+    k_expfield<double><<<gb, 256, 0, b->stream>>>(a->d_w + b->foff[i], static_cast<double*>(b->E[i]), np, b->p[i].ds);
+  }
+  if ((rc = enqueue_propagation<double>(b))) return rc;
+  k_adj_closure_b<<<dim3(a->nclos_max, n), BULK_THREADS, 0, b->stream>>>(a->d_adj);
+  k_adj_scalars_b<<<n, 32, 0, b->stream>>>(a->d_adj);
+  BK(cudaGetLastError());
+  std::vector<double> sc((size_t)n * ADJ_NSC);
+  BK(cudaMemcpyAsync(sc.data(), a->d_sc, sc.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  BK(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < n; ++i) {
+    const double* q = sc.data() + (size_t)i * ADJ_NSC;
+    if (!(q[ADJ_S] > 0.0) || !std::isfinite(q[ADJ_F]))
+      return berr(b, ADSCF_E_NONFINITE, "instance " + std::to_string(i) + ": non-finite or non-positive Q");
+    free_energy[i] = q[ADJ_F];
+  }
+  a->gen = ++b->prop_gen;
+  return ADSCF_OK;
+}
+
+int adscf_batch_backward(adscf_batch* b, double* grad) {
+  if (!b || !grad) return ADSCF_E_ARG;
+  int rc;
+  if ((rc = batch_adj_check(b))) return rc;
+  BatchAdj* a = b->adj;
+  if (!a || a->gen != b->prop_gen)
+    return berr(b, ADSCF_E_STATE, "adscf_batch_backward needs an immediately preceding adscf_batch_forward");
+  cudaStream_t s = b->stream;
+  const double2* tw = static_cast<const double2*>(b->d_tw);
+  const double* fk = static_cast<const double*>(b->d_fk);
+  for (int i = 0; i < b->n; ++i) {
+    const int nzt = (b->hI64[i].gx * b->hI64[i].gy + b->hI64[i].pz.lpc - 1) / b->hI64[i].pz.lpc;
+    BK(cudaMemsetAsync(static_cast<unsigned char*>(a->pool) + a->gpart_off[i], 0, (size_t)nzt * 3 * sizeof(double), s));
+  }
+  for (int T = b->maxns; T >= 1; --T) {
+    if (a->px[T] <= 0) continue;
+    k_adj_x_b<<<a->px[T], BULK_THREADS, a->smx, s>>>(a->d_adj, a->wx, tw, T);
+    k_bulk_strided<double><<<a->py2[T], BULK_THREADS, a->smy, s>>>(a->d_inst2, a->wy2, tw, fk, nullptr, b->d_g64, T, 0);
+    k_adj_z_b<<<a->pz[T], BULK_THREADS, a->smz, s>>>(a->d_adj, a->wz, tw, fk, T);
+    if (T > 1)
+      k_bulk_strided<double><<<a->py1[T], BULK_THREADS, a->smy, s>>>(a->d_inst2, a->wy1, tw, fk, nullptr, b->d_g64, T, 1);
+  }
+  k_adj_grad_b<<<b->n, 32, 0, s>>>(a->d_adj);
+  BK(cudaGetLastError());
+  std::vector<double> sc((size_t)b->n * ADJ_NSC);
+  BK(cudaMemcpyAsync(sc.data(), a->d_sc, sc.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  BK(cudaStreamSynchronize(s));
+  for (int i = 0; i < b->n; ++i) {
+    const double* q = sc.data() + (size_t)i * ADJ_NSC;
+    grad[4 * i + 0] = q[ADJ_DLX];
+    grad[4 * i + 1] = q[ADJ_DLY];
+    grad[4 * i + 2] = q[ADJ_DLZ];
+    grad[4 * i + 3] = q[ADJ_DCHI];
+  }
+  return ADSCF_OK;
+}
 
 int adscf_batch_create(const adscf_params* params, int n, adscf_batch** out) {
   if (!out) return ADSCF_E_ARG;
@@ -730,6 +953,7 @@ int adscf_batch_create(const adscf_params* params, int n, adscf_batch** out) {
 int adscf_batch_destroy(adscf_batch* b) {
   if (!b) return ADSCF_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_adj_destroy(b);
   if (b->g_iter) cudaGraphExecDestroy(b->g_iter);
   cudaFree(b->pool); cudaFree(b->d_inst); cudaFree(b->d_S);
   cudaFree(b->d_tw); cudaFree(b->d_fk); cudaFree(b->d_g64);
@@ -765,6 +989,7 @@ int adscf_batch_get_densities(adscf_batch* b, double* densities) {
 
 int adscf_batch_scf_run(adscf_batch* b, int n_iter, double tol, adscf_iter_result* out) {
   if (!b || n_iter < 0) return ADSCF_E_ARG;
+  ++b->prop_gen;
   int rc = build_graph(b);
   if (rc) return rc;
   for (int i = 0; i < n_iter; ++i) {
@@ -788,6 +1013,7 @@ int adscf_batch_set_stream(adscf_batch* b, void* cuda_stream) {
 
 int adscf_batch_enqueue(adscf_batch* b, int repeats) {
   if (!b || repeats < 0) return ADSCF_E_ARG;
+  ++b->prop_gen;
   int rc = build_graph(b);
   if (rc) return rc;
   for (int i = 0; i < repeats; ++i) BK(cudaGraphLaunch(b->g_iter, b->stream));

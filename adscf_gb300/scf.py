@@ -350,6 +350,18 @@ class Batch:
         self._ck(self.lib.adscf_batch_scf_run(self.h, int(n_iter), float(tol), res))
         return list(res)
 
+    def forward(self, fields):
+        """FP64 bulk batch: free energy per chain of every instance at `fields`."""
+        F = np.empty(self.n)
+        self._ck(self.lib.adscf_batch_forward(self.h, L.dptr(self._pack(fields)), L.dptr(F)))
+        return F
+
+    def backward(self):
+        """[n][4]: dF/dL_x, dF/dL_y, dF/dL_z, dF/dchi per instance."""
+        g = np.empty((self.n, 4))
+        self._ck(self.lib.adscf_batch_backward(self.h, L.dptr(g)))
+        return g
+
     def results(self):
         res = (L.IterResult * self.n)()
         self._ck(self.lib.adscf_batch_results(self.h, res))

@@ -302,6 +302,12 @@ ADSCF_API int adscf_batch_enqueue(adscf_batch *b, int repeats);
 ADSCF_API int adscf_batch_results(adscf_batch *b, adscf_iter_result *out);
 /* kernel launches of one batch iteration */
 ADSCF_API int adscf_batch_launches(const adscf_batch *b);
+/* FP64 bulk batches (canonical): free energy per chain of every instance at
+ * the packed host fields (as adscf_forward), then the reverse-mode adjoint
+ * of every instance in one sweep: grad[4 i + 0..3] = dF/dL_x, dF/dL_y,
+ * dF/dL_z, dF/dchi of instance i (as adscf_backward).                      */
+ADSCF_API int adscf_batch_forward(adscf_batch *b, const double *fields, double *free_energy);
+ADSCF_API int adscf_batch_backward(adscf_batch *b, double *grad);
 
 /* ---- allocation-free propagator step ----------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

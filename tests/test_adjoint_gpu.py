@@ -174,3 +174,32 @@ def test_unit_cell_relaxation_reaches_zero_stress(rng):
 
     d = 0.01
     assert converged_F(L[0] - d) > F and converged_F(L[0] + d) > F
+
+
+def test_batched_adjoint_matches_single_contexts(rng):
+    """adscf_batch_forward / adscf_batch_backward over uneven instances equal
+    each instance's single-context forward / backward."""
+    from adscf_gb300 import Batch
+    insts = [
+        dict(grid=(32, 32, 32), size=(3.9, 4.1, 3.7), ds=0.04, block_length=(0.4, 0.6), chi=18.0),
+        dict(grid=(24, 24, 24), size=(3.3, 3.3, 3.3), ds=0.05, block_length=(0.3, 0.7), chi=22.0),
+        dict(grid=(16, 12, 10), size=(3.3, 3.1, 2.9), ds=0.02, block_length=(0.45, 0.55), chi=15.0),
+        dict(grid=(40, 32, 24), size=(4.6, 3.9, 3.0), ds=0.025, block_length=(0.35, 0.65), chi=25.0),
+    ]
+    for kw in insts:
+        kw.update(geometry=BULK, kappa=KAPPA, precision=FP64)
+    fields = []
+    for kw in insts:
+        gx, gy, gz = kw["grid"]
+        fields.append(0.5 * rng.standard_normal((2, gz, gy, gx)))
+    with Batch(insts) as b:
+        Fb = b.forward(fields)
+        gb = b.backward()
+    for kw, w, F, g in zip(insts, fields, Fb, gb):
+        kw = dict(kw)
+        kw.pop("geometry")
+        with Context(BULK, **kw) as c:
+            F1 = c.forward(w)
+            g1 = c.backward()
+        assert abs(F - F1) < 1e-12 * max(1.0, abs(F1))
+        assert np.allclose(g, g1, rtol=1e-9, atol=1e-12), (g, g1)
