@@ -106,6 +106,7 @@ SIGNATURES = {
     "adscf_backward": (C.c_int, [C.c_void_p, _dp]),
     "adscf_forward_dev": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),
     "adscf_backward_surface": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "adscf_set_adjoint_checkpoint": (C.c_int, [C.c_void_p, C.c_int]),
     "adscf_free_energy_fp64": (C.c_int, [C.c_void_p, C.POINTER(IterResult)]),
     "adscf_set_box": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double]),
     "adscf_batch_create": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p)]),

@@ -45,6 +45,13 @@ struct AdjDev {
   int nqpart, nclos, nztiles;
   double rho, kappa, chi, v0, v1, ds;
   double lx, ly, lz;
+  // where the reverse sweep finds the stored nodes: node t of the forward
+  // chains at slA + (t - tA0) npts (z_{t-1}) and slB + (t - tB0) npts (the
+  // mirror node Ns - t); both are I.slices with offset 0 when every node is
+  // stored, two recomputed segments under checkpointing
+  const double2* slA;
+  const double2* slB;
+  int tA0, tB0;
 };
 
 enum { ADJ_S = 0, ADJ_F = 1, ADJ_AS = 2, ADJ_DCHI = 3, ADJ_DLX = 4, ADJ_DLY = 5, ADJ_DLZ = 6, ADJ_NSC = 8 };
@@ -134,7 +141,7 @@ __device__ __forceinline__ void adj_x_body(const AdjDev& A, int tile, const doub
   const bool fA = chain_type_fwd(I, t) == 0, bA = chain_type_bwd(I, t) == 0;
 
   // forward-chain spectrum: E(t) (q_{t-1}, qdag_{t-1}) -> forward x
-  const double2* slp = I.slices + (size_t)(t - 1) * np;
+  const double2* slp = A.slA + (size_t)(t - 1 - A.tA0) * np;
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     const size_t g = base + e;
     const double2 v = slp[g];
@@ -164,7 +171,7 @@ __device__ __forceinline__ void adj_x_body(const AdjDev& A, int tile, const doub
   const double cat = ds * (double)wA_of(t, I.na), cbt = ds * (double)wB_of(t, I.na, I.ns);
   const double cau = ds * (double)wA_of(u, I.na), cbu = ds * (double)wB_of(u, I.na, I.ns);
   const double aS = first ? A.sc[ADJ_AS] : 0.0;
-  const double2* slu = I.slices + (size_t)u * np;
+  const double2* slu = A.slB + (size_t)(u - A.tB0) * np;
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
     const size_t g = base + e;
     const int si = (e / N) * P.ld + (e % N);
@@ -293,3 +300,36 @@ __device__ __forceinline__ void adj_grad_body(const AdjDev& A) {
 
 static __global__ void k_adj_grad(AdjDev A) { adj_grad_body(A); }
 static __global__ void k_adj_grad_b(const AdjDev* __restrict__ As) { adj_grad_body(As[blockIdx.x]); }
+
+// Contour integral over one segment of nodes s in [s_lo, s_hi] from two
+// recomputed node ranges: q_s at A + (s - a0) npts, qdag_{Ns-s} at
+// B + (Ns - s - b0) npts (trapezoid weights of mod_diblock.f90:143-154).
+// dist accumulates (+=) over the segments in a fixed order; the segment that
+// holds s = 0 also writes the partial sums of q_Ns (= B node Ns).
+static __global__ void __launch_bounds__(BULK_THREADS)
+k_contour_segment(BulkDev<double> I, const double2* __restrict__ A, int a0, const double2* __restrict__ B,
+                  int b0, int s_lo, int s_hi) {
+  __shared__ double red[32];
+  const size_t np = (size_t)I.npts;
+  const int N = I.ns, NA = I.na;
+  double qs = 0.0;
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += (size_t)gridDim.x * blockDim.x) {
+    double accA = 0.0, accB = 0.0;
+    for (int s = s_lo; s <= s_hi; ++s) {
+      const double pr = A[(size_t)(s - a0) * np + p].x * B[(size_t)(N - s - b0) * np + p].y;
+      accA += (double)wA_of(s, NA) * pr;
+      accB += (double)wB_of(s, NA, N) * pr;
+    }
+    I.dist[p] += I.ds * accA;
+    I.dist[np + p] += I.ds * accB;
+    if (s_lo == 0) qs += B[(size_t)(N - b0) * np + p].x;
+  }
+  const double tot = block_reduce_1(qs, red);
+  if (s_lo == 0 && threadIdx.x == 0) I.qpart[blockIdx.x] = tot;
+}
+
+// (1, 1) at every point: node 0 of both chains
+static __global__ void k_fill_ones(double2* __restrict__ z, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    z[i] = make_double2(1.0, 1.0);
+}

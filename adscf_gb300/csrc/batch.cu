@@ -764,6 +764,8 @@ int batch_adj_setup(adscf_batch* b) {
     AdjDev& A = h[i];
     A.I = b->hI64[i];
     A.sa = A.I.spec;
+    A.slA = A.slB = A.I.slices;
+    A.tA0 = A.tB0 = 0;
     A.sf = reinterpret_cast<double2*>(base + o[i].sf);
     A.b = reinterpret_cast<double*>(base + o[i].bb);
     A.w = a->d_w + b->foff[i];

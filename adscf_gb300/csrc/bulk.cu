@@ -690,14 +690,44 @@ void bulk_destroy(adscf_ctx* ctx) {
   cudaFree(ctx->d_qpart);
 }
 
+static int slices_released(adscf_ctx* ctx) {
+  return set_err(ctx, ADSCF_E_STATE, "the propagator slices are released while adjoint checkpointing is on");
+}
 int bulk_enqueue_propagate(adscf_ctx* ctx) {
+  if (!ctx->slices_full) return slices_released(ctx);
   return ctx->prec == ADSCF_SPLIT ? propagate_t<float>(ctx) : propagate_t<double>(ctx);
 }
 int bulk_enqueue_chains(adscf_ctx* ctx) {
+  if (!ctx->slices_full) return slices_released(ctx);
   return ctx->prec == ADSCF_SPLIT ? chains_t<float>(ctx) : chains_t<double>(ctx);
 }
 int bulk_enqueue_contour(adscf_ctx* ctx) {
+  if (!ctx->slices_full) return slices_released(ctx);
   return ctx->prec == ADSCF_SPLIT ? contour_t<float>(ctx) : contour_t<double>(ctx);
+}
+// Slice storage of an FP64 context: all Ns + 1 nodes, or two nodes of scratch
+// (the conversions of the single-step entry points stage through the slice
+// buffer) while checkpointed adjoint passes recompute their nodes elsewhere.
+// The new buffer is allocated before the old one is freed, so a failed
+// allocation leaves the context as it was.
+int bulk_hold_slices(adscf_ctx* ctx, bool full) {
+  if (ctx->prec != ADSCF_FP64) return set_err(ctx, ADSCF_E_STATE, "slice release applies to FP64 contexts");
+  if (full == ctx->slices_full) return ADSCF_OK;
+  const size_t bytes = (size_t)(full ? ctx->ns + 1 : 2) * ctx->npts * sizeof(double2);
+  double2* p = nullptr;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(ctx, ADSCF_E_OOM, "propagator slice storage");
+  }
+  cudaFree(ctx->hb64.slices);
+  ctx->hb64.slices = p;
+  CK(cudaMemcpy(ctx->d_inst, &ctx->hb64, sizeof(ctx->hb64), cudaMemcpyHostToDevice));
+  ctx->slices_full = full;
+  // captured graphs replay the full chains: capture again on next use
+  if (ctx->g_iter) { cudaGraphExecDestroy(ctx->g_iter); ctx->g_iter = nullptr; }
+  if (ctx->g_prop) { cudaGraphExecDestroy(ctx->g_prop); ctx->g_prop = nullptr; }
+  return ADSCF_OK;
 }
 int bulk_enqueue_expfield(adscf_ctx* ctx, const double* d_w) {
   return ctx->prec == ADSCF_SPLIT ? expfield_t<float>(ctx, d_w) : expfield_t<double>(ctx, d_w);

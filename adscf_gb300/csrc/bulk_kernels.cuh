@@ -43,11 +43,12 @@ struct BulkDev {
   double ds;                 // contour step
 };
 
-// X-pass modes
-enum { XM_INIT = 0, XM_STEP = 1, XM_R2S = 2, XM_S2R = 3 };
+// X-pass modes (XM_FROM: start a chain segment at node t from a stored
+// state (q_t, qdag_t) in aux.in, as XM_INIT does from (1, 1) at node 0)
+enum { XM_INIT = 0, XM_STEP = 1, XM_R2S = 2, XM_S2R = 3, XM_FROM = 4 };
 
 struct XAux {
-  const void* in;   // XM_R2S: real input [npts] (T)
+  const void* in;   // XM_R2S: real input [npts] (T); XM_FROM: state [npts] (cplx<T>)
   void* out;        // XM_S2R: real output [npts] (T)
   const void* e;    // XM_R2S / XM_S2R: real factor [npts] (T) or null
 };
@@ -189,6 +190,24 @@ k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work
       s0[g] = mk<T>((T)1, (T)1);
       const EPt<T> ev = load_ept(I.E, g);
       b0[(e / N) * P.ld + (e % N)] = mk<T>(fA ? ev.a : ev.b, bA ? ev.a : ev.b);
+    }
+    __syncthreads();
+    cplx<T>* r = fft_lines<T>(b0, b1, tw, P, line, lt, active, +1);
+    for (int e = threadIdx.x; e < tot; e += blockDim.x)
+      I.spec[base + e] = r[(e / N) * P.ld + (e % N)];
+    return;
+  }
+  if (mode == XM_FROM) {
+    // slice t = the stored state; z = (E_f(t+1) q_t, E_b(t+1) qdag_t) -> forward
+    const bool fA = chain_type_fwd(I, t + 1) == 0, bA = chain_type_bwd(I, t + 1) == 0;
+    const cplx<T>* st = static_cast<const cplx<T>*>(aux.in);
+    cplx<T>* sl = I.slices + (size_t)t * I.npts;
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+      const size_t g = base + e;
+      const cplx<T> q = st[g];
+      sl[g] = q;
+      const EPt<T> ev = load_ept(I.E, g);
+      b0[(e / N) * P.ld + (e % N)] = mk<T>(q.x * (fA ? ev.a : ev.b), q.y * (bA ? ev.a : ev.b));
     }
     __syncthreads();
     cplx<T>* r = fft_lines<T>(b0, b1, tw, P, line, lt, active, +1);

@@ -92,6 +92,8 @@ struct adscf_ctx {
   AdjState* adj = nullptr;
   long long prop_gen = 0;
   adscf_ctx* sib64 = nullptr;   // FP64 sibling of a split context (adscf_free_energy_fp64)
+  int adj_ckpt = 0;             // adjoint checkpoint interval (0: every slice stored, < 0: ceil(sqrt(Ns)))
+  bool slices_full = true;      // all Ns + 1 propagator slices held (bulk_hold_slices)
 };
 
 // errors
@@ -115,6 +117,7 @@ int bulk_r2c(adscf_ctx* ctx, const double* d_prop, double* h_half);
 int bulk_c2r(adscf_ctx* ctx, const double* h_half, double* d_prop);
 int bulk_mix_e(adscf_ctx* ctx);                 // k_mix with E update
 int bulk_set_box(adscf_ctx* ctx);               // k-space tables for new side lengths
+int bulk_hold_slices(adscf_ctx* ctx, bool full);   // all Ns + 1 slices, or two of scratch (FP64)
 void adj_set_box(adscf_ctx* ctx);               // adjoint's copy of the side lengths
 // adjoint (adjoint.cu)
 void adj_destroy(adscf_ctx* ctx);

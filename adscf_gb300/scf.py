@@ -244,6 +244,10 @@ class Context:
         self._ck(self.lib.adscf_free_energy_fp64(self.h, C.byref(res)))
         return res
 
+    def set_adjoint_checkpoint(self, every):
+        """Checkpoint interval of forward/backward (0 off, < 0 ceil(sqrt(Ns)))."""
+        self._ck(self.lib.adscf_set_adjoint_checkpoint(self.h, int(every)))
+
     def backward_surface(self):
         """Films / brushes: (dF/dchi or dF/dww, dF/dU [ntypes][gz+1]) at the
         fields of the last ``forward``."""

@@ -248,6 +248,17 @@ ADSCF_API int adscf_set_pass_plan(adscf_ctx *ctx, int y, int z, int x);
 ADSCF_API int adscf_forward(adscf_ctx *ctx, const double *field, double *free_energy);
 ADSCF_API int adscf_forward_dev(adscf_ctx *ctx, const double *d_field, double *free_energy);
 ADSCF_API int adscf_backward(adscf_ctx *ctx, double *grad);
+/* Checkpointing of the FP64 bulk forward/backward pair (no counterpart in
+ * the reference, which stores every node): every = K > 0 keeps the states
+ * of both chains at nodes kK and at the mirror nodes Ns - (k+1)K + 1 and
+ * recomputes segments of K steps when the contour integral and the reverse
+ * sweep need them; every < 0 picks K = ceil(sqrt(Ns)).  The context then
+ * releases its Ns + 1 propagator slices (storage 2 ceil(Ns/K) + 2K + 4
+ * slices) and its SCF / propagation calls return ADSCF_E_STATE until
+ * every = 0 restores them.  A forward made before the call cannot be
+ * paired with a later backward.  Results equal the stored-slice pass up to
+ * the summation order of the contour integral.                            */
+ADSCF_API int adscf_set_adjoint_checkpoint(adscf_ctx *ctx, int every);
 /* Films and brushes (any precision): adscf_forward gives the free energy
  * per chain at the host fields (the film Calculate_Energy with the external
  * term); adscf_backward_surface then gives dF/dchi (brush: dF/dww) and the

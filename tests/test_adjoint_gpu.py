@@ -121,6 +121,52 @@ def test_backward_state_errors(rng):
             c.forward(w)
 
 
+@pytest.mark.parametrize("grid,size,ds,every", [
+    ((16, 12, 10), (3.3, 3.1, 2.9), 0.05, -1),   # Ns 20, segments of 5 (generic passes)
+    ((16, 12, 10), (3.3, 3.1, 2.9), 0.05, 3),    # ragged last segment
+    ((16, 12, 10), (3.3, 3.1, 2.9), 0.05, 1),
+    ((16, 12, 10), (3.3, 3.1, 2.9), 0.05, 20),   # one segment
+    ((32, 32, 32), (3.9, 4.1, 3.7), 0.04, -1),   # Ns 25; the stored pass runs the register FFTs
+    ((24, 20, 18), (3.6, 3.3, 3.1), 0.03, -1),   # Ns 34 (odd segment count), odd block boundary
+])
+def test_checkpointed_adjoint_matches_stored_slices(rng, grid, size, ds, every):
+    w = fields(grid, size, rng, amp=1.5, noise=0.3)
+    with ctx(grid, size, ds) as c:
+        F0 = c.forward(w)
+        g0 = c.backward()
+        c.set_adjoint_checkpoint(every)
+        F1 = c.forward(w)
+        g1 = c.backward()
+        g1b = c.backward()
+    assert abs(F1 - F0) < 1e-12 * max(1.0, abs(F0))
+    assert np.allclose(g1, g0, rtol=1e-10, atol=1e-12), (g0, g1)
+    assert np.array_equal(g1, g1b)
+
+
+def test_checkpointing_releases_and_restores_the_slices(rng):
+    grid, size, ds = (16, 16, 16), (3.5, 3.5, 3.5), 0.05
+    w = fields(grid, size, rng)
+    with ctx(grid, size, ds) as c:
+        c.forward(w)
+        g0 = c.backward()
+        c.set_adjoint_checkpoint(-1)
+        with pytest.raises(AdscfError):
+            c.propagate_diblock(w)             # the slices are released
+        with pytest.raises(AdscfError):
+            c.backward()                       # the forward predates the mode change
+        c.forward(w)
+        assert np.allclose(c.backward(), g0, rtol=1e-10, atol=1e-12)
+        c.set_adjoint_checkpoint(0)
+        c.forward(w)
+        assert np.array_equal(c.backward(), g0)   # the stored-slice pass again
+        c.set_field(w)
+        r = c.scf_run(3, tol=0.0)
+        assert np.isfinite(r.free_energy)
+    with ctx(grid, size, ds, prec=SPLIT) as c:
+        with pytest.raises(AdscfError):
+            c.set_adjoint_checkpoint(-1)
+
+
 def test_stress_at_saddle_matches_neighbouring_box_free_energies(rng):
     """At a converged (ordered) saddle point dF/dL_x equals the slope of the
     equilibrium free energy between neighbouring box sizes."""
