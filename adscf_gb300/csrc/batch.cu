@@ -24,6 +24,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -76,6 +77,9 @@ struct adscf_batch {
   int* d_list32 = nullptr;              // films sweeping in FP32 / FP64, by contour length
   int* d_list64 = nullptr;
   int n32 = 0, n64 = 0;
+  // shared-memory line sweeps: rows per line (max gz + 1 of the list) and
+  // lanes per block (0: the list sweeps on global memory)
+  int zcap32 = 0, zcap64 = 0, lanes32 = 0, lanes64 = 0;
   int* d_err = nullptr;                 // zero-pivot flag of the sweeps
   // FP64 bulk batches: host copies of the instances and the adjoint state
   std::vector<BulkDev<double>> hI64;
@@ -506,6 +510,25 @@ int build_film(adscf_batch* b) {
   std::stable_sort(l64.begin(), l64.end(), by_work);
   b->n32 = (int)l32.size();
   b->n64 = (int)l64.size();
+  // lanes per block of the shared-memory sweeps: one thread per (film,
+  // chain) runs a serial recurrence, so more, narrower blocks spread the
+  // chains over more of the SMs' schedulers; ADSCF_FILM_LANES overrides
+  {
+    int optin = 0;
+    BK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev));
+    int want = 8;
+    if (const char* e = std::getenv("ADSCF_FILM_LANES")) want = std::max(1, std::min(32, std::atoi(e)));
+    auto lanes = [&](const std::vector<int>& l, size_t es, int& zcap, int& W) {
+      zcap = 0;
+      for (int i : l) zcap = std::max(zcap, b->npts[i]);
+      W = want;
+      while (W > 0 && 2 * (size_t)zcap * W * es > (size_t)optin) W >>= 1;
+    };
+    lanes(l32, sizeof(float), b->zcap32, b->lanes32);
+    lanes(l64, sizeof(double), b->zcap64, b->lanes64);
+    BK(cudaFuncSetAttribute(k_film1d_chains_sm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    BK(cudaFuncSetAttribute(k_film1d_chains_sm<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  }
   BK(cudaMalloc(&b->d_f32, n * sizeof(FilmDev<float>)));
   BK(cudaMalloc(&b->d_f64, n * sizeof(FilmDev<double>)));
   BK(cudaMemcpyAsync(b->d_f32, f32.data(), n * sizeof(FilmDev<float>), cudaMemcpyHostToDevice, b->stream));
@@ -530,12 +553,22 @@ int enqueue_film(adscf_batch* b) {
   cudaStream_t s = b->stream;
   const FilmDev<float>* f32 = static_cast<const FilmDev<float>*>(b->d_f32);
   const FilmDev<double>* f64 = static_cast<const FilmDev<double>*>(b->d_f64);
-  if (b->n32)
+  if (b->n32 && b->lanes32) {
+    const int W = b->lanes32;
+    k_film1d_chains_sm<float><<<dim3((b->n32 + W - 1) / W, 2), W, 2 * (size_t)b->zcap32 * W * sizeof(float), s>>>(
+        f32, b->d_S, b->d_list32, b->n32, b->zcap32);
+  } else if (b->n32) {
     k_film1d_chains_b<float><<<dim3((b->n32 + FILM_THREADS - 1) / FILM_THREADS, 2), FILM_THREADS, 0, s>>>(
         f32, b->d_S, b->d_list32, b->n32);
-  if (b->n64)
+  }
+  if (b->n64 && b->lanes64) {
+    const int W = b->lanes64;
+    k_film1d_chains_sm<double><<<dim3((b->n64 + W - 1) / W, 2), W, 2 * (size_t)b->zcap64 * W * sizeof(double), s>>>(
+        f64, b->d_S, b->d_list64, b->n64, b->zcap64);
+  } else if (b->n64) {
     k_film1d_chains_b<double><<<dim3((b->n64 + FILM_THREADS - 1) / FILM_THREADS, 2), FILM_THREADS, 0, s>>>(
         f64, b->d_S, b->d_list64, b->n64);
+  }
   if (b->n32) k_film_contour_b<float><<<b->n32, 256, 0, s>>>(f32, b->d_list32);
   if (b->n64) k_film_contour_b<double><<<b->n64, 256, 0, s>>>(f64, b->d_list64);
   k_closure_b<<<dim3(1, b->n), SCF_THREADS, 0, s>>>(b->d_S, CL_MEANFIELD | CL_MIXDOTS);

@@ -34,6 +34,17 @@ int ensure_pinned(adscf_ctx* ctx, size_t bytes) {
   return ADSCF_OK;
 }
 
+// page-locked (cudaHostAlloc / cudaHostRegister) host memory: DMA copies go
+// to and from it directly, without the staging memcpy
+bool host_pinned(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 // host -> device through pinned staging (one cudaMemcpyAsync per copy)
 int h2d(adscf_ctx* ctx, double* d, const double* h, size_t n) {
   int rc = ensure_pinned(ctx, n * sizeof(double));
@@ -580,18 +591,26 @@ int adscf_scf_iteration(adscf_ctx* ctx, double* field, double* density, adscf_it
   CK(cudaStreamSynchronize(ctx->stream));
   const size_t nv = nvar(ctx);
   double* xk = hx_slot(ctx, k % ctx->hist_slots);
-  if ((rc = ensure_pinned(ctx, 2 * nv * sizeof(double)))) return rc;
-  std::memcpy(ctx->h_pinned, field, nv * sizeof(double));
-  CK(cudaMemcpyAsync(xk, ctx->h_pinned, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  // page-locked caller buffers are copied directly; others through staging
+  const bool pin = host_pinned(field) && host_pinned(density);
+  if (!pin) {
+    if ((rc = ensure_pinned(ctx, 2 * nv * sizeof(double)))) return rc;
+    std::memcpy(ctx->h_pinned, field, nv * sizeof(double));
+  }
+  double* hf = pin ? field : ctx->h_pinned;
+  double* hd = pin ? density : ctx->h_pinned + nv;
+  CK(cudaMemcpyAsync(xk, hf, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->geometry == ADSCF_BULK && (rc = bulk_enqueue_expfield(ctx, xk))) return rc;
   CK(cudaGraphLaunch(ctx->g_iter, ctx->stream));
   double* xn = hx_slot(ctx, (k + 1) % ctx->hist_slots);
-  CK(cudaMemcpyAsync(ctx->h_pinned, xn, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->h_pinned + nv, ctx->d_dens, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(hf, xn, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(hd, ctx->d_dens, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   adscf_iter_result r{};
   rc = read_result(ctx, &r, nullptr);  // synchronises the stream
-  std::memcpy(field, ctx->h_pinned, nv * sizeof(double));
-  std::memcpy(density, ctx->h_pinned + nv, nv * sizeof(double));
+  if (!pin) {
+    std::memcpy(field, ctx->h_pinned, nv * sizeof(double));
+    std::memcpy(density, ctx->h_pinned + nv, nv * sizeof(double));
+  }
   if (out) *out = r;
   return rc;
 }

@@ -359,6 +359,80 @@ k_film1d_chains_b(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__ 
   film1d_chain<T>(F, field, 0, blockIdx.y);
 }
 
+// One-line films of a batch with the line held in shared memory.  One thread
+// per (film, chain), blockIdx.y = chain; blockDim.x = W lanes.  The Thomas
+// sweep of film1d_chain runs on the same arithmetic in the same order, but q
+// is updated in place in shared memory (u_j replaces q_j once q_j and
+// q_{j+1} have been read) with the elimination factors beside it, both
+// interleaved [j][lane] so that a warp's accesses fall in distinct banks.
+// Only the finished slice goes to global memory (for the contour integral);
+// the sweep itself never waits on a global load of its own stores.
+// Shared memory: 2 zcap W elements, zcap >= gz + 1 of every listed film.
+template <typename T>
+__global__ void __launch_bounds__(32)
+k_film1d_chains_sm(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__ Ss,
+                   const int* __restrict__ films, int nf, int zcap) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int W = blockDim.x, lane = threadIdx.x;
+  const int k = blockIdx.x * W + lane;
+  if (k >= nf) return;
+  const int f = films[k];
+  const FilmDev<T> F = Fs[f];
+  const double* field = Ss[f].hx + (size_t)((*Ss[f].iter) % Ss[f].slots) * ((size_t)Ss[f].ntypes * Ss[f].npts);
+  T* qv = reinterpret_cast<T*>(smraw) + lane;
+  T* gv = qv + (size_t)zcap * W;
+  const int dir = blockIdx.y, gz = F.gz;
+  T* chain = dir == 0 ? F.q : F.qd;
+  for (int j = 0; j <= gz; ++j) {
+    const T v = (dir == 1 && F.brush) ? (T)F.graft[j] : (T)1;
+    qv[j * W] = v;
+    chain[j] = v;
+  }
+  for (int s = 1; s <= F.ns; ++s) {
+    const double ds = film_ds(F.dss, dir, s, F.ns);
+    const int ty = F.brush ? 0 : film_type(dir, s, F.ns, F.na);
+    const double* w = field + (size_t)ty * F.npts;
+    T* qn = chain + (size_t)s * F.npts;
+    T bet = (T)1, uprev = (T)0, cprev = (T)0;
+    T q_jm1 = qv[0], q_j = qv[W];
+    qv[0] = (T)0;
+#pragma unroll 4
+    for (int j = 1; j < gz; ++j) {
+      const T q_jp1 = qv[(j + 1) * W];
+      const T a = (T)(-ds * F.alpha[j]);
+      const T c = (T)(-ds * F.gamma[j]);
+      const T b = (T)(ds * F.beta[j]);
+      const T hw = (T)(0.5 * ds * w[j]);
+      const T diag = (T)1 + b + hw;
+      const T rhs = -a * q_jm1 + ((T)1 - b - hw) * q_j - c * q_jp1;
+      q_jm1 = q_j;
+      q_j = q_jp1;
+      const T g = cprev / bet;
+      bet = diag - a * g;
+      if (bet == (T)0) atomicOr(F.err, 1);
+      uprev = (rhs - a * uprev) / bet;
+      gv[j * W] = g;
+      qv[j * W] = uprev;
+      cprev = c;
+    }
+    {  // row gz: identity, zero right-hand side
+      const T g = cprev / bet;
+      bet = (T)1;
+      uprev = ((T)0 - (T)0 * uprev) / bet;
+      gv[gz * W] = g;
+    }
+    T unext = uprev;
+    qv[gz * W] = unext;
+    qn[gz] = unext;
+    for (int j = gz - 1; j >= 0; --j) {
+      const T u = qv[j * W] - gv[(j + 1) * W] * unext;
+      qv[j * W] = u;
+      qn[j] = u;
+      unext = u;
+    }
+  }
+}
+
 // one block per film of the list
 template <typename T>
 __global__ void __launch_bounds__(256)

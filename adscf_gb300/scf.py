@@ -264,8 +264,16 @@ class Context:
         self._ck(self.lib.adscf_backward(self.h, L.dptr(g)))
         return g
 
-    def scf_iteration(self, field, density_out=None):
-        x = _f64(field).copy()
+    def scf_iteration(self, field, density_out=None, inplace=False):
+        """One iteration with host buffers (adscf_scf_iteration).  With
+        ``inplace`` the float64 C-contiguous ``field`` itself is advanced, so
+        a page-locked array is copied by DMA without staging."""
+        if inplace:
+            if field.dtype != np.float64 or not field.flags.c_contiguous or field.size != self.ntypes * self.npts:
+                raise ValueError("inplace needs a C-contiguous float64 field of ntypes * npts values")
+            x = field
+        else:
+            x = _f64(field).copy()
         d = np.empty_like(x) if density_out is None else density_out
         res = L.IterResult()
         self._ck(self.lib.adscf_scf_iteration(self.h, L.dptr(x), L.dptr(d), C.byref(res)))

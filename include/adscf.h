@@ -194,7 +194,9 @@ ADSCF_API int adscf_get_density(adscf_ctx *ctx, double *density); /* newest phi 
 ADSCF_API int adscf_scf_run(adscf_ctx *ctx, int n_iter, double tol,
                   adscf_iter_result *out);
 /* one iteration with host buffers: field in (x_k) -> field out (x_{k+1}),
- * density out (phi[x_k]); the call a Fortran SCF loop makes per iteration */
+ * density out (phi[x_k]); the call a Fortran SCF loop makes per iteration.
+ * Page-locked buffers (cudaHostAlloc / cudaHostRegister) are copied by DMA
+ * directly; pageable ones go through the context's pinned staging buffer. */
 ADSCF_API int adscf_scf_iteration(adscf_ctx *ctx, double *field, double *density,
                         adscf_iter_result *out);
 

@@ -191,6 +191,20 @@ def test_scf_iteration_host_buffers(rng):
         x2, d2, res = c.scf_iteration(field.reshape(-1))
     assert res.iter == 1
     assert np.array_equal(x1, x2) and np.array_equal(d1, d2)
+    # page-locked buffers advanced in place (DMA without staging)
+    import torch
+    xp = torch.empty(field.size, dtype=torch.float64, pin_memory=True).numpy()
+    dp = torch.empty(field.size, dtype=torch.float64, pin_memory=True).numpy()
+    xp[:] = field.reshape(-1)
+    with mkctx(grid, mixing_type=MIX_ANDERSON, mixing_dim=2) as c:
+        c.set_field(field)
+        x3, d3, _r = c.scf_iteration(xp, dp, inplace=True)
+        x4, d4, _r = c.scf_iteration(x2.copy())       # the pageable path continues the same loop
+    assert x3 is xp and np.array_equal(xp, x2) and np.array_equal(dp, d2)
+    with mkctx(grid, mixing_type=MIX_ANDERSON, mixing_dim=2) as c:
+        c.set_field(field)
+        c.scf_run(2)
+        assert np.array_equal(c.get_field(), x4) and np.array_equal(c.get_density(), d4)
 
 
 def test_bad_arguments_return_status():
