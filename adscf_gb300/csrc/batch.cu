@@ -80,6 +80,8 @@ struct adscf_batch {
   // shared-memory line sweeps: rows per line (max gz + 1 of the list) and
   // lanes per block (0: the list sweeps on global memory)
   int zcap32 = 0, zcap64 = 0, lanes32 = 0, lanes64 = 0;
+  int film_per_warp = 2, film_warps = 2;
+  float* d_tabf = nullptr;              // FP32 mesh factors of the FP32 sweeps
   int* d_err = nullptr;                 // zero-pivot flag of the sweeps
   // FP64 bulk batches: host copies of the instances and the adjoint state
   std::vector<BulkDev<double>> hI64;
@@ -359,6 +361,12 @@ int check_film(const adscf_params& q, int prec, int geom, std::string& why) {
 
 // Film batch: one line per film; tables (coefficients, weights, schedules,
 // wall potentials) in one FP64 array, propagators and SCF state in the pool.
+// shared memory of k_film1d_chains_sm: q, gam and the eliminated right-hand
+// side, and the FP32 field of both types for FP32 sweeps
+size_t film_sweep_smem(int zcap, int W, size_t es) {
+  return 3 * (size_t)zcap * W * es + (es == 4 ? 2 * (size_t)zcap * W * sizeof(float) : 0);
+}
+
 int build_film(adscf_batch* b) {
   const int n = b->n;
   const int geom = b->p[0].geometry;
@@ -414,6 +422,18 @@ int build_film(adscf_batch* b) {
   BK(cudaMalloc(&b->d_fk, tab.size() * sizeof(double)));
   BK(cudaMemcpyAsync(b->d_fk, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, b->stream));
   const double* dtab = static_cast<const double*>(b->d_fk);
+  // FP32 mesh factors of the FP32 sweeps: al, be, ga [npts] per film
+  std::vector<float> tabf;
+  std::vector<size_t> tof(n, SIZE_MAX);
+  for (int i = 0; i < n; ++i) {
+    if (t64[i]) continue;
+    tof[i] = tabf.size();
+    for (const std::vector<double>* v : {&tb[i].al, &tb[i].be, &tb[i].ga})
+      for (size_t j = 0; j < b->npts[i]; ++j) tabf.push_back((float)(*v)[j]);
+  }
+  BK(cudaMalloc(&b->d_tabf, std::max<size_t>(1, tabf.size()) * sizeof(float)));
+  if (!tabf.empty())
+    BK(cudaMemcpyAsync(b->d_tabf, tabf.data(), tabf.size() * sizeof(float), cudaMemcpyHostToDevice, b->stream));
   // pool
   Carve c;
   struct Off { size_t q, qd, gam, dist, dens, hx, hr, qpart, part, gram, coef; };
@@ -468,6 +488,10 @@ int build_film(adscf_batch* b) {
       D.err = b->d_err;
       D.dx = q.sizex; D.dy = q.sizey;
       D.w1 = nullptr;
+      D.alf = tof[i] == SIZE_MAX ? nullptr : b->d_tabf + tof[i];
+      D.bef = tof[i] == SIZE_MAX ? nullptr : b->d_tabf + tof[i] + np;
+      D.gaf = tof[i] == SIZE_MAX ? nullptr : b->d_tabf + tof[i] + 2 * np;
+      D.wf = nullptr;   // the batch sweep keeps the FP32 field in shared memory
     };
     if (t64[i]) { fill(f64[i]); l64.push_back(i); }
     else { fill(f32[i]); l32.push_back(i); }
@@ -510,19 +534,26 @@ int build_film(adscf_batch* b) {
   std::stable_sort(l64.begin(), l64.end(), by_work);
   b->n32 = (int)l32.size();
   b->n64 = (int)l64.size();
-  // lanes per block of the shared-memory sweeps: one thread per (film,
-  // chain) runs a serial recurrence, so more, narrower blocks spread the
-  // chains over more of the SMs' schedulers; ADSCF_FILM_LANES overrides
+  // layout of the shared-memory sweeps: one thread per (film, chain) runs a
+  // serial recurrence, so the first `per_warp` lanes of each warp work and
+  // a block holds `warps` warps: W = warps * per_warp lines share the
+  // block's shared memory.  ADSCF_FILM_LANES / ADSCF_FILM_WARPS override.
   {
     int optin = 0;
     BK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev));
-    int want = 8;
-    if (const char* e = std::getenv("ADSCF_FILM_LANES")) want = std::max(1, std::min(32, std::atoi(e)));
+    b->film_per_warp = 2;
+    b->film_warps = 2;
+    if (const char* e = std::getenv("ADSCF_FILM_LANES")) b->film_per_warp = std::max(1, std::min(32, std::atoi(e)));
+    if (const char* e = std::getenv("ADSCF_FILM_WARPS")) b->film_warps = std::max(1, std::min(8, std::atoi(e)));
     auto lanes = [&](const std::vector<int>& l, size_t es, int& zcap, int& W) {
       zcap = 0;
       for (int i : l) zcap = std::max(zcap, b->npts[i]);
-      W = want;
-      while (W > 0 && 2 * (size_t)zcap * W * es > (size_t)optin) W >>= 1;
+      W = b->film_warps * b->film_per_warp;
+      // fewer warps while a block's lines do not fit (W = 0: global sweep)
+      int warps = b->film_warps;
+      while (warps > 0 && film_sweep_smem(zcap, warps * b->film_per_warp, es) > (size_t)optin) --warps;
+      W = warps * b->film_per_warp;
+      if (warps == 0) W = 0;
     };
     lanes(l32, sizeof(float), b->zcap32, b->lanes32);
     lanes(l64, sizeof(double), b->zcap64, b->lanes64);
@@ -553,18 +584,21 @@ int enqueue_film(adscf_batch* b) {
   cudaStream_t s = b->stream;
   const FilmDev<float>* f32 = static_cast<const FilmDev<float>*>(b->d_f32);
   const FilmDev<double>* f64 = static_cast<const FilmDev<double>*>(b->d_f64);
+  const int pw = b->film_per_warp;
   if (b->n32 && b->lanes32) {
     const int W = b->lanes32;
-    k_film1d_chains_sm<float><<<dim3((b->n32 + W - 1) / W, 2), W, 2 * (size_t)b->zcap32 * W * sizeof(float), s>>>(
-        f32, b->d_S, b->d_list32, b->n32, b->zcap32);
+    k_film1d_chains_sm<float><<<dim3((b->n32 + W - 1) / W, 2), 32 * (W / pw),
+                                film_sweep_smem(b->zcap32, W, sizeof(float)), s>>>(
+        f32, b->d_S, b->d_list32, b->n32, b->zcap32, pw);
   } else if (b->n32) {
     k_film1d_chains_b<float><<<dim3((b->n32 + FILM_THREADS - 1) / FILM_THREADS, 2), FILM_THREADS, 0, s>>>(
         f32, b->d_S, b->d_list32, b->n32);
   }
   if (b->n64 && b->lanes64) {
     const int W = b->lanes64;
-    k_film1d_chains_sm<double><<<dim3((b->n64 + W - 1) / W, 2), W, 2 * (size_t)b->zcap64 * W * sizeof(double), s>>>(
-        f64, b->d_S, b->d_list64, b->n64, b->zcap64);
+    k_film1d_chains_sm<double><<<dim3((b->n64 + W - 1) / W, 2), 32 * (W / pw),
+                                 film_sweep_smem(b->zcap64, W, sizeof(double)), s>>>(
+        f64, b->d_S, b->d_list64, b->n64, b->zcap64, pw);
   } else if (b->n64) {
     k_film1d_chains_b<double><<<dim3((b->n64 + FILM_THREADS - 1) / FILM_THREADS, 2), FILM_THREADS, 0, s>>>(
         f64, b->d_S, b->d_list64, b->n64);
@@ -994,6 +1028,7 @@ int adscf_batch_destroy(adscf_batch* b) {
   cudaFree(b->d_tw); cudaFree(b->d_fk); cudaFree(b->d_g64);
   for (auto& C : b->cls) { cudaFree(C.wx); cudaFree(C.wy); cudaFree(C.wz); }
   cudaFree(b->d_f32); cudaFree(b->d_f64); cudaFree(b->d_list32); cudaFree(b->d_list64);
+  cudaFree(b->d_tabf);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
   delete b;

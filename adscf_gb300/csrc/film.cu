@@ -19,12 +19,15 @@ struct FilmState {
   double* d_wA = nullptr;
   double* d_wB = nullptr;
   double* d_graft = nullptr;
+  float* d_alf = nullptr;       // FP32 mesh factors and field of FP32 line sweeps
+  float* d_wf = nullptr;
   void* d_q = nullptr;
   void* d_qd = nullptr;
   void* d_gam = nullptr;
   void* d_w1 = nullptr;
   int* d_err = nullptr;
   double max_ratio = 1.0;       // largest neighbour spacing ratio of the mesh
+  int optin = 0;                // opt-in shared memory per block
   // free energy at fixed fields and its wall-potential gradient
   double* d_fe_w = nullptr;     // [ntypes][npts] field copy
   double* d_fe_part = nullptr;  // [nplanes][FE_N]
@@ -53,6 +56,36 @@ FieldRef make_ref(adscf_ctx* ctx, const double* d_w) {
   return r;
 }
 
+// grids, lanes per block and shared memory of the three ADI sweeps: lines of
+// gx, gy and gz + 1 points per lane.  Each lane runs a serial recurrence, so
+// FILM_THREADS lanes are halved until the blocks cover every SM twice (152
+// SMs) and a block's lines fit in shared memory.
+struct AdiLaunch {
+  dim3 gx, gy, gz;
+  int wx, wy, wz;
+  size_t sx, sy, sz;
+};
+template <typename T>
+AdiLaunch adi_launch(const FilmState* F, const FilmDev<T>& D, int chains) {
+  AdiLaunch A;
+  auto lanes = [&](int n, size_t per, int nl) {
+    int W = FILM_THREADS;
+    while (W > 1 && (per * n * W * sizeof(T) > (size_t)F->optin || (size_t)((nl + W - 1) / W) * chains < 2 * 152))
+      W >>= 1;
+    return W;
+  };
+  A.wx = lanes(D.gx, 3, D.gy * (D.gz - 1));
+  A.wy = lanes(D.gy, 3, D.gx * (D.gz - 1));
+  A.wz = lanes(D.gz + 1, 2, D.nlines);
+  A.sx = adi_smem(D.gx, A.wx, sizeof(T));
+  A.sy = adi_smem(D.gy, A.wy, sizeof(T));
+  A.sz = 2 * (size_t)(D.gz + 1) * A.wz * sizeof(T);
+  A.gx = dim3((D.gy * (D.gz - 1) + A.wx - 1) / A.wx, chains);
+  A.gy = dim3((D.gx * (D.gz - 1) + A.wy - 1) / A.wy, chains);
+  A.gz = dim3((D.nlines + A.wz - 1) / A.wz, chains);
+  return A;
+}
+
 template <typename T>
 int chains_t(adscf_ctx* ctx, const double* d_w) {
   FilmState* F = ctx->film;
@@ -62,15 +95,21 @@ int chains_t(adscf_ctx* ctx, const double* d_w) {
   if (ctx->geometry == ADSCF_FILM_3D) {
     // node 0 of both chains = 1, then ns Douglas ADI steps (three sweeps each)
     k_film_fill<T><<<std::max(1, (D.npts + 255) / 256), 256, 0, s>>>(D.q, D.qd, D.npts);
-    const dim3 gx_((D.gy * (D.gz - 1) + FILM_THREADS - 1) / FILM_THREADS, 2);
-    const dim3 gy_((D.gx * (D.gz - 1) + FILM_THREADS - 1) / FILM_THREADS, 2);
-    const dim3 gz_((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 2);
+    if (sizeof(T) == 4) {
+      const size_t n = (size_t)ctx->ntypes * D.npts;
+      k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
+    }
+    const AdiLaunch A = adi_launch<T>(F, D, 2);
     for (int st = 1; st <= D.ns; ++st) {
-      k_adi_x<T><<<gx_, FILM_THREADS, 0, s>>>(D, fr, st);
-      k_adi_y<T><<<gy_, FILM_THREADS, 0, s>>>(D, st);
-      k_adi_z<T><<<gz_, FILM_THREADS, 0, s>>>(D, fr, st);
+      k_adi_x<T><<<A.gx, A.wx, A.sx, s>>>(D, fr, st);
+      k_adi_y<T><<<A.gy, A.wy, A.sy, s>>>(D, st);
+      k_adi_z<T><<<A.gz, A.wz, A.sz, s>>>(D, fr, st);
     }
   } else {
+    if (sizeof(T) == 4) {
+      const size_t n = (size_t)ctx->ntypes * D.npts;
+      k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
+    }
     const dim3 g((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 2);
     k_film1d_chains<T><<<g, FILM_THREADS, 0, s>>>(D, fr);
   }
@@ -106,13 +145,15 @@ int step_single_t(adscf_ctx* ctx, double* d_prop, const double* d_w, double ds) 
   FieldRef fr{};
   fr.direct = d_w;
   if (ctx->geometry == ADSCF_FILM_3D) {
-    const dim3 gx_((D.gy * (D.gz - 1) + FILM_THREADS - 1) / FILM_THREADS, 1);
-    const dim3 gy_((D.gx * (D.gz - 1) + FILM_THREADS - 1) / FILM_THREADS, 1);
-    const dim3 gz_((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 1);
-    k_adi_x<T><<<gx_, FILM_THREADS, 0, s>>>(D, fr, 1);
-    k_adi_y<T><<<gy_, FILM_THREADS, 0, s>>>(D, 1);
-    k_adi_z<T><<<gz_, FILM_THREADS, 0, s>>>(D, fr, 1);
+    if (sizeof(T) == 4)   // one field (type 0) of npts values
+      k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
+    const AdiLaunch A = adi_launch<T>(F, D, 1);
+    k_adi_x<T><<<A.gx, A.wx, A.sx, s>>>(D, fr, 1);
+    k_adi_y<T><<<A.gy, A.wy, A.sy, s>>>(D, 1);
+    k_adi_z<T><<<A.gz, A.wz, A.sz, s>>>(D, fr, 1);
   } else {
+    if (sizeof(T) == 4)   // one field (type 0) of npts values
+      k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
     const dim3 g((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 1);
     k_film1d_chains<T><<<g, FILM_THREADS, 0, s>>>(D, fr);
   }
@@ -158,6 +199,11 @@ void fill_dev(adscf_ctx* ctx, FilmState* F, const adscf_params* p) {
   D.dx = p->sizex / p->gx;
   D.dy = p->sizey / p->gy;
   D.w1 = static_cast<T*>(F->d_w1);
+  const size_t n1 = (size_t)ctx->gz + 1;
+  D.alf = F->d_alf;
+  D.bef = F->d_alf ? F->d_alf + n1 : nullptr;
+  D.gaf = F->d_alf ? F->d_alf + 2 * n1 : nullptr;
+  D.wf = F->d_wf;
 }
 
 }  // namespace
@@ -213,6 +259,30 @@ int film_create(adscf_ctx* ctx, const adscf_params* p) {
     if (!p->graft) return set_err(ctx, ADSCF_E_ARG, "brush needs the grafting distribution");
     CK(cudaMalloc(&F->d_graft, (gz + 1) * sizeof(double)));
     CK(cudaMemcpy(F->d_graft, p->graft, (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  CK(cudaDeviceGetAttribute(&F->optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->dev));
+  if (ctx->geometry == ADSCF_FILM_3D) {
+    const size_t es = F->t64 ? sizeof(double) : sizeof(float);
+    const int nmax = std::max(ctx->gx, std::max(ctx->gy, gz + 1));
+    if (adi_smem(nmax, 1, es) > (size_t)F->optin) return set_err(ctx, ADSCF_E_ARG, "ADI line too long for shared memory");
+    // shared memory is a per-function limit set in the launching file
+    CK(cudaFuncSetAttribute(k_adi_x<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, F->optin));
+    CK(cudaFuncSetAttribute(k_adi_y<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, F->optin));
+    CK(cudaFuncSetAttribute(k_adi_z<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, F->optin));
+    CK(cudaFuncSetAttribute(k_adi_x<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, F->optin));
+    CK(cudaFuncSetAttribute(k_adi_y<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, F->optin));
+    CK(cudaFuncSetAttribute(k_adi_z<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, F->optin));
+  }
+  if (!F->t64) {
+    std::vector<float> f3(3 * (size_t)(gz + 1));
+    for (int j = 0; j <= gz; ++j) {
+      f3[j] = (float)al[j];
+      f3[gz + 1 + j] = (float)be[j];
+      f3[2 * (gz + 1) + j] = (float)ga[j];
+    }
+    CK(cudaMalloc(&F->d_alf, f3.size() * sizeof(float)));
+    CK(cudaMemcpy(F->d_alf, f3.data(), f3.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&F->d_wf, (size_t)ctx->ntypes * ctx->npts * sizeof(float)));
   }
   ctx->contour_blocks = (int)std::min<size_t>(((size_t)ctx->npts + 255) / 256, 152 * 4);
   CK(cudaMalloc(&ctx->d_qpart, ctx->contour_blocks * sizeof(double)));
@@ -276,6 +346,7 @@ void film_destroy(adscf_ctx* ctx) {
   cudaFree(F->d_fe_w); cudaFree(F->d_fe_part); cudaFree(F->d_fe_out);
   cudaFree(F->d_alpha); cudaFree(F->d_beta); cudaFree(F->d_gamma);
   cudaFree(F->d_dss); cudaFree(F->d_wA); cudaFree(F->d_wB); cudaFree(F->d_graft);
+  cudaFree(F->d_alf); cudaFree(F->d_wf);
   cudaFree(F->d_q); cudaFree(F->d_qd); cudaFree(F->d_gam); cudaFree(F->d_w1);
   cudaFree(F->d_err); cudaFree(ctx->d_qpart);
   delete F;

@@ -59,7 +59,110 @@ struct FilmDev {
   // ADI (Film_3D) only
   double dx, dy;
   T* w1;                 // [2][npts] intermediate q*, q** of the ADI sweeps
+  // FP32 line sweeps (1D chains): FP32 copies of the mesh factors and, for
+  // single contexts, of the field ([ntypes][npts], filled per propagation)
+  const float* alf;
+  const float* bef;
+  const float* gaf;
+  float* wf;
 };
+
+// ---------------------------------------------------------------------------
+// Coefficients of CN row j at step size ds: a = -ds alpha_j, c = -ds gamma_j,
+// b = ds beta_j and hw = ds w_j / 2.  FP64 sweeps form each product in FP64
+// and round once.  FP32 sweeps multiply FP32 copies of the mesh factors and
+// of the field by the FP32 step: at most one more rounding per factor, on a
+// sweep that rounds every operation at that level.  Two FP64 products and a
+// conversion per factor per row would make the FP32 sweeps wait on GB300's
+// narrow FP64 pipe.
+// ---------------------------------------------------------------------------
+// Right-hand side of CN row j.  FP64 sweeps use the reference's form,
+// -a q_{j-1} + (1 - b - hw) q_j - c q_{j+1}.  FP32 sweeps solve for the
+// increment u = q' - q of the step instead: the same matrix with right-hand
+// side -2 [a (q_{j-1} - q_j) + c (q_{j+1} - q_j) + hw q_j] (b = -(a + c)
+// exactly in the mesh formulas), and rows 0 and gz give u = -q.  The
+// differences keep a constant profile invariant under the rounded
+// coefficients, and the solve's rounding is relative to the O(ds) increment
+// rather than to the O(ds/dz^2) matrix entries, which would otherwise bias
+// the decay of smooth modes coherently over the contour.
+// Explicitly rounded arithmetic of the 1D line sweeps.  The single-context
+// and the batched kernels inline the same sweep into different code; with
+// every operation rounded explicitly no contraction choice of the compiler
+// can make the two differ, and a batched film follows its single context
+// bit for bit in either precision.
+__device__ __forceinline__ float r_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double r_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float r_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double r_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float r_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double r_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float r_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double r_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float r_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double r_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <typename T>
+__device__ __forceinline__ T cn_rhs(T a, T b, T c, T hw, T qm, T q0, T qp) {
+  if constexpr (sizeof(T) == 4) {
+    T t = r_mul(hw, q0);
+    t = r_fma(c, r_sub(qp, q0), t);
+    t = r_fma(a, r_sub(qm, q0), t);
+    return r_mul((T)-2, t);
+  } else {
+    T t = r_mul(-a, qm);
+    t = r_fma(r_sub(r_sub((T)1, b), hw), q0, t);
+    return r_fma(-c, qp, t);
+  }
+}
+
+struct CnStep {
+  double ds;
+  float dsf, hdsf;       // (float)ds, (float)(ds / 2)
+};
+__device__ __forceinline__ CnStep cn_step(double ds) {
+  return CnStep{ds, (float)ds, (float)(0.5 * ds)};
+}
+template <typename T>
+__device__ __forceinline__ void cn_row(const FilmDev<T>& F, const CnStep& st, int j, double w64, float w32,
+                                       T& a, T& c, T& b, T& hw) {
+  if constexpr (sizeof(T) == 4) {
+    a = r_mul(-st.dsf, F.alf[j]);
+    c = r_mul(-st.dsf, F.gaf[j]);
+    b = r_mul(st.dsf, F.bef[j]);
+    hw = r_mul(st.hdsf, w32);
+  } else {
+    a = (T)(-st.ds * F.alpha[j]);
+    c = (T)(-st.ds * F.gamma[j]);
+    b = (T)(st.ds * F.beta[j]);
+    hw = (T)(0.5 * st.ds * w64);
+  }
+}
+
+// One row of the Thomas elimination: returns gam_j and advances the pivot
+// state, the eliminated right-hand side and c_{j-1}.  FP64 divides by the
+// pivot (bet = pivot); FP32 keeps its correctly rounded reciprocal (bet =
+// 1 / pivot) and multiplies, one reciprocal instead of two divisions per row
+// (the FP32 sweeps are bound by instruction issue).  Row 0 starts from
+// bet = 1 in both forms.
+template <typename T>
+__device__ __forceinline__ T thomas_row(T& bet, T& cprev, T& uprev, T a, T c, T diag, T rhs, int* err) {
+  if constexpr (sizeof(T) == 4) {
+    const T g = r_mul(cprev, bet);
+    const T piv = r_fma(-a, g, diag);
+    if (piv == (T)0) atomicOr(err, 1);
+    bet = __frcp_rn(piv);
+    uprev = r_mul(r_fma(-a, uprev, rhs), bet);
+    cprev = c;
+    return g;
+  } else {
+    const T g = r_div(cprev, bet);
+    bet = r_fma(-a, g, diag);
+    if (bet == (T)0) atomicOr(err, 1);
+    uprev = r_div(r_fma(-a, uprev, rhs), bet);
+    cprev = c;
+    return g;
+  }
+}
 
 // chain type of step s: forward A then B, backward B then A
 __device__ __forceinline__ int film_type(int dir, int s, int ns, int na) {
@@ -88,48 +191,53 @@ __device__ __forceinline__ void film1d_chain(const FilmDev<T>& F, const double* 
     for (int j = 0; j <= gz; ++j)
       chain[(size_t)j * L + line] = (dir == 1 && F.brush) ? (T)F.graft[j] : (T)1;
   for (int s = 1; s <= F.ns; ++s) {
-    const double ds = film_ds(F.dss, dir, s, F.ns);
+    const CnStep st = cn_step(film_ds(F.dss, dir, s, F.ns));
     const int ty = (F.brush || F.single) ? 0 : film_type(dir, s, F.ns, F.na);
     const double* w = field + (size_t)ty * F.npts;
+    const float* wl = sizeof(T) == 4 ? F.wf + (size_t)ty * F.npts : nullptr;
     const T* qp = chain + (size_t)(s - 1) * F.npts;
     T* qn = chain + (size_t)s * F.npts;
-    // forward elimination
+    // forward elimination (increment form for FP32 sweeps, see cn_rhs)
+    constexpr bool inc = sizeof(T) == 4;
     T bet = (T)1;            // row 0: identity
-    T uprev = (T)0;          // u_0 = 0 (zero right-hand side)
-    qn[line] = (T)0;
-    T cprev = (T)0;          // c_0 = 0
     T q_jm1 = qp[line], q_j = qp[(size_t)L + line];
+    T uprev = inc ? -q_jm1 : (T)0;   // zero right-hand side (increment: -q_0)
+    qn[line] = uprev;
+    T cprev = (T)0;          // c_0 = 0
     for (int j = 1; j <= gz; ++j) {
       T a, c, diag, rhs;
       if (j < gz) {
         const T q_jp1 = qp[(size_t)(j + 1) * L + line];
-        a = (T)(-ds * F.alpha[j]);
-        c = (T)(-ds * F.gamma[j]);
-        const T b = (T)(ds * F.beta[j]);
-        const T hw = (T)(0.5 * ds * w[(size_t)j * L + line]);
-        diag = (T)1 + b + hw;
-        rhs = -a * q_jm1 + ((T)1 - b - hw) * q_j - c * q_jp1;
+        const size_t i = (size_t)j * L + line;
+        T b, hw;
+        cn_row<T>(F, st, j, sizeof(T) == 4 ? 0.0 : w[i], sizeof(T) == 4 ? wl[i] : 0.f, a, c, b, hw);
+        diag = r_add(r_add((T)1, b), hw);
+        rhs = cn_rhs<T>(a, b, c, hw, q_jm1, q_j, q_jp1);
         q_jm1 = q_j;
         q_j = q_jp1;
       } else {
-        a = (T)0; c = (T)0; diag = (T)1; rhs = (T)0;
+        a = (T)0; c = (T)0; diag = (T)1; rhs = inc ? -q_j : (T)0;
       }
-      const T g = cprev / bet;
-      bet = diag - a * g;
-      if (bet == (T)0) atomicOr(F.err, 1);
-      uprev = (rhs - a * uprev) / bet;
-      gam[(size_t)j * L + line] = g;
+      gam[(size_t)j * L + line] = thomas_row<T>(bet, cprev, uprev, a, c, diag, rhs, F.err);
       qn[(size_t)j * L + line] = uprev;
-      cprev = c;
     }
-    // back substitution u_j -= gam_{j+1} u_{j+1}
+    // back substitution u_j -= gam_{j+1} u_{j+1} (increment: q' = q + u)
     T unext = uprev;
+    if (inc) qn[(size_t)gz * L + line] = r_add(q_j, unext);
     for (int j = gz - 1; j >= 0; --j) {
-      const T u = qn[(size_t)j * L + line] - gam[(size_t)(j + 1) * L + line] * unext;
-      qn[(size_t)j * L + line] = u;
+      const size_t i = (size_t)j * L + line;
+      const T u = r_fma(-gam[i + L], unext, qn[i]);
+      qn[i] = inc ? r_add(qp[i], u) : u;
       unext = u;
     }
   }
+}
+
+// FP32 copy of the current field for the FP32 line sweeps of a single context
+static __global__ void k_film_wconv(FieldRef fr, float* __restrict__ wf, size_t n) {
+  const double* w = fr.get();
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    wf[i] = (float)w[i];
 }
 
 template <typename T>
@@ -185,19 +293,38 @@ __device__ __forceinline__ void cyclic_solve(const T a, const T b, const T c, in
   for (int j = 0; j < n; ++j) out[j * os] = out[j * os] - fact * z[j * gs];
 }
 
+// The three sweeps keep each thread's line in shared memory, interleaved
+// [point][lane] (blockDim.x = W lanes, conflict-free): the right-hand side
+// is formed there, solved in place, and written out once, so the serial
+// recurrences wait on shared-memory latency instead of on global loads of
+// their own stores.  Shared memory per block: adi_smem(n, W, sizeof(T)).
+__host__ __device__ __forceinline__ size_t adi_smem(int n, int W, size_t es) { return 3 * (size_t)n * W * es; }
+
+// FP32 sweeps read the FP32 field copy; FP64 sweeps the field
+template <typename T>
+__device__ __forceinline__ T adi_dsw(const FilmDev<T>& F, const CnStep& st, const double* w, int ty, size_t i) {
+  if constexpr (sizeof(T) == 4) return st.dsf * F.wf[(size_t)ty * F.npts + i];
+  else return (T)(st.ds * w[i]);
+}
+
 // x sweep: (1 - ds Dxx/2) q* = [1 + ds Dxx/2 + ds Dyy + ds Dzz - ds w] q  (:90-102)
 // one thread per (y, z interior); q* written to w1.
 template <typename T>
 __global__ void __launch_bounds__(FILM_THREADS)
 k_adi_x(FilmDev<T> F, FieldRef fr, int s) {
-  const int gx = F.gx, gy = F.gy, gz = F.gz, L = F.nlines;
-  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int gx = F.gx, gy = F.gy, gz = F.gz, L = F.nlines, W = blockDim.x;
+  const int id = blockIdx.x * W + threadIdx.x;
   const int dir = blockIdx.y;
   if (id >= gy * (gz - 1)) return;
+  T* r = reinterpret_cast<T*>(smraw) + threadIdx.x;
+  T* gs = r + (size_t)gx * W;
+  T* zs = gs + (size_t)gx * W;
   const int y = id % gy, z = 1 + id / gy;
   const double ds = film_ds(F.dss, dir, s, F.ns);
+  const CnStep st = cn_step(ds);
   const int ty = (F.brush || F.single) ? 0 : film_type(dir, s, F.ns, F.na);
-  const double* w = fr.get() + (size_t)ty * F.npts;
+  const double* w = sizeof(T) == 4 ? nullptr : fr.get() + (size_t)ty * F.npts;
   const T* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;
   T* out = F.w1 + (size_t)dir * F.npts;
   const T ax = (T)(-ds / F.dx / F.dx / 2.0), bx = (T)(ds / F.dx / F.dx), cx = ax;
@@ -205,21 +332,22 @@ k_adi_x(FilmDev<T> F, FieldRef fr, int s) {
   const T az = (T)(-ds * F.alpha[z]), bz = (T)(ds * F.beta[z]), cz = (T)(-ds * F.gamma[z]);
   const int ym = (y + gy - 1) % gy, yp = (y + 1) % gy;
   const size_t row = (size_t)z * L + (size_t)y * gx;
-  // right-hand side into the output row (then solved in place)
   for (int x = 0; x < gx; ++x) {
     const int xm = (x + gx - 1) % gx, xp = (x + 1) % gx;
     const T c0 = p0[row + x];
-    const T r = -ax * p0[row + xm] - (T)2 * ay * p0[(size_t)z * L + (size_t)ym * gx + x] -
-                (T)2 * az * p0[(size_t)(z - 1) * L + (size_t)y * gx + x] - cx * p0[row + xp] -
-                (T)2 * cy * p0[(size_t)z * L + (size_t)yp * gx + x] -
-                (T)2 * cz * p0[(size_t)(z + 1) * L + (size_t)y * gx + x] +
-                ((T)1 - bx - by * (T)2 - bz * (T)2 - (T)(ds * w[row + x])) * c0;
-    out[row + x] = r;
+    const T qxm = p0[row + xm], qxp = p0[row + xp];
+    const T qym = p0[(size_t)z * L + (size_t)ym * gx + x], qyp = p0[(size_t)z * L + (size_t)yp * gx + x];
+    const T qzm = p0[(size_t)(z - 1) * L + (size_t)y * gx + x], qzp = p0[(size_t)(z + 1) * L + (size_t)y * gx + x];
+    const T dsw = adi_dsw<T>(F, st, w, ty, row + x);
+    if constexpr (sizeof(T) == 4)   // increment q* - q (b = -(a + c) on every axis; see cn_rhs)
+      r[x * W] = (T)-2 * (ax * (qxm - c0) + cx * (qxp - c0) + ay * (qym - c0) + cy * (qyp - c0) +
+                          az * (qzm - c0) + cz * (qzp - c0)) - dsw * c0;
+    else
+      r[x * W] = -ax * qxm - (T)2 * ay * qym - (T)2 * az * qzm - cx * qxp - (T)2 * cy * qyp - (T)2 * cz * qzp +
+                 ((T)1 - bx - by * (T)2 - bz * (T)2 - dsw) * c0;
   }
-  // scratch for this line: gam and z vectors in the gam buffer, [x][line id]
-  T* gbase = F.gam + (size_t)dir * 2 * (size_t)gx * (gy * (gz - 1)) ;
-  cyclic_solve<T>(ax, (T)1 + bx, cx, gx, out + row, 1, out + row, 1, gbase + id,
-                  gbase + (size_t)gx * (gy * (gz - 1)) + id, (size_t)(gy * (gz - 1)), F.err);
+  cyclic_solve<T>(ax, (T)1 + bx, cx, gx, r, W, r, W, gs, zs, W, F.err);
+  for (int x = 0; x < gx; ++x) out[row + x] = sizeof(T) == 4 ? p0[row + x] + r[x * W] : r[x * W];
 }
 
 // y sweep: (1 - ds Dyy/2) q** = q* - ds Dyy q / 2  (:108-119); one thread
@@ -227,10 +355,14 @@ k_adi_x(FilmDev<T> F, FieldRef fr, int s) {
 template <typename T>
 __global__ void __launch_bounds__(FILM_THREADS)
 k_adi_y(FilmDev<T> F, int s) {
-  const int gx = F.gx, gy = F.gy, gz = F.gz, L = F.nlines;
-  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int gx = F.gx, gy = F.gy, gz = F.gz, L = F.nlines, W = blockDim.x;
+  const int id = blockIdx.x * W + threadIdx.x;
   const int dir = blockIdx.y;
   if (id >= gx * (gz - 1)) return;
+  T* r = reinterpret_cast<T*>(smraw) + threadIdx.x;
+  T* gs = r + (size_t)gy * W;
+  T* zs = gs + (size_t)gy * W;
   const int x = id % gx, z = 1 + id / gx;
   const double ds = film_ds(F.dss, dir, s, F.ns);
   const T* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;
@@ -239,12 +371,19 @@ k_adi_y(FilmDev<T> F, int s) {
   const size_t col = (size_t)z * L + x;
   for (int y = 0; y < gy; ++y) {
     const int ym = (y + gy - 1) % gy, yp = (y + 1) % gy;
-    const size_t i = col + (size_t)y * gx;
-    w1[i] = ay * p0[col + (size_t)ym * gx] + w1[i] + by * p0[i] + cy * p0[col + (size_t)yp * gx];
+    const size_t i = col + (size_t)y * gx, im = col + (size_t)ym * gx, ip = col + (size_t)yp * gx;
+    if constexpr (sizeof(T) == 4) {   // increment q** - q* from e = q - q*
+      const T e0 = p0[i] - w1[i];
+      r[y * W] = ay * ((p0[im] - w1[im]) - e0) + cy * ((p0[ip] - w1[ip]) - e0);
+    } else {
+      r[y * W] = ay * p0[im] + w1[i] + by * p0[i] + cy * p0[ip];
+    }
   }
-  T* gbase = F.gam + (size_t)dir * 2 * (size_t)gy * (gx * (gz - 1));
-  cyclic_solve<T>(ay, (T)1 + by, cy, gy, w1 + col, gx, w1 + col, gx, gbase + id,
-                  gbase + (size_t)gy * (gx * (gz - 1)) + id, (size_t)(gx * (gz - 1)), F.err);
+  cyclic_solve<T>(ay, (T)1 + by, cy, gy, r, W, r, W, gs, zs, W, F.err);
+  for (int y = 0; y < gy; ++y) {
+    const size_t i = col + (size_t)y * gx;
+    w1[i] = sizeof(T) == 4 ? w1[i] + r[y * W] : r[y * W];
+  }
 }
 
 // z sweep: (1 - ds Dzz/2 + ds w/2) q' = q** - ds Dzz q / 2 + ds w q / 2
@@ -252,45 +391,52 @@ k_adi_y(FilmDev<T> F, int s) {
 template <typename T>
 __global__ void __launch_bounds__(FILM_THREADS)
 k_adi_z(FilmDev<T> F, FieldRef fr, int s) {
-  const int gz = F.gz, L = F.nlines;
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int gz = F.gz, L = F.nlines, W = blockDim.x;
+  const int line = blockIdx.x * W + threadIdx.x;
   const int dir = blockIdx.y;
   if (line >= L) return;
-  const double ds = film_ds(F.dss, dir, s, F.ns);
+  T* us = reinterpret_cast<T*>(smraw) + threadIdx.x;
+  T* gs = us + (size_t)(gz + 1) * W;
+  const CnStep st = cn_step(film_ds(F.dss, dir, s, F.ns));
   const int ty = (F.brush || F.single) ? 0 : film_type(dir, s, F.ns, F.na);
-  const double* w = fr.get() + (size_t)ty * F.npts;
+  const double* w = sizeof(T) == 4 ? nullptr : fr.get() + (size_t)ty * F.npts;
+  const float* wl = sizeof(T) == 4 ? F.wf + (size_t)ty * F.npts : nullptr;
   const T* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;
   const T* w1 = F.w1 + (size_t)dir * F.npts;
   T* qn = (dir == 0 ? F.q : F.qd) + (size_t)s * F.npts;
-  T* gam = F.gam + (size_t)dir * (gz + 1) * L;
+  // FP32: increment q' - q** from f = q - q** (q** = 0 on the walls)
+  constexpr bool inc = sizeof(T) == 4;
   T bet = (T)1, uprev = (T)0, cprev = (T)0;
-  qn[line] = (T)0;
+  T f_jm1 = p0[line], f_j = inc && gz > 1 ? p0[(size_t)L + line] - w1[(size_t)L + line] : (T)0;
+  us[0] = (T)0;
   for (int j = 1; j <= gz; ++j) {
     T a, c, diag, rhs;
     const size_t i = (size_t)j * L + line;
     if (j < gz) {
-      a = (T)(-ds * F.alpha[j]);
-      c = (T)(-ds * F.gamma[j]);
-      const T bz = (T)(ds * F.beta[j]);
-      const T hw = (T)(0.5 * ds * w[i]);
+      T bz, hw;
+      cn_row<T>(F, st, j, sizeof(T) == 4 ? 0.0 : w[i], sizeof(T) == 4 ? wl[i] : 0.f, a, c, bz, hw);
       diag = (T)1 + bz + hw;
-      rhs = a * p0[i - L] + w1[i] + (bz + hw) * p0[i] + c * p0[i + L];
+      if constexpr (inc) {
+        const T f_jp1 = j + 1 < gz ? p0[i + L] - w1[i + L] : p0[i + L];
+        rhs = a * (f_jm1 - f_j) + c * (f_jp1 - f_j) + hw * f_j;
+        f_jm1 = f_j;
+        f_j = f_jp1;
+      } else {
+        rhs = a * p0[i - L] + w1[i] + (bz + hw) * p0[i] + c * p0[i + L];
+      }
     } else {
       a = (T)0; c = (T)0; diag = (T)1; rhs = (T)0;
     }
-    const T g = cprev / bet;
-    bet = diag - a * g;
-    if (bet == (T)0) atomicOr(F.err, 1);
-    uprev = (rhs - a * uprev) / bet;
-    gam[i] = g;
-    qn[i] = uprev;
-    cprev = c;
+    gs[j * W] = thomas_row<T>(bet, cprev, uprev, a, c, diag, rhs, F.err);
+    us[j * W] = uprev;
   }
   T unext = uprev;
+  qn[(size_t)gz * L + line] = unext;
   for (int j = gz - 1; j >= 0; --j) {
     const size_t i = (size_t)j * L + line;
-    const T u = qn[i] - gam[i + L] * unext;
-    qn[i] = u;
+    const T u = us[j * W] - gs[(j + 1) * W] * unext;
+    qn[i] = inc && j > 0 ? w1[i] + u : u;
     unext = u;
   }
 }
@@ -360,20 +506,28 @@ k_film1d_chains_b(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__ 
 }
 
 // One-line films of a batch with the line held in shared memory.  One thread
-// per (film, chain), blockIdx.y = chain; blockDim.x = W lanes.  The Thomas
-// sweep of film1d_chain runs on the same arithmetic in the same order, but q
-// is updated in place in shared memory (u_j replaces q_j once q_j and
-// q_{j+1} have been read) with the elimination factors beside it, both
-// interleaved [j][lane] so that a warp's accesses fall in distinct banks.
+// per (film, chain), blockIdx.y = chain; W = per_warp lanes in each warp of
+// the block.  The Thomas
+// sweep of film1d_chain runs on the same arithmetic in the same order, on
+// q, the elimination factors and the eliminated right-hand side in shared
+// memory, interleaved [j][lane] so that a warp's accesses fall in distinct
+// banks; the back substitution writes the new q over the old one.
 // Only the finished slice goes to global memory (for the contour integral);
-// the sweep itself never waits on a global load of its own stores.
-// Shared memory: 2 zcap W elements, zcap >= gz + 1 of every listed film.
+// the sweep itself never waits on a global load of its own stores.  FP32
+// sweeps also keep the film's field in FP32 there.
+// Shared memory: 3 zcap W elements of T (q, gam, the eliminated right-hand
+// side) + 2 zcap W floats for FP32 sweeps, zcap >= gz + 1 of every film.
 template <typename T>
-__global__ void __launch_bounds__(32)
+__global__ void __launch_bounds__(256)
 k_film1d_chains_sm(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__ Ss,
-                   const int* __restrict__ films, int nf, int zcap) {
+                   const int* __restrict__ films, int nf, int zcap, int per_warp) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int W = blockDim.x, lane = threadIdx.x;
+  constexpr bool inc = sizeof(T) == 4;
+  // the first per_warp lanes of each warp work (a warp's instruction stream
+  // is serial, so few lanes per warp means more streams per SM)
+  if ((threadIdx.x & 31) >= per_warp) return;
+  const int W = (blockDim.x >> 5) * per_warp;
+  const int lane = (threadIdx.x >> 5) * per_warp + (threadIdx.x & 31);
   const int k = blockIdx.x * W + lane;
   if (k >= nf) return;
   const int f = films[k];
@@ -381,6 +535,8 @@ k_film1d_chains_sm(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__
   const double* field = Ss[f].hx + (size_t)((*Ss[f].iter) % Ss[f].slots) * ((size_t)Ss[f].ntypes * Ss[f].npts);
   T* qv = reinterpret_cast<T*>(smraw) + lane;
   T* gv = qv + (size_t)zcap * W;
+  T* dv = gv + (size_t)zcap * W;
+  float* wv = reinterpret_cast<float*>(reinterpret_cast<T*>(smraw) + 3 * (size_t)zcap * W) + lane;
   const int dir = blockIdx.y, gz = F.gz;
   T* chain = dir == 0 ? F.q : F.qd;
   for (int j = 0; j <= gz; ++j) {
@@ -388,46 +544,45 @@ k_film1d_chains_sm(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__
     qv[j * W] = v;
     chain[j] = v;
   }
+  if constexpr (sizeof(T) == 4) {   // the field in FP32, once per propagation
+    for (int ty = 0; ty < F.ntypes; ++ty)
+      for (int j = 0; j <= gz; ++j) wv[((size_t)ty * zcap + j) * W] = (float)field[(size_t)ty * F.npts + j];
+  }
   for (int s = 1; s <= F.ns; ++s) {
-    const double ds = film_ds(F.dss, dir, s, F.ns);
+    const CnStep st = cn_step(film_ds(F.dss, dir, s, F.ns));
     const int ty = F.brush ? 0 : film_type(dir, s, F.ns, F.na);
     const double* w = field + (size_t)ty * F.npts;
+    const float* wl = wv + (size_t)ty * zcap * W;
     T* qn = chain + (size_t)s * F.npts;
-    T bet = (T)1, uprev = (T)0, cprev = (T)0;
+    T bet = (T)1, cprev = (T)0;
     T q_jm1 = qv[0], q_j = qv[W];
-    qv[0] = (T)0;
+    T uprev = inc ? -q_jm1 : (T)0;
+    dv[0] = uprev;
 #pragma unroll 4
     for (int j = 1; j < gz; ++j) {
       const T q_jp1 = qv[(j + 1) * W];
-      const T a = (T)(-ds * F.alpha[j]);
-      const T c = (T)(-ds * F.gamma[j]);
-      const T b = (T)(ds * F.beta[j]);
-      const T hw = (T)(0.5 * ds * w[j]);
-      const T diag = (T)1 + b + hw;
-      const T rhs = -a * q_jm1 + ((T)1 - b - hw) * q_j - c * q_jp1;
+      T a, c, b, hw;
+      cn_row<T>(F, st, j, sizeof(T) == 4 ? 0.0 : w[j], sizeof(T) == 4 ? wl[j * W] : 0.f, a, c, b, hw);
+      const T diag = r_add(r_add((T)1, b), hw);
+      const T rhs = cn_rhs<T>(a, b, c, hw, q_jm1, q_j, q_jp1);
       q_jm1 = q_j;
       q_j = q_jp1;
-      const T g = cprev / bet;
-      bet = diag - a * g;
-      if (bet == (T)0) atomicOr(F.err, 1);
-      uprev = (rhs - a * uprev) / bet;
-      gv[j * W] = g;
-      qv[j * W] = uprev;
-      cprev = c;
+      gv[j * W] = thomas_row<T>(bet, cprev, uprev, a, c, diag, rhs, F.err);
+      dv[j * W] = uprev;
     }
-    {  // row gz: identity, zero right-hand side
-      const T g = cprev / bet;
-      bet = (T)1;
-      uprev = ((T)0 - (T)0 * uprev) / bet;
-      gv[gz * W] = g;
-    }
+    // row gz: identity (zero right-hand side; increment: -q_gz)
+    gv[gz * W] = thomas_row<T>(bet, cprev, uprev, (T)0, (T)0, (T)1, inc ? -q_j : (T)0, F.err);
     T unext = uprev;
-    qv[gz * W] = unext;
-    qn[gz] = unext;
+    {
+      const T v = inc ? r_add(q_j, unext) : unext;
+      qv[gz * W] = v;
+      qn[gz] = v;
+    }
     for (int j = gz - 1; j >= 0; --j) {
-      const T u = qv[j * W] - gv[(j + 1) * W] * unext;
-      qv[j * W] = u;
-      qn[j] = u;
+      const T u = r_fma(-gv[(j + 1) * W], unext, dv[j * W]);
+      const T v = inc ? r_add(qv[j * W], u) : u;
+      qv[j * W] = v;
+      qn[j] = v;
       unext = u;
     }
   }

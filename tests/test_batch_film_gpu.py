@@ -54,10 +54,11 @@ def test_film_batch_follows_single_contexts(rng, prec, mixing):
             for i, c in enumerate(singles):
                 rs = c.scf_run(1)
                 assert rb[i].iter == rs.iter
-                # same line code, inlined into different kernels (FMA
-                # contraction may differ): agreement to rounding.  Anderson
-                # amplifies it on the graded film, which these settings drive
-                # away from the saddle (accuracy ~1e3 by iteration 7)
+                # the line sweeps round every operation explicitly, so the
+                # batched and single kernels agree to the contour and
+                # reduction order; Anderson amplifies that on the graded film,
+                # which these settings drive away from the saddle (accuracy
+                # ~1e3 by iteration 7)
                 rtol = 1e-10 if mixing == MIX_LAMBDA else 1e-6
                 assert abs(rb[i].free_energy - rs.free_energy) <= rtol * max(1.0, abs(rs.free_energy)), (it, i)
                 assert abs(rb[i].accuracy - rs.accuracy) <= 10 * rtol * rs.accuracy + 1e-30, (it, i)
