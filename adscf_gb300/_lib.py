@@ -55,6 +55,9 @@ class Params(C.Structure):
         ("ext_potential", _dp),
         ("ww", C.c_double),
         ("graft", _dp),
+        ("nblocks", C.c_int),
+        ("blocks", _dp),
+        ("block_types", C.POINTER(C.c_int)),
     ]
 
 

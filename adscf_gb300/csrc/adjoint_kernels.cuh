@@ -168,8 +168,9 @@ __device__ __forceinline__ void adj_x_body(const AdjDev& A, int tile, const doub
   const bool fA1 = chain_type_fwd(I, t + 1) == 0, bA1 = chain_type_bwd(I, t + 1) == 0;
   const int u = I.ns - t;
   const double ds = A.ds;
-  const double cat = ds * (double)wA_of(t, I.na), cbt = ds * (double)wB_of(t, I.na, I.ns);
-  const double cau = ds * (double)wA_of(u, I.na), cbu = ds * (double)wB_of(u, I.na, I.ns);
+  const float2 wnt = node_weights(I, t), wnu = node_weights(I, u);
+  const double cat = ds * (double)wnt.x, cbt = ds * (double)wnt.y;
+  const double cau = ds * (double)wnu.x, cbu = ds * (double)wnu.y;
   const double aS = first ? A.sc[ADJ_AS] : 0.0;
   const double2* slu = A.slB + (size_t)(u - A.tB0) * np;
   for (int e = threadIdx.x; e < tot; e += blockDim.x) {
@@ -311,14 +312,15 @@ k_contour_segment(BulkDev<double> I, const double2* __restrict__ A, int a0, cons
                   int b0, int s_lo, int s_hi) {
   __shared__ double red[32];
   const size_t np = (size_t)I.npts;
-  const int N = I.ns, NA = I.na;
+  const int N = I.ns;
   double qs = 0.0;
   for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += (size_t)gridDim.x * blockDim.x) {
     double accA = 0.0, accB = 0.0;
     for (int s = s_lo; s <= s_hi; ++s) {
       const double pr = A[(size_t)(s - a0) * np + p].x * B[(size_t)(N - s - b0) * np + p].y;
-      accA += (double)wA_of(s, NA) * pr;
-      accB += (double)wB_of(s, NA, N) * pr;
+      const float2 wn = node_weights(I, s);
+      accA += (double)wn.x * pr;
+      accB += (double)wn.y * pr;
     }
     I.dist[p] += I.ds * accA;
     I.dist[np + p] += I.ds * accB;

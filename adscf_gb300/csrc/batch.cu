@@ -173,6 +173,7 @@ int build(adscf_batch* b) {
     BulkDev<T>& d = I[i];
     d.gx = q.gx; d.gy = q.gy; d.gz = q.gz;
     d.npts = q.gx * q.gy * q.gz;
+    if (q.nblocks) return berr(b, ADSCF_E_ARG, "instance " + std::to_string(i) + ": batches take diblock chains");
     const int sa = nint_b(q.block_length[0] / q.ds), sb = nint_b(q.block_length[1] / q.ds);
     d.ns = sa + sb; d.na = sa; d.nb = sb;
     d.ds = q.ds;

@@ -202,6 +202,28 @@ int create_t(adscf_ctx* ctx) {
   I.gx = ctx->gx; I.gy = ctx->gy; I.gz = ctx->gz;
   I.npts = ctx->npts;
   I.ns = ctx->ns; I.na = ctx->na; I.nb = ctx->nb;
+  I.nblk = ctx->nblk;
+  for (int k = 0; k < ADSCF_MAX_BLOCKS; ++k) I.bend[k] = ctx->bend[k];
+  I.btype = ctx->btype;
+  I.wtab = nullptr;
+  if (ctx->nblk) {
+    // Propagate_Multiblock (mod_multiblock.f90:148-160): per block, 1/2 at
+    // its end nodes and 1 inside, summed by monomer type
+    std::vector<float2> wt(ctx->ns + 1, make_float2(0.f, 0.f));
+    int s0 = 0;
+    for (int k = 0; k < ctx->nblk; ++k) {
+      const int s1 = ctx->bend[k];
+      float* acc = (ctx->btype >> k) & 1u ? &wt[0].y : &wt[0].x;
+      for (int s = s0; s <= s1; ++s) {
+        const float w = (s == s0 ? 0.5f : 0.f) + (s == s1 ? 0.5f : 0.f) + ((s > s0 && s < s1) ? 1.f : 0.f);
+        acc[2 * s] += w;
+      }
+      s0 = s1;
+    }
+    CK(cudaMalloc(&ctx->d_wtab, wt.size() * sizeof(float2)));
+    CK(cudaMemcpy(ctx->d_wtab, wt.data(), wt.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    I.wtab = ctx->d_wtab;
+  }
   I.ds = ctx->p.ds;
   if (!make_plan(ctx->gx, I.px) || !make_plan(ctx->gy, I.py) || !make_plan(ctx->gz, I.pz))
     return set_err(ctx, ADSCF_E_ARG, "grid sizes must be products of 2, 3 and 5");
@@ -684,6 +706,7 @@ void bulk_destroy(adscf_ctx* ctx) {
   } else {
     cudaFree(ctx->hb64.spec); cudaFree(ctx->hb64.slices); cudaFree(ctx->hb64.E);
   }
+  cudaFree(ctx->d_wtab);
   cudaFree(ctx->d_inst); cudaFree(ctx->d_tw); cudaFree(ctx->d_fk);
   cudaFree(ctx->d_tw64); cudaFree(ctx->d_g64); cudaFree(ctx->d_flags);
   cudaFree(ctx->d_work_x); cudaFree(ctx->d_work_y); cudaFree(ctx->d_work_z);

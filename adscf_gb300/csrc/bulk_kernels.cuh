@@ -21,6 +21,7 @@
 // so the real-space Boltzmann factors, the slice store and the k-space
 // factor never take an extra pass over memory.
 #pragma once
+#include "adscf.h"
 #include "fft.cuh"
 
 #define BULK_THREADS 256
@@ -30,6 +31,13 @@ struct BulkDev {
   int gx, gy, gz;
   int npts;
   int ns, na, nb;            // contour steps, A-block steps (fwd), B-block steps (bwd)
+  // linear block sequence (nblk > 0; 0 = the diblock of na / nb): block k
+  // ends at contour node bend[k] and has monomer type bit k of btype; node
+  // weights per type in wtab [ns+1] (trapezoid per block, summed by type)
+  int nblk;
+  int bend[ADSCF_MAX_BLOCKS];
+  unsigned btype;
+  const float2* wtab;
   Plan1D px, py, pz;
   // exp(-ds k^2) tables in `fk`: g_xy[gy*gx] (hi then lo), g_z[gz]/N (hi then
   // lo); lo parts are the FP32 rounding residues (zero in FP64)
@@ -80,9 +88,21 @@ __device__ __forceinline__ void store_ept(float* E, size_t p, int c, double e) {
 __device__ __forceinline__ void store_ept(double* E, size_t p, int c, double e) { E[2 * p + c] = e; }
 
 template <typename T>
-__device__ __forceinline__ int chain_type_fwd(const BulkDev<T>& I, int t) { return t <= I.na ? 0 : 1; }
+__device__ __forceinline__ int seq_type(const BulkDev<T>& I, int t) {
+  int k = 0;
+  while (k < I.nblk - 1 && t > I.bend[k]) ++k;
+  return (int)((I.btype >> k) & 1u);
+}
+// monomer type (0 A, 1 B) of step t (node t-1 -> t) of the forward chain,
+// and of step t of the backward chain (forward step Ns + 1 - t)
 template <typename T>
-__device__ __forceinline__ int chain_type_bwd(const BulkDev<T>& I, int t) { return t <= I.nb ? 1 : 0; }
+__device__ __forceinline__ int chain_type_fwd(const BulkDev<T>& I, int t) {
+  return I.nblk ? seq_type(I, t) : (t <= I.na ? 0 : 1);
+}
+template <typename T>
+__device__ __forceinline__ int chain_type_bwd(const BulkDev<T>& I, int t) {
+  return I.nblk ? seq_type(I, I.ns + 1 - t) : (t <= I.nb ? 1 : 0);
+}
 
 // ---------------------------------------------------------------------------
 // The (kx, ky) = (0, 0) z pencil carries the mean of both propagators; FP32
@@ -386,6 +406,12 @@ __device__ __forceinline__ float wA_of(int s, int na) {
 __device__ __forceinline__ float wB_of(int s, int na, int n) {
   return (s == na ? 0.5f : 0.f) + (s == n ? 0.5f : 0.f) + ((s > na && s < n) ? 1.f : 0.f);
 }
+// contour weights of node s for types A and B
+template <typename T>
+__device__ __forceinline__ float2 node_weights(const BulkDev<T>& I, int s) {
+  if (I.nblk) return I.wtab[s];
+  return make_float2(wA_of(s, I.na), wB_of(s, I.na, I.ns));
+}
 
 struct FF {  // compensated float accumulator
   float hi, lo;
@@ -407,7 +433,7 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
   __shared__ double red[32];
   const BulkDev<T> I = insts[blockIdx.y];
   const double ds = I.ds;
-  const int N = I.ns, NA = I.na;
+  const int N = I.ns;
   const cplx<T>* sl = I.slices;
   const size_t np = I.npts;
   double qsum = 0.0;
@@ -422,14 +448,14 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
         if (s == 0) qsum += (double)b.x;
         // node s: q_s * qdag_{N-s}
         const float x1 = (float)a.x, y1 = (float)b.y;
-        float wa = wA_of(s, NA), wb = wB_of(s, NA, N);
-        if (wa != 0.f) ff_add_prod(fa, x1, y1, wa);
-        if (wb != 0.f) ff_add_prod(fb, x1, y1, wb);
+        float2 wn = node_weights(I, s);
+        if (wn.x != 0.f) ff_add_prod(fa, x1, y1, wn.x);
+        if (wn.y != 0.f) ff_add_prod(fb, x1, y1, wn.y);
         if (u != s) {  // node N-s: q_{N-s} * qdag_s
           const float x2 = (float)b.x, y2 = (float)a.y;
-          wa = wA_of(u, NA); wb = wB_of(u, NA, N);
-          if (wa != 0.f) ff_add_prod(fa, x2, y2, wa);
-          if (wb != 0.f) ff_add_prod(fb, x2, y2, wb);
+          wn = node_weights(I, u);
+          if (wn.x != 0.f) ff_add_prod(fa, x2, y2, wn.x);
+          if (wn.y != 0.f) ff_add_prod(fb, x2, y2, wn.y);
         }
       }
       accA += (double)fa.hi + (double)fa.lo;
@@ -441,12 +467,14 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
         const cplx<T> b = sl[(size_t)u * np + p];
         if (s == 0) qsum += (double)b.x;
         double pr = (double)a.x * (double)b.y;
-        accA += (double)wA_of(s, NA) * pr;
-        accB += (double)wB_of(s, NA, N) * pr;
+        float2 wn = node_weights(I, s);
+        accA += (double)wn.x * pr;
+        accB += (double)wn.y * pr;
         if (u != s) {
           pr = (double)b.x * (double)a.y;
-          accA += (double)wA_of(u, NA) * pr;
-          accB += (double)wB_of(u, NA, N) * pr;
+          wn = node_weights(I, u);
+          accA += (double)wn.x * pr;
+          accB += (double)wn.y * pr;
         }
       }
     }

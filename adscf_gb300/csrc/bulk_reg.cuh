@@ -67,7 +67,7 @@ k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
 
   if (mode == XM_INIT || mode == XM_R2S) {
     if (mode == XM_INIT) {
-      const bool fA = 1 <= I.na, bA = 1 > I.nb;
+      const bool fA = chain_type_fwd(I, 1) == 0, bA = chain_type_bwd(I, 1) == 0;
       cplx<T>* s0 = I.slices;
 #pragma unroll
       for (int m = 0; m < R1; ++m) {
@@ -113,9 +113,9 @@ k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
     return;
   }
   // A or B factor per chain and step (forward A then B, backward B then A)
-  const bool fA = t <= I.na, bA = t > I.nb;
+  const bool fA = chain_type_fwd(I, t) == 0, bA = chain_type_bwd(I, t) == 0;
   const bool more = t < ns;
-  const bool fA2 = (t + 1) <= I.na, bA2 = (t + 1) > I.nb;
+  const bool fA2 = chain_type_fwd(I, t + 1) == 0, bA2 = chain_type_bwd(I, t + 1) == 0;
   cplx<T>* sl = I.slices + (size_t)t * npts;
 #pragma unroll
   for (int m = 0; m < R1; ++m) {
@@ -368,9 +368,9 @@ k_rx_p(const BulkDev<T>* __restrict__ insts, int ntiles, const cplx<T>* __restri
   cplx<T>* sc = scr + line * F::LS;
   cplx<T>* spec = I.spec;
   // A or B factor per chain and step (forward A then B, backward B then A)
-  const bool fA = t <= I.na, bA = t > I.nb;
+  const bool fA = chain_type_fwd(I, t) == 0, bA = chain_type_bwd(I, t) == 0;
   const bool more = t < ns;
-  const bool fA2 = (t + 1) <= I.na, bA2 = (t + 1) > I.nb;
+  const bool fA2 = chain_type_fwd(I, t + 1) == 0, bA2 = chain_type_bwd(I, t + 1) == 0;
   cplx<T>* sl = I.slices + (size_t)t * npts;
   cplx<T> nx[R1];
   int tile = blockIdx.x;

@@ -316,8 +316,8 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   float2* sc = scr + line * F::LS;
   // Boltzmann factor choice: node t of each chain, then node t+1
   const int tt = init ? 1 : t;
-  const bool fA = tt <= I.na, bA = tt > I.nb;
-  const bool fA2 = (t + 1) <= I.na, bA2 = (t + 1) > I.nb;
+  const bool fA = chain_type_fwd(I, tt) == 0, bA = chain_type_bwd(I, tt) == 0;
+  const bool fA2 = chain_type_fwd(I, t + 1) == 0, bA2 = chain_type_bwd(I, t + 1) == 0;
   float2* sl = I.slices + (size_t)t * I.npts;
   int it = 0, issued = 0, done = 0;
   for (int z = blockIdx.x; z < gz; z += gridDim.x, ++it) {

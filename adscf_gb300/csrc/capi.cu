@@ -165,6 +165,17 @@ int validate(const adscf_params* p, std::string& why) {
   if (!(p->sizex > 0 && p->sizey > 0 && p->sizez > 0)) { why = "box size"; return ADSCF_E_ARG; }
   if (p->geometry != ADSCF_BULK && !p->dz) { why = "films need dz"; return ADSCF_E_ARG; }
   if (!p->dss && !(p->ds > 0)) { why = "ds"; return ADSCF_E_ARG; }
+  if (p->nblocks) {
+    if (p->geometry != ADSCF_BULK) { why = "block sequences are for bulk contexts"; return ADSCF_E_ARG; }
+    if (p->dss) { why = "block sequences take the uniform step ds"; return ADSCF_E_ARG; }
+    if (p->nblocks < 1 || p->nblocks > ADSCF_MAX_BLOCKS || !p->blocks || !p->block_types) {
+      why = "nblocks must be 1..16 with blocks and block_types"; return ADSCF_E_ARG;
+    }
+    for (int k = 0; k < p->nblocks; ++k)
+      if (!(p->blocks[k] >= 0) || (p->block_types[k] != 0 && p->block_types[k] != 1)) {
+        why = "block lengths >= 0, block types 0 (A) or 1 (B)"; return ADSCF_E_ARG;
+      }
+  }
   return ADSCF_OK;
 }
 
@@ -210,6 +221,13 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
   if (!ctx) return ADSCF_E_OOM;
   ctx->p = *p;
   ctx->p.dss = nullptr; ctx->p.dz = nullptr; ctx->p.ext_potential = nullptr; ctx->p.graft = nullptr;
+  ctx->p.blocks = nullptr; ctx->p.block_types = nullptr;
+  if (p->nblocks) {   // own copies, so that ctx->p can create sibling contexts
+    ctx->blk_len.assign(p->blocks, p->blocks + p->nblocks);
+    ctx->blk_type.assign(p->block_types, p->block_types + p->nblocks);
+    ctx->p.blocks = ctx->blk_len.data();
+    ctx->p.block_types = ctx->blk_type.data();
+  }
   ctx->geometry = p->geometry;
   ctx->prec = p->precision;
   // kernel-variant switches for A/B checks (results are identical in exact
@@ -226,7 +244,18 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
   ctx->npts = p->gx * p->gy * ctx->nplanes;
   ctx->ntypes = p->geometry == ADSCF_BRUSH ? 1 : 2;
   // contour discretisation (Initialize_Diblock, mod_diblock.f90:74-75)
-  if (p->dss) {
+  if (p->nblocks) {
+    // Initialize_Multiblock (mod_multiblock.f90:80-81): nint(length / ds) per block
+    ctx->nblk = p->nblocks;
+    int s0 = 0;
+    for (int k = 0; k < p->nblocks; ++k) {
+      s0 += nint(p->blocks[k] / p->ds);
+      ctx->bend[k] = s0;
+      if (p->block_types[k]) ctx->btype |= 1u << k;
+    }
+    ctx->ns = s0;
+    ctx->na = (ctx->btype & 1u) ? 0 : ctx->bend[0];   // first block's A steps (diagnostics)
+  } else if (p->dss) {
     ctx->ns = p->ns;
     ctx->na = p->geometry == ADSCF_BRUSH ? p->ns : p->n_a;
   } else {

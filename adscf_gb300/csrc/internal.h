@@ -24,6 +24,12 @@ struct adscf_ctx {
   int npts = 0;                 // points per species
   int ntypes = 2;
   int ns = 0, na = 0, nb = 0;   // contour steps
+  int nblk = 0;                 // bulk block sequence (0: the diblock of na / nb)
+  int bend[ADSCF_MAX_BLOCKS] = {};
+  unsigned btype = 0;
+  float2* d_wtab = nullptr;     // [ns+1] node weights (A, B) of a block sequence
+  std::vector<double> blk_len;  // the block sequence's lengths and types
+  std::vector<int> blk_type;
   double volume = 0, dvol = 0;
   cudaStream_t stream = nullptr;      // stream all work goes to
   cudaStream_t own_stream = nullptr;  // the context's own stream

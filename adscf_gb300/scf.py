@@ -36,8 +36,11 @@ def make_params(geometry=L.BULK, grid=(32, 32, 32), size=(4.0, 4.0, 4.0), ds=0.0
                 block_length=(0.5, 0.5), ensemble=1, rho=1.0, mu=0.0, kappa=25.0, chi=20.0,
                 monomer_volume=(1.0, 1.0), precision=L.FP64, mixing_type=L.MIX_LAMBDA,
                 mixing_dim=2, lam=0.1, lam_warm=1.0e-3, warm_iters=0, dss=None, n_a=0,
-                dz=None, int_scheme=1, int_span=0, ext_potential=None, ww=1.0, graft=None):
-    """adscf_params of one instance; returns (params, arrays it points into)."""
+                dz=None, int_scheme=1, int_span=0, ext_potential=None, ww=1.0, graft=None,
+                blocks=None, block_types=None):
+    """adscf_params of one instance; returns (params, arrays it points into).
+    ``blocks`` / ``block_types`` give a bulk linear block sequence (lengths and
+    monomer types 0 = A, 1 = B) in place of the diblock of ``block_length``."""
     keep = []
     p = L.Params()
     p.geometry = geometry
@@ -69,6 +72,15 @@ def make_params(geometry=L.BULK, grid=(32, 32, 32), size=(4.0, 4.0, 4.0), ds=0.0
     p.int_scheme = int_scheme
     p.int_span = int_span
     p.ww = ww
+    if blocks is not None:
+        bl = _f64(blocks)
+        bt = np.ascontiguousarray(block_types, dtype=np.int32)
+        if bt.size != bl.size:
+            raise ValueError("blocks and block_types differ in length")
+        keep += [bl, bt]
+        p.nblocks = bl.size
+        p.blocks = L.dptr(bl)
+        p.block_types = bt.ctypes.data_as(C.POINTER(C.c_int))
     return p, keep
 
 
@@ -81,7 +93,7 @@ class Context:
                  precision=L.FP64, mixing_type=L.MIX_LAMBDA, mixing_dim=2,
                  lam=0.1, lam_warm=1.0e-3, warm_iters=0, dss=None, n_a=0,
                  dz=None, int_scheme=1, int_span=0, ext_potential=None,
-                 ww=1.0, graft=None, lib=None):
+                 ww=1.0, graft=None, blocks=None, block_types=None, lib=None):
         self.lib = lib or L.load()
         p, self._keep = make_params(
             geometry=geometry, grid=grid, size=size, ds=ds, block_length=block_length,
@@ -89,7 +101,8 @@ class Context:
             monomer_volume=monomer_volume, precision=precision, mixing_type=mixing_type,
             mixing_dim=mixing_dim, lam=lam, lam_warm=lam_warm, warm_iters=warm_iters,
             dss=dss, n_a=n_a, dz=dz, int_scheme=int_scheme, int_span=int_span,
-            ext_potential=ext_potential, ww=ww, graft=graft)
+            ext_potential=ext_potential, ww=ww, graft=graft, blocks=blocks,
+            block_types=block_types)
         self.params = p
         h = C.c_void_p()
         rc = self.lib.adscf_ctx_create(C.byref(p), C.byref(h))

@@ -25,7 +25,8 @@
 extern "C" {
 #endif
 
-#define ADSCF_ABI_VERSION 1
+#define ADSCF_ABI_VERSION 2
+#define ADSCF_MAX_BLOCKS 16   /* blocks of a linear multiblock chain */
 
 #if defined(__GNUC__)
 #define ADSCF_API __attribute__((visibility("default")))
@@ -84,6 +85,15 @@ typedef struct adscf_params {
                                added inside Calculate_Mean_Ext_Fields; NULL=0 */
   double ww;                /* brush: w = ww*phi + U (mod_virial_expansion) */
   const double *graft;      /* brush: [gz+1] grafting distribution q-dag_0   */
+  /* bulk linear block sequence (Initialize_Multiblock / Propagate_Multiblock,
+     Polymer_Modules/mod_multiblock.f90:46-180; Propagate_Triblock and the
+     homopolymer are its 3- and 1-block cases): nblocks > 0 replaces the
+     diblock of block_length.  Block k has nint(blocks[k]/ds) segments of
+     monomer type block_types[k] (0 = A, 1 = B); densities are per type, the
+     sum of the block distributions of that type.  At most ADSCF_MAX_BLOCKS. */
+  int nblocks;
+  const double *blocks;
+  const int *block_types;
 } adscf_params;
 
 typedef struct adscf_ctx adscf_ctx;

@@ -140,6 +140,73 @@ def propagate_diblock(field, grid, size, ds, block_length, ensemble=1, rho=1.0,
     return out
 
 
+def propagate_multiblock(field, grid, size, ds, blocks, types, ensemble=1, rho=1.0, mu=0.0):
+    """Propagate_Multiblock, Bulk_3D_FFT/Polymer_Modules/mod_multiblock.f90:112-180
+    (Propagate_Triblock, mod_triblock.f90:103-170, is the same loop with three
+    blocks), followed by the driver's sum of block densities by monomer type
+    (Calculate_Densities, Main_Multiblock/main_multiblock.f90:531-536).
+
+    blocks: block lengths; types: monomer type per block (0 = A, 1 = B);
+    block segments nint(length / ds) (mod_multiblock.f90:80).  Returns a dict
+    with Qsum, distribution[block], density[block], density_type[type], mu,
+    rho and energy.
+    """
+    volume, dvol = volume_parameters(grid, size)
+    shape = field.shape[1:]
+    explaplace = calculate_laplace(grid, size, ds)
+    expfield = calculate_expfield(field, ds)
+    nseg = [int(np.floor(b / ds + 0.5)) for b in blocks]
+    segments = sum(nseg)
+    nb = len(blocks)
+    qq = np.empty((segments + 1,) + shape)
+    qqdag = np.empty((segments + 1,) + shape)
+    prop = np.ones(shape)                               # :127-137
+    qq[0] = prop
+    s0 = 0
+    for k in range(nb):
+        for s in range(s0 + 1, s0 + nseg[k] + 1):
+            prop = propagate_step(prop, expfield[types[k]], explaplace)
+            qq[s] = prop
+        s0 += nseg[k]
+    prop = np.ones(shape)                               # :139-149
+    qqdag[0] = prop
+    s0 = 0
+    for k in range(nb - 1, -1, -1):
+        for s in range(s0 + 1, s0 + nseg[k] + 1):
+            prop = propagate_step(prop, expfield[types[k]], explaplace)
+            qqdag[s] = prop
+        s0 += nseg[k]
+    mono = segments
+    qsum = dvol * qq[mono].sum()                        # :152
+    dist = np.zeros((nb,) + shape)
+    s0 = 0
+    for k in range(nb):                                 # :154-165
+        d = 0.5 * ds * qq[s0] * qqdag[mono - s0]
+        for s in range(s0 + 1, s0 + nseg[k]):
+            d = d + ds * qq[s] * qqdag[mono - s]
+        s0 += nseg[k]
+        dist[k] = d + 0.5 * ds * qq[s0] * qqdag[mono - s0]
+    out = dict(Qsum=qsum, distribution=dist, segments=segments, block_segments=nseg,
+               volume=volume, dvol=dvol)
+    if ensemble == 1:                                   # :170-173
+        out["density"] = rho * volume * dist / qsum
+        out["mu"] = np.log(rho * volume / qsum)
+        out["rho"] = rho
+        out["energy"] = rho * volume * (out["mu"] - 1.0)
+    elif ensemble == 2:                                 # :174-177
+        out["density"] = np.exp(mu) * dist
+        out["mu"] = mu
+        out["rho"] = out["density"].sum() * dvol / volume / (ds * segments)
+        out["energy"] = -out["rho"] * volume
+    else:
+        raise ValueError("Invalid ensemble")
+    dt = np.zeros((2,) + shape)
+    for k in range(nb):
+        dt[types[k]] += out["density"][k]
+    out["density_type"] = dt
+    return out
+
+
 def density_by_type(blk_density, monomer_type=(0, 1)):
     """Calculate_Densities, main_diblock.f90:277-283: block -> monomer type."""
     dens = np.zeros_like(blk_density)

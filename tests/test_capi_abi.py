@@ -50,7 +50,7 @@ def test_struct_layout_matches_c(tmp_path):
 
 
 def test_status_strings_without_gpu(lib):
-    assert lib.adscf_abi_version() == 1
+    assert lib.adscf_abi_version() == 2
     assert lib.adscf_status_string(3).decode() == "zero tridiagonal pivot"
 
 

@@ -84,3 +84,37 @@ def test_mean_field_helfand_model():
     dens = np.array([[0.6], [0.5]])
     w = oi.mean_fields(dens, kappa=10.0, chi=20.0)
     assert np.allclose(w[:, 0], [10 * 0.1 + 20 * 0.5, 10 * 0.1 + 20 * 0.6])
+
+
+def test_multiblock_two_blocks_is_the_diblock(rng):
+    grid, size, ds = (6, 4, 5), (3.0, 2.0, 2.5), 0.02
+    w = 0.5 * rng.standard_normal((2, 5, 4, 6))
+    d = ob.propagate_diblock(w, grid, size, ds, (0.3, 0.7))
+    m = ob.propagate_multiblock(w, grid, size, ds, (0.3, 0.7), (0, 1))
+    assert m["Qsum"] == d["Qsum"]
+    assert np.array_equal(m["density"], d["density"])
+    assert np.array_equal(m["density_type"], ob.density_by_type(d["density"]))
+
+
+def test_multiblock_constant_fields():
+    """Constant w_A, w_B: q_N = exp(-sum over blocks of w_type * length) and
+    each block's density is rho * (its length) (mod_multiblock.f90:170)."""
+    grid, size, ds = (4, 4, 4), (2.0, 2.0, 2.0), 0.01
+    w = np.stack([np.full((4, 4, 4), 0.3), np.full((4, 4, 4), -0.2)])
+    blocks, types = (0.5, 0.1, 0.1, 0.1, 0.1, 0.1), (0, 1, 0, 1, 0, 1)
+    r = ob.propagate_multiblock(w, grid, size, ds, blocks, types, rho=0.8)
+    assert np.isclose(r["Qsum"], 8.0 * np.exp(-(0.3 * 0.7 - 0.2 * 0.3)), rtol=1e-12)
+    for k, b in enumerate(blocks):
+        assert np.allclose(r["density"][k], 0.8 * b, rtol=1e-12)
+    assert np.allclose(r["density_type"][0], 0.8 * 0.7) and np.allclose(r["density_type"][1], 0.8 * 0.3)
+
+
+def test_multiblock_reversed_sequence_is_the_same_chain(rng):
+    """A linear chain read from its other end: same Q, block densities reversed."""
+    grid, size, ds = (6, 4, 4), (3.0, 2.0, 2.0), 0.02
+    w = 0.5 * rng.standard_normal((2, 4, 4, 6))
+    blocks, types = (0.2, 0.3, 0.1, 0.4), (0, 1, 1, 0)
+    a = ob.propagate_multiblock(w, grid, size, ds, blocks, types)
+    b = ob.propagate_multiblock(w, grid, size, ds, blocks[::-1], types[::-1])
+    assert np.isclose(a["Qsum"], b["Qsum"], rtol=1e-12)
+    assert np.allclose(a["density"], b["density"][::-1], rtol=1e-10, atol=1e-14)
