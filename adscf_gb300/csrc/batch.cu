@@ -81,6 +81,7 @@ struct adscf_batch {
   // lanes per block (0: the list sweeps on global memory)
   int zcap32 = 0, zcap64 = 0, lanes32 = 0, lanes64 = 0;
   int film_per_warp = 2, film_warps = 2;
+  int max_slots = 2;                    // longest mixing history of the instances
   float* d_tabf = nullptr;              // FP32 mesh factors of the FP32 sweeps
   int* d_err = nullptr;                 // zero-pivot flag of the sweeps
   // FP64 bulk batches: host copies of the instances and the adjoint state
@@ -189,6 +190,7 @@ int build(adscf_batch* b) {
     b->ns[i] = d.ns;
     b->npts[i] = d.npts;
     b->slots[i] = q.mixing_type == 3 ? q.mixing_dim + 1 : 2;
+    b->max_slots = std::max(b->max_slots, b->slots[i]);
     b->foff[i + 1] = b->foff[i] + 2 * (size_t)d.npts;
     b->maxns = std::max(b->maxns, d.ns);
   }
@@ -397,6 +399,7 @@ int build_film(adscf_batch* b) {
     na[i] = a;
     b->npts[i] = q.gz + 1;
     b->slots[i] = q.mixing_type == 3 ? q.mixing_dim + 1 : 2;
+    b->max_slots = std::max(b->max_slots, b->slots[i]);
     b->foff[i + 1] = b->foff[i] + (size_t)nt * b->npts[i];
     b->maxns = std::max(b->maxns, ns);
     t64[i] = film_sweep_fp64(b->prec, tb[i].max_ratio) ? 1 : 0;
@@ -606,7 +609,7 @@ int enqueue_film(adscf_batch* b) {
   }
   if (b->n32) k_film_contour_b<float><<<b->n32, 256, 0, s>>>(f32, b->d_list32);
   if (b->n64) k_film_contour_b<double><<<b->n64, 256, 0, s>>>(f64, b->d_list64);
-  k_closure_b<<<dim3(1, b->n), SCF_THREADS, 0, s>>>(b->d_S, CL_MEANFIELD | CL_MIXDOTS);
+  launch_closure_b(b->d_S, b->max_slots, CL_MEANFIELD | CL_MIXDOTS, dim3(1, b->n), s);
   k_solve_b<<<b->n, 64, 0, s>>>(b->d_S, 1, 1);
   k_mix_b<float><<<dim3(1, b->n), SCF_THREADS, 0, s>>>(b->d_S, 1);
   BK(cudaGetLastError());
@@ -669,7 +672,7 @@ int enqueue_iteration(adscf_batch* b) {
   int rc = enqueue_propagation<T>(b);
   if (rc) return rc;
   cudaStream_t s = b->stream;
-  k_closure_b<<<dim3(b->clos_grid, b->n), SCF_THREADS, 0, s>>>(b->d_S, CL_MEANFIELD | CL_MIXDOTS);
+  launch_closure_b(b->d_S, b->max_slots, CL_MEANFIELD | CL_MIXDOTS, dim3(b->clos_grid, b->n), s);
   k_solve_b<<<b->n, 64, 0, s>>>(b->d_S, 1, 1);
   k_mix_b<T><<<dim3(b->mix_grid, b->n), SCF_THREADS, 0, s>>>(b->d_S, b->mix_grid);
   BK(cudaGetLastError());

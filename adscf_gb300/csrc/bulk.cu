@@ -269,7 +269,13 @@ int create_t(adscf_ctx* ctx) {
   }
   I.spec = spec; I.slices = slices; I.E = E;
   I.dist = ctx->d_dist;
-  ctx->contour_blocks = (int)std::min<size_t>((np + BULK_THREADS - 1) / BULK_THREADS, 152 * 4);
+  {  // one resident wave of the contour kernel (a streaming grid-stride loop)
+    int per_sm = 0, nsm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bulk_contour<T>, BULK_THREADS, 0));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->dev));
+    ctx->contour_blocks = (int)std::min<size_t>((np + BULK_THREADS - 1) / BULK_THREADS,
+                                                (size_t)std::max(1, per_sm) * std::max(1, nsm));
+  }
   CK(cudaMalloc(&ctx->d_qpart, ctx->contour_blocks * sizeof(double)));
   I.qpart = ctx->d_qpart;
 

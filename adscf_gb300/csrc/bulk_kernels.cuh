@@ -441,6 +441,7 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
     double accA = 0.0, accB = 0.0;
     if constexpr (sizeof(T) == 4) {
       FF fa = {0.f, 0.f}, fb = {0.f, 0.f};
+#pragma unroll 4
       for (int s = 0; 2 * s <= N; ++s) {
         const int u = N - s;
         const cplx<T> a = sl[(size_t)s * np + p];
@@ -461,6 +462,7 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
       accA += (double)fa.hi + (double)fa.lo;
       accB += (double)fb.hi + (double)fb.lo;
     } else {
+#pragma unroll 4
       for (int s = 0; 2 * s <= N; ++s) {
         const int u = N - s;
         const cplx<T> a = sl[(size_t)s * np + p];

@@ -114,7 +114,7 @@ int enqueue_iteration(adscf_ctx* ctx) {
   // films read the field from the current history slot: the closure kernel
   // and the film sweep both locate it through the device counter
   if ((rc = enqueue_propagate(ctx, nullptr))) return rc;
-  k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, CL_MEANFIELD | CL_MIXDOTS);
+  launch_closure(ctx->S, CL_MEANFIELD | CL_MIXDOTS, ctx->closure_blocks, ctx->stream);
   k_solve<<<1, 64, 0, ctx->stream>>>(ctx->S, 1, 1);
   CK(cudaGetLastError());
   if (ctx->geometry == ADSCF_BULK) return bulk_mix_e(ctx);
@@ -284,6 +284,7 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
       cudaMalloc(&ctx->d_tmp, std::max<size_t>(2 * nv, 2 * (size_t)ctx->npts) * sizeof(double)) ||
       cudaMalloc(&ctx->d_hx, ctx->hist_slots * nv * sizeof(double)) ||
       cudaMalloc(&ctx->d_hr, ctx->hist_slots * nv * sizeof(double)) ||
+      (p->mixing_type == 3 && cudaMalloc(&ctx->d_hy, ctx->hist_slots * nv * sizeof(double))) ||
       cudaMalloc(&ctx->d_gram, SCF_MAX_SLOTS * SCF_MAX_SLOTS * sizeof(double)) ||
       cudaMalloc(&ctx->d_coef, 2 * SCF_MAX_SLOTS * sizeof(double)) ||
       cudaMalloc(&ctx->d_res, R_COUNT * sizeof(double)) ||
@@ -333,7 +334,7 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
   if (ctx->geometry == ADSCF_BULK) S.chain_len = p->ds * ctx->ns;
   S.dist = ctx->d_dist;
   S.dens = ctx->d_dens;
-  S.hx = ctx->d_hx; S.hr = ctx->d_hr;
+  S.hx = ctx->d_hx; S.hr = ctx->d_hr; S.hy = ctx->d_hy;
   S.slots = ctx->hist_slots;
   S.mixing_type = p->mixing_type;
   S.warm = p->warm_iters > p->mixing_dim ? p->warm_iters : p->mixing_dim;
@@ -363,7 +364,7 @@ int adscf_ctx_destroy(adscf_ctx* ctx) {
   if (ctx->geometry == ADSCF_BULK) bulk_destroy(ctx);
   else film_destroy(ctx);
   cudaFree(ctx->d_dist); cudaFree(ctx->d_dens); cudaFree(ctx->d_tmp);
-  cudaFree(ctx->d_hx); cudaFree(ctx->d_hr); cudaFree(ctx->d_gram);
+  cudaFree(ctx->d_hx); cudaFree(ctx->d_hr); cudaFree(ctx->d_hy); cudaFree(ctx->d_gram);
   cudaFree(ctx->d_coef); cudaFree(ctx->d_res); cudaFree(ctx->d_iter);
   cudaFree(ctx->d_part); cudaFree(ctx->d_wz); cudaFree(ctx->d_ext);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
@@ -388,7 +389,7 @@ int adscf_propagate_diblock_dev(adscf_ctx* ctx, const double* d_field, double* d
   }
   ScfDev S2 = ctx->S;
   S2.dens = d_density;
-  k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, 0);
+  launch_closure(S2, 0, ctx->closure_blocks, ctx->stream);
   k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
   CK(cudaGetLastError());
   return read_result(ctx, nullptr, out);
@@ -421,7 +422,7 @@ int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* den
   if ((rc = film_check_pivot(ctx))) return rc;
   ScfDev S2 = ctx->S;
   S2.dens = d_out;
-  k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, 0);
+  launch_closure(S2, 0, ctx->closure_blocks, ctx->stream);
   k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
   CK(cudaGetLastError());
   if ((rc = read_result(ctx, nullptr, out))) return rc;
@@ -490,7 +491,7 @@ int adscf_interaction_energy(adscf_ctx* ctx, const double* density, double* ener
   S2.slots = 1;
   S2.mixing_type = 1;
   // the closure reads *iter to locate slots; slot 0 of S2 is d_tmp+nv
-  k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, CL_MEANFIELD | CL_KEEP_OLD);
+  launch_closure(S2, CL_MEANFIELD | CL_KEEP_OLD, ctx->closure_blocks, ctx->stream);
   k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
   CK(cudaGetLastError());
   double r[R_COUNT];
@@ -727,7 +728,7 @@ int adscf_enqueue(adscf_ctx* ctx, int stage, int repeats) {
       if (ctx->geometry == ADSCF_BULK) rc = bulk_enqueue_contour(ctx);
       else rc = film_enqueue_contour(ctx);
     } else if (stage == ADSCF_STAGE_UPDATE) {
-      k_closure<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, CL_MEANFIELD | CL_MIXDOTS);
+      launch_closure(ctx->S, CL_MEANFIELD | CL_MIXDOTS, ctx->closure_blocks, ctx->stream);
       k_solve<<<1, 64, 0, ctx->stream>>>(ctx->S, 1, 1);
       CK(cudaGetLastError());
       rc = ctx->geometry == ADSCF_BULK ? bulk_mix_e(ctx)

@@ -646,7 +646,7 @@ static __global__ void __launch_bounds__(256) k_film_fe(ScfDev S, const double* 
 // out: [0] F, [1] dF/dchi (brush: dF/dww), [2 + c*nplanes + z] dF/dU_c(z)
 static __global__ void k_film_fe_sc(ScfDev S, const double* __restrict__ part, double* __restrict__ out) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const double Q = q_total(S);
+  const double Q = q_total_serial(S);
   double t[FE_N] = {0, 0, 0, 0, 0, 0, 0};
   for (int z = 0; z < S.nplanes; ++z)
     for (int k = 0; k < FE_N; ++k) t[k] += S.wz[z] * part[z * FE_N + k];

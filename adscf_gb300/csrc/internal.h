@@ -72,6 +72,7 @@ struct adscf_ctx {
   double* d_dens = nullptr;
   double* d_hx = nullptr;
   double* d_hr = nullptr;
+  double* d_hy = nullptr;       // Anderson: x_j + lambda r_j per slot
   double* d_qpart = nullptr;
   double* d_part = nullptr;
   double* d_gram = nullptr;

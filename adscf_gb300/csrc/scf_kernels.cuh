@@ -53,6 +53,7 @@ struct ScfDev {
   double* dens;              // [ntypes][npts] phi (old in, new out)
   double* hx;                // [slots][ntypes*npts] field history
   double* hr;                // [slots][ntypes*npts] residual history
+  double* hy;                // [slots][ntypes*npts] x_j + lambda r_j (Anderson), or null
   int slots;                 // m+1
   int mixing_type, warm;     // warm: Anderson for iter > warm
   double lambda, lam_warm;
@@ -67,10 +68,35 @@ struct ScfDev {
   double mixds;              //   and contour step
 };
 
+// Q = qscale * (sum of the contour kernel's per-block partials) in one fixed
+// order: lane-strided partial sums s_l (blocks b = l mod 32, increasing b),
+// then a butterfly over the 32 lanes.  Floating-point addition commutes
+// exactly, so every lane of the butterfly ends with the same bits, and
+// q_total_serial replays the same additions in one thread: every caller sees
+// the same Q.  All 32 lanes of a warp must call q_total.
+__device__ __forceinline__ double warp_sum_fixed(const double* v, int n, size_t stride) {
+  const int lane = threadIdx.x & 31;
+  double s = 0.0;
+  for (int b = lane; b < n; b += 32) s += v[(size_t)b * stride];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
 __device__ __forceinline__ double q_total(const ScfDev& S) {
-  double q = 0.0;
-  for (int b = 0; b < S.nqpart; ++b) q += S.qpart[b];
-  return q * S.qscale;
+  return warp_sum_fixed(S.qpart, S.nqpart, 1) * S.qscale;
+}
+__device__ __forceinline__ double q_total_serial(const ScfDev& S) {
+  double s[32];
+  for (int l = 0; l < 32; ++l) {
+    s[l] = 0.0;
+    for (int b = l; b < S.nqpart; b += 32) s[l] += S.qpart[b];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double t[32];
+    for (int l = 0; l < 32; ++l) t[l] = s[l] + s[l ^ o];
+    for (int l = 0; l < 32; ++l) s[l] = t[l];
+  }
+  return s[0] * S.qscale;
 }
 
 __device__ __forceinline__ double density_scale(const ScfDev& S, double Q) {
@@ -83,8 +109,9 @@ enum { CL_MEANFIELD = 1, CL_MIXDOTS = 2, CL_KEEP_OLD = 4 };
 // Non-template kernels are defined once, in scf.cu.  The `_b` forms run a
 // batch of independent instances: instance blockIdx.y (closure, mix) or
 // blockIdx.x (solve) of the ScfDev array, with per-instance partials.
-__global__ void k_closure(ScfDev S, int flags);
-__global__ void k_closure_b(const ScfDev* __restrict__ Ss, int flags);
+// closure launches (the kernels are specialised by history length)
+void launch_closure(const ScfDev& S, int flags, int grid, cudaStream_t st);
+void launch_closure_b(const ScfDev* Ss, int max_slots, int flags, dim3 grid, cudaStream_t st);
 __global__ void k_mixdots(ScfDev S);
 __global__ void k_solve(ScfDev S, int have_closure, int do_mix);
 __global__ void k_solve_b(const ScfDev* __restrict__ Ss, int have_closure, int do_mix);
@@ -94,8 +121,10 @@ __global__ void k_meanfield_only(ScfDev S, const double* __restrict__ dens, doub
 // Per point: phi_new = scale*dist; accuracy; mean field; residual into the
 // history slot of iteration k; energy and mixing partial sums.  Block `bid`
 // of `nb` blocks working on this instance.
+template <int NS>
 __device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid, int nb) {
-  __shared__ double red[NPART * 32];
+  constexpr int NA = NP_FIXED + NS;   // partial sums held per thread
+  __shared__ double red[NA * 32];
   const double Q = q_total(S);
   const double scale = density_scale(S, Q);
   const int k = *S.iter;
@@ -106,9 +135,9 @@ __device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid
   double* rk = S.hr + (size_t)cur * nv;
   const bool anderson = (flags & CL_MIXDOTS) && S.mixing_type == 3;
   const bool lam = (flags & CL_MIXDOTS) && S.mixing_type == 2 && k > 1;
-  double acc[NPART];
+  double acc[NA];
 #pragma unroll
-  for (int i = 0; i < NPART; ++i) acc[i] = 0.0;
+  for (int i = 0; i < NA; ++i) acc[i] = 0.0;
   for (int p = bid * blockDim.x + threadIdx.x; p < S.npts; p += nb * blockDim.x) {
     const int z = p / S.plane;
     const double wgt = S.wz ? S.wz[z] : S.dvol;
@@ -144,6 +173,7 @@ __device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid
       acc[P_PHIW] += wgt * phi[c] * x;
       const double r = interior ? wn[c] - x : 0.0;
       rk[i] = r;
+      if (anderson && S.hy) S.hy[(size_t)cur * nv + i] = x + S.lambda * r;
       if (!interior) continue;
       if (lam) {
         const double dx = x - S.hx[(size_t)prv * nv + i];
@@ -153,7 +183,7 @@ __device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid
       }
       if (anderson) {
 #pragma unroll
-        for (int j = 0; j < SCF_MAX_SLOTS; ++j) {
+        for (int j = 0; j < NS; ++j) {
           if (j < S.slots) {
             const double rj = (j == cur) ? r : S.hr[(size_t)j * nv + i];
             acc[NP_FIXED + j] += r * rj;
@@ -164,28 +194,44 @@ __device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-  for (int i = 0; i < NPART; ++i) {
+  for (int i = 0; i < NA; ++i) {
     double x = acc[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) red[i * 32 + warp] = x;
   }
   __syncthreads();
-  if (threadIdx.x < NPART) {
+  if (threadIdx.x < NPART) {   // entries past NA (slots this closure does not hold) are 0
     double r = 0.0;
-    for (int w = 0; w < nw; ++w) r += red[threadIdx.x * 32 + w];
+    if (threadIdx.x < NA)
+      for (int w = 0; w < nw; ++w) r += red[threadIdx.x * 32 + w];
     S.part[(size_t)bid * NPART + threadIdx.x] = r;
   }
 }
 
+// one kernel per slot capacity (3: lambda/simple or m <= 2, 11: m <= 10,
+// SCF_MAX_SLOTS), so the partial sums held per thread fit the history
+template <int NS>
 __global__ void __launch_bounds__(SCF_THREADS)
-k_closure(ScfDev S, int flags) { closure_body(S, flags, blockIdx.x, gridDim.x); }
+k_closure(ScfDev S, int flags) { closure_body<NS>(S, flags, blockIdx.x, gridDim.x); }
 
+template <int NS>
 __global__ void __launch_bounds__(SCF_THREADS)
 k_closure_b(const ScfDev* __restrict__ Ss, int flags) {
   const ScfDev S = Ss[blockIdx.y];
   if ((int)blockIdx.x >= S.npart_blocks) return;
-  closure_body(S, flags, blockIdx.x, S.npart_blocks);
+  closure_body<NS>(S, flags, blockIdx.x, S.npart_blocks);
+}
+
+void launch_closure(const ScfDev& S, int flags, int grid, cudaStream_t st) {
+  if (S.slots <= 3) k_closure<3><<<grid, SCF_THREADS, 0, st>>>(S, flags);
+  else if (S.slots <= 11) k_closure<11><<<grid, SCF_THREADS, 0, st>>>(S, flags);
+  else k_closure<SCF_MAX_SLOTS><<<grid, SCF_THREADS, 0, st>>>(S, flags);
+}
+void launch_closure_b(const ScfDev* Ss, int max_slots, int flags, dim3 grid, cudaStream_t st) {
+  if (max_slots <= 3) k_closure_b<3><<<grid, SCF_THREADS, 0, st>>>(Ss, flags);
+  else if (max_slots <= 11) k_closure_b<11><<<grid, SCF_THREADS, 0, st>>>(Ss, flags);
+  else k_closure_b<SCF_MAX_SLOTS><<<grid, SCF_THREADS, 0, st>>>(Ss, flags);
 }
 
 // Mixing dots only (for adscf_mix): x_k, r_k already in the history slot.
@@ -213,6 +259,7 @@ k_mixdots(ScfDev S) {
 #pragma unroll
       for (int j = 0; j < SCF_MAX_SLOTS; ++j)
         if (j < S.slots) acc[NP_FIXED + j] += r * S.hr[(size_t)j * nv + i];
+      if (S.hy) S.hy[(size_t)cur * nv + i] = S.hx[(size_t)cur * nv + i] + S.lambda * r;
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -295,10 +342,17 @@ __device__ void lu_solve_nr(double* a, double* b, int n) {
 // density/energy terms (k_closure) rather than only mixing dots.
 __device__ __forceinline__ void solve_body(const ScfDev& S, int have_closure, int do_mix) {
   __shared__ double tot[NPART];
-  if (threadIdx.x < NPART) {
-    double r = 0.0;
-    for (int b = 0; b < S.npart_blocks; ++b) r += S.part[(size_t)b * NPART + threadIdx.x];
-    tot[threadIdx.x] = r;
+  __shared__ double qsh;
+  {  // each entry summed by one warp in a fixed order (whatever the block size)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = warp; i < NPART; i += nw) {
+      const double r = warp_sum_fixed(S.part + i, S.npart_blocks, NPART);
+      if (lane == 0) tot[i] = r;
+    }
+    if (have_closure && warp == 0) {
+      const double q = q_total(S);
+      if (lane == 0) qsh = q;
+    }
   }
   __syncthreads();
   if (threadIdx.x != 0) return;
@@ -306,7 +360,7 @@ __device__ __forceinline__ void solve_body(const ScfDev& S, int have_closure, in
   const int cur = k % S.slots;
   double* res = S.res;
   if (have_closure) {
-    const double Q = q_total(S);
+    const double Q = qsh;
     double mu, rho, energy;
     if (S.ensemble == 1) {
       rho = S.rho;
@@ -402,7 +456,10 @@ __global__ void k_solve_b(const ScfDev* __restrict__ Ss, int have_closure, int d
 #endif  // ADSCF_SCF_IMPL
 
 // x_{k+1} = sum_j a_j x_j + b_j r_j into the next history slot; optional
-// E = exp(-ds x/2) for the pseudo-spectral propagator.
+// E = exp(-ds x/2) for the pseudo-spectral propagator.  After the Anderson
+// warm-up every b_j is lambda a_j, so with the history y_j = x_j + lambda r_j
+// (written by the closure) the step is sum_j a_j y_j: half the history reads
+// and FP64 multiply-adds.
 template <typename T>
 __device__ __forceinline__ void mix_body(const ScfDev& S, T* E, double ds, int bid, int nb) {
   __shared__ double ca[SCF_MAX_SLOTS], cb[SCF_MAX_SLOTS];
@@ -415,12 +472,17 @@ __device__ __forceinline__ void mix_body(const ScfDev& S, T* E, double ds, int b
   }
   __syncthreads();
   const size_t nv = (size_t)S.ntypes * S.npts;
+  const bool use_y = S.hy && S.mixing_type == 3 && kn - 1 > S.warm;
   for (size_t i = bid * (size_t)blockDim.x + threadIdx.x; i < nv; i += (size_t)nb * blockDim.x) {
     double x;
     const int z = (int)((i % S.npts) / S.plane);
     const bool interior = !S.wall_mask || (z > 0 && z < S.nplanes - 1);
     if (!interior) {
       x = S.hx[(size_t)cur * nv + i];
+    } else if (use_y) {
+      x = 0.0;
+      for (int j = 0; j < S.slots; ++j)
+        if (ca[j] != 0.0) x += ca[j] * S.hy[(size_t)j * nv + i];
     } else {
       x = 0.0;
       for (int j = 0; j < S.slots; ++j) {
