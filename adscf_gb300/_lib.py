@@ -110,6 +110,12 @@ SIGNATURES = {
     "adscf_forward_dev": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),
     "adscf_backward_surface": (C.c_int, [C.c_void_p, _dp, _dp]),
     "adscf_set_adjoint_checkpoint": (C.c_int, [C.c_void_p, C.c_int]),
+    "adscf_ddft_set_mobility": (C.c_int, [C.c_void_p, C.c_int, C.c_double, _dp, C.c_double]),
+    "adscf_ddft_rhs": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "adscf_conjugate_fields": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_int, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)]),
+    "adscf_ddft_step": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_int, C.c_double, C.c_int,
+                                  C.POINTER(C.c_int)]),
     "adscf_free_energy_fp64": (C.c_int, [C.c_void_p, C.POINTER(IterResult)]),
     "adscf_set_box": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double]),
     "adscf_batch_create": (C.c_int, [C.POINTER(Params), C.c_int, C.POINTER(C.c_void_p)]),

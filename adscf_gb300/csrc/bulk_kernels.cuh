@@ -53,7 +53,9 @@ struct BulkDev {
 
 // X-pass modes (XM_FROM: start a chain segment at node t from a stored
 // state (q_t, qdag_t) in aux.in, as XM_INIT does from (1, 1) at node 0)
-enum { XM_INIT = 0, XM_STEP = 1, XM_R2S = 2, XM_S2R = 3, XM_FROM = 4 };
+// (XM_C2S / XM_S2C: complex data in aux.in / aux.out, forward x FFT into
+// the spectrum / inverse x FFT out of it, nothing else)
+enum { XM_INIT = 0, XM_STEP = 1, XM_R2S = 2, XM_S2R = 3, XM_FROM = 4, XM_C2S = 5, XM_S2C = 6 };
 
 struct XAux {
   const void* in;   // XM_R2S: real input [npts] (T); XM_FROM: state [npts] (cplx<T>)
@@ -235,6 +237,15 @@ k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work
       I.spec[base + e] = r[(e / N) * P.ld + (e % N)];
     return;
   }
+  if (mode == XM_C2S) {
+    const cplx<T>* in = static_cast<const cplx<T>*>(aux.in);
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) b0[(e / N) * P.ld + (e % N)] = in[base + e];
+    __syncthreads();
+    cplx<T>* r = fft_lines<T>(b0, b1, tw, P, line, lt, active, +1);
+    for (int e = threadIdx.x; e < tot; e += blockDim.x)
+      I.spec[base + e] = r[(e / N) * P.ld + (e % N)];
+    return;
+  }
   if (mode == XM_R2S) {
     const T* in = static_cast<const T*>(aux.in);
     const T* ee = static_cast<const T*>(aux.e);
@@ -265,6 +276,11 @@ k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work
       if (ee) v *= ee[g];
       out[g] = v;
     }
+    return;
+  }
+  if (mode == XM_S2C) {
+    cplx<T>* out = static_cast<cplx<T>*>(aux.out);
+    for (int e = threadIdx.x; e < tot; e += blockDim.x) out[base + e] = r[(e / N) * P.ld + (e % N)];
     return;
   }
   // contour node t of both chains (A or B factor per chain and step)

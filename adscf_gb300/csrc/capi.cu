@@ -367,6 +367,7 @@ int adscf_ctx_destroy(adscf_ctx* ctx) {
   cudaFree(ctx->d_hx); cudaFree(ctx->d_hr); cudaFree(ctx->d_hy); cudaFree(ctx->d_gram);
   cudaFree(ctx->d_coef); cudaFree(ctx->d_res); cudaFree(ctx->d_iter);
   cudaFree(ctx->d_part); cudaFree(ctx->d_wz); cudaFree(ctx->d_ext);
+  cudaFree(ctx->d_mob); cudaFree(ctx->d_ddft);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;

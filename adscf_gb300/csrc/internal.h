@@ -28,6 +28,8 @@ struct adscf_ctx {
   int bend[ADSCF_MAX_BLOCKS] = {};
   unsigned btype = 0;
   float2* d_wtab = nullptr;     // [ns+1] node weights (A, B) of a block sequence
+  double* d_mob = nullptr;      // DDFT: [3][npts] mobility_qq (AA, AB, BB) per wave vector
+  double* d_ddft = nullptr;     // DDFT: density, its rate, mu [2][npts] each, complex staging
   std::vector<double> blk_len;  // the block sequence's lengths and types
   std::vector<int> blk_type;
   double volume = 0, dvol = 0;

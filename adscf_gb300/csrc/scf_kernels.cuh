@@ -51,6 +51,7 @@ struct ScfDev {
   double rho, mu, volume, chain_len;   // chain_len = ds * segments (GC rho)
   const double* dist;        // [ntypes][npts] contour integrals
   double* dens;              // [ntypes][npts] phi (old in, new out)
+  const double* target;      // [ntypes][npts] density of the conjugate-field solve (CL_CONJ)
   double* hx;                // [slots][ntypes*npts] field history
   double* hr;                // [slots][ntypes*npts] residual history
   double* hy;                // [slots][ntypes*npts] x_j + lambda r_j (Anderson), or null
@@ -104,7 +105,10 @@ __device__ __forceinline__ double density_scale(const ScfDev& S, double Q) {
 }
 
 // flags for k_closure
-enum { CL_MEANFIELD = 1, CL_MIXDOTS = 2, CL_KEEP_OLD = 4 };
+// CL_CONJ: the inverse problem of Get_Conjugate_Fields (main_multiblock.f90:
+// 566-640): residual phi[w] - target instead of the mean-field residual, and
+// the accuracy max |residual| (Check_Accuracy of that driver, :773-783)
+enum { CL_MEANFIELD = 1, CL_MIXDOTS = 2, CL_KEEP_OLD = 4, CL_CONJ = 8 };
 
 // Non-template kernels are defined once, in scf.cu.  The `_b` forms run a
 // batch of independent instances: instance blockIdx.y (closure, mix) or
@@ -146,11 +150,31 @@ __device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid
     for (int c = 0; c < S.ntypes; ++c) {
       phi[c] = scale * S.dist[(size_t)c * S.npts + p];
       const double old = S.dens[(size_t)c * S.npts + p];
-      acc[P_ACC] += (old - phi[c]) * (old - phi[c]);
+      if (!(flags & CL_CONJ)) acc[P_ACC] += (old - phi[c]) * (old - phi[c]);
       if (!(flags & CL_KEEP_OLD)) S.dens[(size_t)c * S.npts + p] = phi[c];
     }
     if (S.ntypes == 2) acc[P_RHO] += wgt * (phi[0] + phi[1]);
     else acc[P_RHO] += wgt * phi[0];
+    if (flags & CL_CONJ) {
+      for (int c = 0; c < S.ntypes; ++c) {
+        const size_t i = (size_t)c * S.npts + p;
+        const double x = xk[i];
+        const double r = phi[c] - S.target[i];
+        rk[i] = r;
+        acc[P_ACC] = fmax(acc[P_ACC], fabs(r));
+        if (anderson && S.hy) S.hy[(size_t)cur * nv + i] = x + S.lambda * r;
+        if (anderson) {
+#pragma unroll
+          for (int j = 0; j < NS; ++j) {
+            if (j < S.slots) {
+              const double rj = (j == cur) ? r : S.hr[(size_t)j * nv + i];
+              acc[NP_FIXED + j] += r * rj;
+            }
+          }
+        }
+      }
+      continue;
+    }
     if (!(flags & CL_MEANFIELD)) continue;
     if (S.homopolymer) {
       const double u = S.ext ? S.ext[z] : 0.0;
@@ -193,18 +217,23 @@ __device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const bool amax = flags & CL_CONJ;   // P_ACC holds a maximum
 #pragma unroll
   for (int i = 0; i < NA; ++i) {
     double x = acc[i];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = (amax && i == P_ACC) ? fmax(x, y) : x + y;
+    }
     if (lane == 0) red[i * 32 + warp] = x;
   }
   __syncthreads();
   if (threadIdx.x < NPART) {   // entries past NA (slots this closure does not hold) are 0
     double r = 0.0;
     if (threadIdx.x < NA)
-      for (int w = 0; w < nw; ++w) r += red[threadIdx.x * 32 + w];
+      for (int w = 0; w < nw; ++w)
+        r = (amax && threadIdx.x == P_ACC) ? fmax(r, red[threadIdx.x * 32 + w]) : r + red[threadIdx.x * 32 + w];
     S.part[(size_t)bid * NPART + threadIdx.x] = r;
   }
 }
@@ -346,7 +375,15 @@ __device__ __forceinline__ void solve_body(const ScfDev& S, int have_closure, in
   {  // each entry summed by one warp in a fixed order (whatever the block size)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int i = warp; i < NPART; i += nw) {
-      const double r = warp_sum_fixed(S.part + i, S.npart_blocks, NPART);
+      double r;
+      if (have_closure == 2 && i == P_ACC) {   // conjugate-field solve: max over blocks
+        r = 0.0;
+        for (int b = lane; b < S.npart_blocks; b += 32) r = fmax(r, S.part[(size_t)b * NPART + i]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
+      } else {
+        r = warp_sum_fixed(S.part + i, S.npart_blocks, NPART);
+      }
       if (lane == 0) tot[i] = r;
     }
     if (have_closure && warp == 0) {

@@ -10,6 +10,8 @@ real):
   records between groups) and Film_CK_AD/Film_1D/Main_Diblock_Melt/
   main_diblock_melt.f90:270-296 (``layout="film"``, adds int_scheme and
   mesh_type; the Film_3D deck has the same records).
+* ``read_mobilities`` -- Read_Mobilities of the multiblock DDFT driver
+  (Main_Multiblock/main_multiblock.f90:462-485).
 * ``read_input_interactions`` -- Initialize_Interactions, Bulk_3D_FFT/
   Interaction_Modules/mod_FloryHuggins.f90:40-62 (kappa, the upper triangle
   of chi, monomer volumes).
@@ -110,6 +112,25 @@ def read_input_interactions(path, components=2) -> dict:
     r.skip()
     vol = [r.value() for _ in range(components)]
     return {"kappa": kappa, "chi": chi, "monomer_volume": vol}
+
+
+def read_mobilities(path, small=1.0e-6):
+    """Read_Mobilities, Bulk_3D_FFT/Main_Multiblock/main_multiblock.f90:
+    462-485: nq, dq, three skipped records, then nq rows "q LAA LAB LBB" with
+    q = i dq (1-based i, checked to `small`).  Returns (dq, table [nq][3])
+    for Context.ddft_set_mobility."""
+    r = _Records(path)
+    nq = r.value(_int)
+    dq = r.value()
+    for _ in range(3):
+        r.skip()
+    table = np.zeros((nq, 3))
+    for i in range(nq):
+        q, aa, ab, bb = r.values(4)
+        if abs(q - (i + 1) * dq) >= small:
+            raise ValueError(f"q values in mobility are not consistent: {q} vs {(i + 1) * dq}")
+        table[i] = (aa, ab, bb)
+    return dq, table
 
 
 def context_kwargs(general: dict, interactions: dict, **overrides) -> dict:

@@ -257,6 +257,36 @@ class Context:
         self._ck(self.lib.adscf_free_energy_fp64(self.h, C.byref(res)))
         return res
 
+    # -- DDFT (bulk) ------------------------------------------------------
+    def ddft_set_mobility(self, table, dq, wcutoff):
+        """Mobilities from input_mobilities rows: table [nq][3] (AA, AB, BB)."""
+        t = _f64(table)
+        self._ck(self.lib.adscf_ddft_set_mobility(self.h, int(t.size // 3), float(dq), L.dptr(t),
+                                                  float(wcutoff)))
+
+    def ddft_rhs(self, mu):
+        """d rho / dt for mu [2][npts] (the k-space part of the DDFT step)."""
+        m = _f64(mu, 2 * self.npts)
+        out = np.empty(2 * self.npts)
+        self._ck(self.lib.adscf_ddft_rhs(self.h, L.dptr(m), L.dptr(out)))
+        return out.reshape(np.shape(mu))
+
+    def conjugate_fields(self, density, accuracy=1.0e-3, itermax=2000):
+        """Get_Conjugate_Fields from the current field: (status, iterations)."""
+        d = _f64(density, 2 * self.npts)
+        st, it = C.c_int(), C.c_int()
+        self._ck(self.lib.adscf_conjugate_fields(self.h, L.dptr(d), float(accuracy), int(itermax),
+                                                 C.byref(st), C.byref(it)))
+        return st.value, it.value
+
+    def ddft_step(self, density, timestep, floor_density=False, accuracy=1.0e-3, itermax=2000):
+        """One DDFT_Timestep_Euler: returns (new density, status)."""
+        d = _f64(density, 2 * self.npts).copy()
+        st = C.c_int()
+        self._ck(self.lib.adscf_ddft_step(self.h, L.dptr(d), float(timestep), int(bool(floor_density)),
+                                          float(accuracy), int(itermax), C.byref(st)))
+        return d.reshape(np.shape(density)), st.value
+
     def set_adjoint_checkpoint(self, every):
         """Checkpoint interval of forward/backward (0 off, < 0 ceil(sqrt(Ns)))."""
         self._ck(self.lib.adscf_set_adjoint_checkpoint(self.h, int(every)))

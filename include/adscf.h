@@ -271,6 +271,36 @@ ADSCF_API int adscf_backward(adscf_ctx *ctx, double *grad);
  * paired with a later backward.  Results equal the stored-slice pass up to
  * the summation order of the contour integral.                            */
 ADSCF_API int adscf_set_adjoint_checkpoint(adscf_ctx *ctx, int every);
+/* ---- dynamic density functional theory (bulk, two monomer types) -----
+ * The DDFT step of the multiblock driver (Bulk_3D_FFT/Main_Multiblock/
+ * main_multiblock.f90).
+ * adscf_ddft_set_mobility: Read_Mobilities (:441-506) from the rows of
+ *   input_mobilities: table[nq][3] = (Lambda_AA, Lambda_AB, Lambda_BB) at
+ *   q = (i+1) dq; mobility_qq(k) = min(|k|^2 Lambda(|k|), wcutoff) with the
+ *   reference's interpolation between rows.
+ * adscf_ddft_rhs: d rho / dt = -IFFT(mobility_qq FFT(mu)) for a host
+ *   mu[2][npts] (:836-861), into ddensity[2][npts].
+ * adscf_conjugate_fields: Get_Conjugate_Fields (:566-640) -- the context's
+ *   mixing iterates its current field until max |phi[w] - density| <=
+ *   accuracy / 2 (warm-up restarted on every call, as the reference's
+ *   iter_status); *status = 0 converged, 1 within accuracy but not half of
+ *   it, 2 not found (ADSCF_E_NONFINITE when the accuracy is >= 0.1 or not
+ *   finite, where the reference stops).  adscf_get_field then returns the
+ *   conjugate field.  The reference uses Anderson mixing with lambda 0.5,
+ *   accuracy 1e-3 and 2000 iterations.
+ * adscf_ddft_step: DDFT_Timestep_Euler (:794-880) on density[2][npts]
+ *   (in/out): conjugate fields, mu = mean fields of the density minus the
+ *   conjugate field, the Euler step with timestep, the floor at 1e-4 when
+ *   floor_density, and the conjugate fields of the new density (*status as
+ *   above; with floor_density and status >= 1 the density becomes that of
+ *   the field found).  No counterpart of these four entry points is a
+ *   separate reference procedure except as cited.                         */
+ADSCF_API int adscf_ddft_set_mobility(adscf_ctx *ctx, int nq, double dq, const double *table, double wcutoff);
+ADSCF_API int adscf_ddft_rhs(adscf_ctx *ctx, const double *mu, double *ddensity);
+ADSCF_API int adscf_conjugate_fields(adscf_ctx *ctx, const double *density, double accuracy, int itermax,
+                                     int *status, int *iterations);
+ADSCF_API int adscf_ddft_step(adscf_ctx *ctx, double *density, double timestep, int floor_density,
+                              double accuracy, int itermax, int *status);
 /* Films and brushes (any precision): adscf_forward gives the free energy
  * per chain at the host fields (the film Calculate_Energy with the external
  * term); adscf_backward_surface then gives dF/dchi (brush: dF/dww) and the
