@@ -610,7 +610,7 @@ int enqueue_film(adscf_batch* b) {
   if (b->n32) k_film_contour_b<float><<<b->n32, 256, 0, s>>>(f32, b->d_list32);
   if (b->n64) k_film_contour_b<double><<<b->n64, 256, 0, s>>>(f64, b->d_list64);
   launch_closure_b(b->d_S, b->max_slots, CL_MEANFIELD | CL_MIXDOTS, dim3(1, b->n), s);
-  k_solve_b<<<b->n, 64, 0, s>>>(b->d_S, 1, 1);
+  k_solve_b<<<b->n, SOLVE_THREADS, 0, s>>>(b->d_S, 1, 1);
   k_mix_b<float><<<dim3(1, b->n), SCF_THREADS, 0, s>>>(b->d_S, 1);
   BK(cudaGetLastError());
   return ADSCF_OK;
@@ -673,7 +673,7 @@ int enqueue_iteration(adscf_batch* b) {
   if (rc) return rc;
   cudaStream_t s = b->stream;
   launch_closure_b(b->d_S, b->max_slots, CL_MEANFIELD | CL_MIXDOTS, dim3(b->clos_grid, b->n), s);
-  k_solve_b<<<b->n, 64, 0, s>>>(b->d_S, 1, 1);
+  k_solve_b<<<b->n, SOLVE_THREADS, 0, s>>>(b->d_S, 1, 1);
   k_mix_b<T><<<dim3(b->mix_grid, b->n), SCF_THREADS, 0, s>>>(b->d_S, b->mix_grid);
   BK(cudaGetLastError());
   return ADSCF_OK;

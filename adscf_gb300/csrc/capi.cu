@@ -115,7 +115,7 @@ int enqueue_iteration(adscf_ctx* ctx) {
   // and the film sweep both locate it through the device counter
   if ((rc = enqueue_propagate(ctx, nullptr))) return rc;
   launch_closure(ctx->S, CL_MEANFIELD | CL_MIXDOTS, ctx->closure_blocks, ctx->stream);
-  k_solve<<<1, 64, 0, ctx->stream>>>(ctx->S, 1, 1);
+  k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(ctx->S, 1, 1);
   CK(cudaGetLastError());
   if (ctx->geometry == ADSCF_BULK) return bulk_mix_e(ctx);
   k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, nullptr, 0.0);
@@ -391,7 +391,7 @@ int adscf_propagate_diblock_dev(adscf_ctx* ctx, const double* d_field, double* d
   ScfDev S2 = ctx->S;
   S2.dens = d_density;
   launch_closure(S2, 0, ctx->closure_blocks, ctx->stream);
-  k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
+  k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(S2, 1, 0);
   CK(cudaGetLastError());
   return read_result(ctx, nullptr, out);
 }
@@ -424,7 +424,7 @@ int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* den
   ScfDev S2 = ctx->S;
   S2.dens = d_out;
   launch_closure(S2, 0, ctx->closure_blocks, ctx->stream);
-  k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
+  k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(S2, 1, 0);
   CK(cudaGetLastError());
   if ((rc = read_result(ctx, nullptr, out))) return rc;
   return d2h(ctx, density, d_out, nv);
@@ -493,7 +493,7 @@ int adscf_interaction_energy(adscf_ctx* ctx, const double* density, double* ener
   S2.mixing_type = 1;
   // the closure reads *iter to locate slots; slot 0 of S2 is d_tmp+nv
   launch_closure(S2, CL_MEANFIELD | CL_KEEP_OLD, ctx->closure_blocks, ctx->stream);
-  k_solve<<<1, 64, 0, ctx->stream>>>(S2, 1, 0);
+  k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(S2, 1, 0);
   CK(cudaGetLastError());
   double r[R_COUNT];
   CK(cudaMemcpyAsync(r, ctx->d_res, sizeof(r), cudaMemcpyDeviceToHost, ctx->stream));
@@ -528,7 +528,7 @@ int adscf_mix_dev(adscf_ctx* ctx, double* d_field, const double* d_dfield, int i
   ScfDev S2 = ctx->S;
   S2.wall_mask = 0;  // the caller packs what is mixed (Mix_Fields)
   k_mixdots<<<ctx->closure_blocks, SCF_THREADS, 0, ctx->stream>>>(S2);
-  k_solve<<<1, 64, 0, ctx->stream>>>(S2, 0, 1);
+  k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(S2, 0, 1);
   k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(S2, nullptr, 0.0);
   CK(cudaGetLastError());
   const int nxt = (iter + 1) % ctx->hist_slots;
@@ -730,7 +730,7 @@ int adscf_enqueue(adscf_ctx* ctx, int stage, int repeats) {
       else rc = film_enqueue_contour(ctx);
     } else if (stage == ADSCF_STAGE_UPDATE) {
       launch_closure(ctx->S, CL_MEANFIELD | CL_MIXDOTS, ctx->closure_blocks, ctx->stream);
-      k_solve<<<1, 64, 0, ctx->stream>>>(ctx->S, 1, 1);
+      k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(ctx->S, 1, 1);
       CK(cudaGetLastError());
       rc = ctx->geometry == ADSCF_BULK ? bulk_mix_e(ctx)
            : (k_mix<float><<<ctx->mix_blocks, SCF_THREADS, 0, ctx->stream>>>(ctx->S, nullptr, 0.0),

@@ -208,7 +208,7 @@ int conj_solve(adscf_ctx* ctx, const double* d_target, double tol, int itermax, 
   for (it = 1; it <= itermax; ++it) {
     if ((rc = bulk_enqueue_propagate(ctx))) return rc;
     launch_closure(S2, CL_CONJ | CL_MIXDOTS, ctx->closure_blocks, st);
-    k_solve<<<1, 64, 0, st>>>(S2, 2, 1);
+    k_solve<<<1, SOLVE_THREADS, 0, st>>>(S2, 2, 1);
     CK(cudaGetLastError());
     double r[R_COUNT];
     CK(cudaMemcpyAsync(r, ctx->d_res, sizeof(r), cudaMemcpyDeviceToHost, st));

@@ -27,6 +27,8 @@
 #define SCF_MAX_SLOTS (SCF_MAX_HIST + 1)
 #define NP_FIXED 7
 #define NPART (NP_FIXED + SCF_MAX_SLOTS)
+// the solve's block: one warp per partial-sum entry at a time (8 warps)
+#define SOLVE_THREADS 256
 
 enum { P_ACC = 0, P_PHIW = 1, P_EINT = 2, P_RHO = 3, P_EEXT = 4, P_LNUM = 5, P_LDEN = 6 };
 
