@@ -143,18 +143,44 @@ __device__ __forceinline__ void ff_fma(float& sh, float& sl, float ch, float cl,
   sl = t - (sh - s);
 }
 
+// (ah, al) += (bh, bl) in float-float (TwoSum of the high parts)
+__device__ __forceinline__ void ff_add(float& ah, float& al, float bh, float bl) {
+  const float s = ah + bh;
+  const float bb = s - ah;
+  const float t = (ah - (s - bb)) + (bh - bb) + al + bl;
+  ah = s + t;
+  al = t - (ah - s);
+}
+
+// out[z] = sum_d c[d] in[z - d mod n] in float-float.  The pencil is one
+// CTA's extra work in its pass, so its serial chain sets that CTA's finish:
+// four interleaved partial sums per output (d mod 4) shorten the dependent
+// chain fourfold, and are combined pairwise at the end.
 __device__ __forceinline__ void dc_pencil_apply(int n, DcPencil D) {
   for (int z = threadIdx.x; z < n; z += blockDim.x) {
-    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-    for (int d = 0; d < n; ++d) {
-      int zz = z - d;
-      if (zz < 0) zz += n;
-      const float2 p = D.in[zz];
-      const float2 c = D.c[d];
-      ff_fma(rh, rl, c.x, c.y, p.x);
-      ff_fma(ih, il, c.x, c.y, p.y);
+    float rh[4] = {0.f, 0.f, 0.f, 0.f}, rl[4] = {0.f, 0.f, 0.f, 0.f};
+    float ih[4] = {0.f, 0.f, 0.f, 0.f}, il[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int d0 = 0; d0 < n; d0 += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int d = d0 + u;
+        if (d < n) {
+          int zz = z - d;
+          if (zz < 0) zz += n;
+          const float2 p = D.in[zz];
+          const float2 c = D.c[d];
+          ff_fma(rh[u], rl[u], c.x, c.y, p.x);
+          ff_fma(ih[u], il[u], c.x, c.y, p.y);
+        }
+      }
     }
-    D.out[z] = make_float2(rh + rl, ih + il);
+    ff_add(rh[0], rl[0], rh[1], rl[1]);
+    ff_add(rh[2], rl[2], rh[3], rl[3]);
+    ff_add(rh[0], rl[0], rh[2], rl[2]);
+    ff_add(ih[0], il[0], ih[1], il[1]);
+    ff_add(ih[2], il[2], ih[3], il[3]);
+    ff_add(ih[0], il[0], ih[2], il[2]);
+    D.out[z] = make_float2(rh[0] + rl[0], ih[0] + il[0]);
   }
 }
 
