@@ -422,9 +422,11 @@ def batch_legs(torch, A, stream, args):
     return out
 
 
-def run_profile():
+def run_profile(pass_plan=None):
     """One SCF iteration's stages at 128^3, ds = 0.05 (20 contour steps, 340 MB
-    of slices) on the split path: the kernels of the bench, few launches."""
+    of slices) on the split path: the kernels of the bench, few launches.
+    ``pass_plan`` (y, z, x) pins the pass kernels (with ADSCF_AUTOTUNE=0 the
+    context skips the tuner's candidate launches)."""
     import adscf_gb300 as A
     from adscf_gb300 import _lib as L_
     w = c3_fields()
@@ -432,6 +434,8 @@ def run_profile():
                   block_length=(F_A, 1.0 - F_A), kappa=KAPPA, chi=CHI, precision=A.SPLIT,
                   mixing_type=A.MIX_ANDERSON, mixing_dim=M_HIST, lam=LAM, lam_warm=LAM,
                   warm_iters=M_HIST)
+    if pass_plan:
+        c.set_pass_plan(*pass_plan)
     c.set_field(w)
     for st in (L_.STAGE_PROPAGATE, L_.STAGE_CONTOUR, L_.STAGE_UPDATE):
         c._ck(c.lib.adscf_enqueue(c.h, st, 1))
@@ -457,9 +461,13 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="small run for ncu: one propagation, contour and update of the "
                          "split path at 128^3 with 20 contour steps")
+    ap.add_argument("--pass-plan", default=None,
+                    help="with --profile: pin the Y, Z, X pass kernels, e.g. 2,2,3 "
+                         "(0 plain, 1 persistent, 2 TMA, 3 fused XY)")
     args = ap.parse_args()
     if args.profile:
-        return run_profile()
+        plan = tuple(int(v) for v in args.pass_plan.split(",")) if args.pass_plan else None
+        return run_profile(plan)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     if args.impl == "reference":
