@@ -126,9 +126,11 @@ template <typename T>
 __device__ __forceinline__ void cn_row(const FilmDev<T>& F, const CnStep& st, int j, double w64, float w32,
                                        T& a, T& c, T& b, T& hw) {
   if constexpr (sizeof(T) == 4) {
+    // b_j = ds (alpha_j + gamma_j) exactly in the mesh formulas: b = -(a + c)
+    // keeps the rounded row conservative and spares a load and a product
     a = r_mul(-st.dsf, F.alf[j]);
     c = r_mul(-st.dsf, F.gaf[j]);
-    b = r_mul(st.dsf, F.bef[j]);
+    b = -r_add(a, c);
     hw = r_mul(st.hdsf, w32);
   } else {
     a = (T)(-st.ds * F.alpha[j]);
@@ -138,11 +140,20 @@ __device__ __forceinline__ void cn_row(const FilmDev<T>& F, const CnStep& st, in
   }
 }
 
+// the hardware reciprocal (MUFU, within one ulp): one instruction on the
+// sweep's critical path instead of a correctly rounded sequence
+__device__ __forceinline__ float rcp_hw(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // One row of the Thomas elimination: returns gam_j and advances the pivot
 // state, the eliminated right-hand side and c_{j-1}.  FP64 divides by the
-// pivot (bet = pivot); FP32 keeps its correctly rounded reciprocal (bet =
-// 1 / pivot) and multiplies, one reciprocal instead of two divisions per row
-// (the FP32 sweeps are bound by instruction issue).  Row 0 starts from
+// pivot (bet = pivot); FP32 keeps its reciprocal (bet = 1 / pivot) and
+// multiplies: one reciprocal instead of two divisions per row (the FP32
+// sweeps are bound by instruction issue; the increment form keeps the
+// reciprocal's ulp relative to the small increment).  Row 0 starts from
 // bet = 1 in both forms.
 template <typename T>
 __device__ __forceinline__ T thomas_row(T& bet, T& cprev, T& uprev, T a, T c, T diag, T rhs, int* err) {
@@ -150,7 +161,7 @@ __device__ __forceinline__ T thomas_row(T& bet, T& cprev, T& uprev, T a, T c, T 
     const T g = r_mul(cprev, bet);
     const T piv = r_fma(-a, g, diag);
     if (piv == (T)0) atomicOr(err, 1);
-    bet = __frcp_rn(piv);
+    bet = rcp_hw(piv);
     uprev = r_mul(r_fma(-a, uprev, rhs), bet);
     cprev = c;
     return g;
@@ -578,6 +589,7 @@ k_film1d_chains_sm(const FilmDev<T>* __restrict__ Fs, const ScfDev* __restrict__
       qv[gz * W] = v;
       qn[gz] = v;
     }
+#pragma unroll 4
     for (int j = gz - 1; j >= 0; --j) {
       const T u = r_fma(-gv[(j + 1) * W], unext, dv[j * W]);
       const T v = inc ? r_add(qv[j * W], u) : u;

@@ -22,8 +22,8 @@ def ctx(grid, size, ds, prec=FP64, **kw):
                    warm_iters=4, **kw)
 
 
-@pytest.mark.parametrize("grid,prec,tol", [((12, 10, 8), FP64, 1e-12), ((32, 32, 32), FP64, 1e-12),
-                                           ((32, 32, 32), SPLIT, 2e-6)])
+@pytest.mark.parametrize("grid,prec,tol", [((12, 10, 8), FP64, 1e-12), ((15, 9, 10), FP64, 1e-12),
+                                           ((32, 32, 32), FP64, 1e-12), ((32, 32, 32), SPLIT, 2e-6)])
 def test_ddft_rhs_matches_oracle(grid, prec, tol, rng):
     gx, gy, gz = grid
     size = (6.0, 5.0, 4.0)

@@ -14,7 +14,9 @@ SIX = ((0.5, 0.1, 0.1, 0.1, 0.1, 0.1), (0, 1, 0, 1, 0, 1))   # Main_Multiblock's
 ABA = ((0.25, 0.5, 0.25), (0, 1, 0))
 BAAB = ((0.2, 0.3, 0.1, 0.4), (1, 0, 0, 1))                   # adjacent blocks of one type
 HOMO = ((1.0,), (0,))
-SEQS = [SIX, ABA, BAAB, HOMO]
+ZERO = ((0.5, 0.0, 0.5), (0, 1, 0))                             # a zero-length block
+SIXTEEN = (tuple([0.0625] * 16), tuple(k % 2 for k in range(16)))   # the maximum count
+SEQS = [SIX, ABA, BAAB, HOMO, ZERO, SIXTEEN]
 
 
 def mbctx(grid, size, ds, prec, seq, **kw):
