@@ -67,11 +67,14 @@ def test_single_mode_decay():
 
 
 @pytest.mark.parametrize("prec", [FP64, SPLIT])
-def test_constant_field_known_answer(prec):
-    """w = const: q(s) = exp(-w s), Q = V exp(-w), phi_A = rho f_A."""
-    grid, size, ds = (16, 8, 12), (3.0, 2.0, 2.5), 0.02
+@pytest.mark.parametrize("grid", [(16, 8, 12), (256, 256, 256)])
+def test_constant_field_known_answer(prec, grid):
+    """w = const: q(s) = exp(-w s), Q = V exp(-w), phi_A = rho f_A; also at
+    the largest register line length (256^3, 20 contour steps)."""
+    size, ds = (3.0, 2.0, 2.5), (0.02 if grid[0] == 16 else 0.05)
     w0 = 0.7
-    field = np.full((2, 12, 8, 16), w0)
+    gx, gy, gz = grid
+    field = np.full((2, gz, gy, gx), w0)
     with mkctx(grid, size, ds, prec, f=(0.3, 0.7)) as c:
         dens, res = c.propagate_diblock(field)
     V = 15.0
