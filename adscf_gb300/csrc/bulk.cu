@@ -189,6 +189,10 @@ int setup_tma(adscf_ctx* ctx, void* spec) {
     CK(cudaMalloc(&ctx->d_flags, sizeof(int)));
     CK(cudaMemset(ctx->d_flags, 0, sizeof(int)));
   }
+  if (!ctx->d_dcin) {
+    CK(cudaMalloc(&ctx->d_dcin, 2 * (size_t)NN * sizeof(float2)));
+    CK(cudaMemset(ctx->d_dcin, 0, 2 * (size_t)NN * sizeof(float2)));
+  }
   ctx->tma = NN;
   return ADSCF_OK;
 }
@@ -354,7 +358,7 @@ void xy_pass(adscf_ctx* ctx, int t) {
   const BulkDev<float>* df = static_cast<const BulkDev<float>*>(ctx->d_inst);
   const float2* twf = static_cast<const float2*>(ctx->d_tw);
   k_xy_tma<NN><<<ctx->xy_grid, tmak::XYLayout<NN>::THREADS, ctx->xy_smem, ctx->stream>>>(
-      df, ctx->tmap_y, twf, t, ctx->d_flags);
+      df, ctx->tmap_y, twf, ctx->d_g64, ctx->d_dcin, t, ctx->d_flags);
 }
 
 template <typename T, int NN>
@@ -366,7 +370,8 @@ void step_nn(adscf_ctx* ctx, int t) {
   const double* g64 = ctx->d_g64;
   cudaStream_t s = ctx->stream;
   const size_t sm = ctx->smem_x;
-  auto spass = [&](int kind) {
+  // dc = 0: the TMA z pass leaves the (0, 0) pencil to the fused XY pass
+  auto spass = [&](int kind, int dc = 1) {
     const int pk = kind == 2 ? ctx->plan_z : ctx->plan_y;
     if constexpr (sizeof(T) == 4 && (NN == 64 || NN == 128)) {
       if (pk == PK_TMA) {
@@ -377,9 +382,9 @@ void step_nn(adscf_ctx* ctx, int t) {
         const int tiles = z ? ctx->tma_tiles_z : ctx->tma_tiles_y;
         const int grid = std::min(ctx->tma_grid, tiles);
         const CUtensorMap& map = z ? ctx->tmap_z : ctx->tmap_y;
-        if (kind == 0) k_rs_tma<NN, 0><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, ctx->d_flags);
-        else if (kind == 1) k_rs_tma<NN, 1><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, ctx->d_flags);
-        else k_rs_tma<NN, 2><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, ctx->d_flags);
+        if (kind == 0) k_rs_tma<NN, 0><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
+        else if (kind == 1) k_rs_tma<NN, 1><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
+        else k_rs_tma<NN, 2><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
         return;
       }
     }
@@ -393,7 +398,7 @@ void step_nn(adscf_ctx* ctx, int t) {
   };
   if constexpr (sizeof(T) == 4 && (NN == 64 || NN == 128)) {
     if (ctx->plan_x == PK_FUSED) {   // Z, then Yi + X + Yf of the next step in one plane pass
-      spass(2);
+      spass(2, 0);
       xy_pass<NN>(ctx, t);
       return;
     }
@@ -714,7 +719,7 @@ void bulk_destroy(adscf_ctx* ctx) {
   }
   cudaFree(ctx->d_wtab);
   cudaFree(ctx->d_inst); cudaFree(ctx->d_tw); cudaFree(ctx->d_fk);
-  cudaFree(ctx->d_tw64); cudaFree(ctx->d_g64); cudaFree(ctx->d_flags);
+  cudaFree(ctx->d_tw64); cudaFree(ctx->d_g64); cudaFree(ctx->d_flags); cudaFree(ctx->d_dcin);
   cudaFree(ctx->d_work_x); cudaFree(ctx->d_work_y); cudaFree(ctx->d_work_z);
   cudaFree(ctx->d_qpart);
 }

@@ -70,15 +70,18 @@ __device__ __forceinline__ double emul(double z, double hi, double) { return z *
 
 // Boltzmann factors of one point, stored interleaved so one 16-byte (FP32)
 // or 16-byte (FP64) load brings both species: FP32 keeps (A, B, A residue,
-// B residue) as float4, FP64 keeps (A, B) as double2.
+// B residue) as float4, FP64 keeps (A, B) as double2.  No kernel that reads
+// them writes them, so they are read through the non-coherent path: the
+// compiler may then issue these loads ahead of the slice stores that follow
+// them (which it cannot prove do not alias).
 template <typename T>
 struct EPt { T a, b, al, bl; };
 __device__ __forceinline__ EPt<float> load_ept(const float* E, size_t g) {
-  const float4 v = reinterpret_cast<const float4*>(E)[g];
+  const float4 v = __ldg(reinterpret_cast<const float4*>(E) + g);
   return {v.x, v.y, v.z, v.w};
 }
 __device__ __forceinline__ EPt<double> load_ept(const double* E, size_t g) {
-  const double2 v = reinterpret_cast<const double2*>(E)[g];
+  const double2 v = __ldg(reinterpret_cast<const double2*>(E) + g);
   return {v.x, v.y, 0.0, 0.0};
 }
 // e = exp(-ds w/2) of species c at point p
@@ -154,15 +157,19 @@ __device__ __forceinline__ void ff_add(float& ah, float& al, float bh, float bl)
 
 // out[z] = sum_d c[d] in[z - d mod n] in float-float.  The pencil is one
 // CTA's extra work in its pass, so its serial chain sets that CTA's finish:
-// four interleaved partial sums per output (d mod 4) shorten the dependent
-// chain fourfold, and are combined pairwise at the end.
+// eight interleaved partial sums per output (chain u = d mod 8, each in
+// increasing d) shorten the dependent chain eightfold, and are combined
+// pairwise: ((0+1) + (2+3)) + ((4+5) + (6+7)).  The fused XY pass evaluates
+// the same sums with one lane per chain (dc_point) and gets the same bits.
+constexpr int kDcChains = 8;
 __device__ __forceinline__ void dc_pencil_apply(int n, DcPencil D) {
   for (int z = threadIdx.x; z < n; z += blockDim.x) {
-    float rh[4] = {0.f, 0.f, 0.f, 0.f}, rl[4] = {0.f, 0.f, 0.f, 0.f};
-    float ih[4] = {0.f, 0.f, 0.f, 0.f}, il[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int d0 = 0; d0 < n; d0 += 4) {
+    float rh[kDcChains], rl[kDcChains], ih[kDcChains], il[kDcChains];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < kDcChains; ++u) rh[u] = rl[u] = ih[u] = il[u] = 0.f;
+    for (int d0 = 0; d0 < n; d0 += kDcChains) {
+#pragma unroll
+      for (int u = 0; u < kDcChains; ++u) {
         const int d = d0 + u;
         if (d < n) {
           int zz = z - d;
@@ -174,12 +181,13 @@ __device__ __forceinline__ void dc_pencil_apply(int n, DcPencil D) {
         }
       }
     }
-    ff_add(rh[0], rl[0], rh[1], rl[1]);
-    ff_add(rh[2], rl[2], rh[3], rl[3]);
-    ff_add(rh[0], rl[0], rh[2], rl[2]);
-    ff_add(ih[0], il[0], ih[1], il[1]);
-    ff_add(ih[2], il[2], ih[3], il[3]);
-    ff_add(ih[0], il[0], ih[2], il[2]);
+#pragma unroll
+    for (int st = 1; st < kDcChains; st *= 2)
+#pragma unroll
+      for (int u = 0; u < kDcChains; u += 2 * st) {
+        ff_add(rh[u], rl[u], rh[u + st], rl[u + st]);
+        ff_add(ih[u], il[u], ih[u + st], il[u + st]);
+      }
     D.out[z] = make_float2(rh[0] + rl[0], ih[0] + il[0]);
   }
 }

@@ -109,7 +109,7 @@ template <int N, int KIND>
 __global__ void __launch_bounds__(BULK_THREADS, 2)
 k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUtensorMap tmap,
          int ntiles, const float2* __restrict__ gtw, const float* __restrict__ fk,
-         const double* __restrict__ g64, int t, int* __restrict__ err) {
+         const double* __restrict__ g64, int t, int dc, int* __restrict__ err) {
   using LY = tmak::TmaLayout<N>;
   using F = typename LY::F;
   constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
@@ -130,28 +130,6 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   const int gx = I.gx, gy = I.gy;
   const int lgx = regk::ilog2(gx);
   const int tw_off = zdir ? I.pz.tw_off : I.py.tw_off;
-  if (threadIdx.x == 0) {
-    tmak::mbar_init(&bar[0], 1);
-    tmak::mbar_init(&bar[1], 1);
-    tmak::fence_mbar_init();
-  }
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
-  if constexpr (KIND == 2) {
-    const float* gzt = fk + I.gz_off;
-    for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) gzs[i] = gzt[i];
-  }
-  const size_t es = zdir ? (size_t)gx * gy : (size_t)gx;
-  float2* spec = I.spec;
-  // (0, 0) pencil in float-float (CTA 0 handles tile 0 first)
-  const bool dcblk = zdir && blockIdx.x == 0;
-  float2* dcf = reinterpret_cast<float2*>(smraw + LY::dc_off);
-  const DcPencil dcp{dcf, dcf + N, dcf + 2 * N};
-  __syncthreads();
-  if (dcblk) {
-    dc_pencil_load<float>(spec, es, N, g64 + I.g64_off, dcp);
-    __syncthreads();
-    dc_pencil_apply(N, dcp);
-  }
   auto coords = [&](int tile, int b, int& cx, int& cy, int& cz) {
     const int L0 = tile * LPC;
     const int o = L0 >> lgx, x0 = (L0 & (gx - 1)) + b * tmak::kBoxCols;
@@ -166,9 +144,31 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       tmak::tma_load_3d(buf + (size_t)s * LY::tile_elems + b * LY::box_elems, &tmap, &bar[s], cx, cy, cz);
     }
   };
-  // loads issued / completed per stage (thread 0), to drain on an early exit
   int issued[2] = {0, 0}, done[2] = {0, 0};
-  if (threadIdx.x == 0 && blockIdx.x < ntiles) { issue_load(blockIdx.x, 0); issued[0] = 1; }
+  if (threadIdx.x == 0) {
+    tmak::mbar_init(&bar[0], 1);
+    tmak::mbar_init(&bar[1], 1);
+    tmak::fence_mbar_init();
+    if (blockIdx.x < ntiles) { issue_load(blockIdx.x, 0); issued[0] = 1; }
+  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
+  if constexpr (KIND == 2) {
+    const float* gzt = fk + I.gz_off;
+    for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) gzs[i] = gzt[i];
+  }
+  const size_t es = zdir ? (size_t)gx * gy : (size_t)gx;
+  float2* spec = I.spec;
+  // (0, 0) pencil in float-float (CTA 0 handles tile 0 first); with dc = 0
+  // the fused XY pass that follows applies it instead
+  const bool dcblk = zdir && dc && blockIdx.x == 0;
+  float2* dcf = reinterpret_cast<float2*>(smraw + LY::dc_off);
+  const DcPencil dcp{dcf, dcf + N, dcf + 2 * N};
+  __syncthreads();
+  if (dcblk) {
+    dc_pencil_load<float>(spec, es, N, g64 + I.g64_off, dcp);
+    __syncthreads();
+    dc_pencil_apply(N, dcp);
+  }
   const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
   const int box = line / tmak::kBoxCols, col = line % tmak::kBoxCols;
   float2* sc = ex + line * F::LS;
@@ -273,10 +273,44 @@ struct XYLayout {
   static constexpr uint32_t plane_bytes = (uint32_t)N * N * 8;
   static constexpr size_t sc_off = plane_bytes;             // plane at 0 (1024-aligned)
   static constexpr size_t tw_off = sc_off + (size_t)LINES * F::LS * sizeof(float2);
-  static constexpr size_t bar_off = ((tw_off + N * sizeof(float2) + 15) / 16) * 16;
+  static constexpr size_t dc_off = tw_off + N * sizeof(float2);     // (0,0) pencil in [N], kernel [N]
+  static constexpr size_t bar_off = ((dc_off + 2 * N * sizeof(float2) + 15) / 16) * 16;
   static constexpr size_t bytes = bar_off + sizeof(uint64_t) + 1024;   // + alignment slack
   static_assert(N % LINES == 0 || LINES % N == 0, "rounds of whole lines");
 };
+
+// (0, 0) entry of plane z after the z pass, in float-float: the circular
+// convolution sum_d c[d] in[z - d mod n] that the z pass's pencil CTA
+// evaluates (dc_pencil_apply), for one output.  Lanes 0-7 of the calling
+// warp run the eight real-part chains ((d mod 8) = lane), lanes 8-15 the
+// imaginary ones, each summing its terms in increasing d; the chains are then
+// combined pairwise as ((0+1) + (2+3)) + ((4+5) + (6+7)) -- the operations
+// of the pencil CTA in the same order, so the result is bit for bit the
+// same.  Every lane of the warp calls it; the value is returned in lane 0.
+__device__ __forceinline__ float2 dc_point(const float2* in, const float2* c, int n, int z) {
+  const int lane = threadIdx.x & 31;
+  const int u = lane & (kDcChains - 1);
+  const bool im = lane & kDcChains;
+  float sh = 0.f, sl = 0.f;
+  if (lane < 2 * kDcChains) {
+    for (int d = u; d < n; d += kDcChains) {
+      int zz = z - d;
+      if (zz < 0) zz += n;
+      const float2 p = in[zz];
+      const float2 cc = c[d];
+      ff_fma(sh, sl, cc.x, cc.y, im ? p.y : p.x);
+    }
+  }
+#pragma unroll
+  for (int st = 1; st < kDcChains; st *= 2) {
+    const float oh = __shfl_down_sync(0xffffffffu, sh, st);
+    const float ol = __shfl_down_sync(0xffffffffu, sl, st);
+    if ((u & (2 * st - 1)) == 0) ff_add(sh, sl, oh, ol);
+  }
+  const float r = sh + sl;
+  const float ri = __shfl_down_sync(0xffffffffu, r, kDcChains);
+  return make_float2(r, ri);
+}
 
 // element (row j, column x) of a plane held as N/16 swizzled 16-column boxes
 template <int N>
@@ -289,7 +323,8 @@ __device__ __forceinline__ int plane_at(int j, int x) {
 template <int N>
 __global__ void __launch_bounds__(512, 1)
 k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUtensorMap tmap,
-         const float2* __restrict__ gtw, int t, int* __restrict__ err) {
+         const float2* __restrict__ gtw, const double* __restrict__ g64,
+         float2* __restrict__ dcin, int t, int* __restrict__ err) {
   using LY = tmak::XYLayout<N>;
   using F = typename LY::F;
   constexpr int R1 = F::R1, TPL = F::TPL, LINES = LY::LINES;
@@ -299,17 +334,40 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   float2* plane = reinterpret_cast<float2*>(smraw);
   float2* scr = reinterpret_cast<float2*>(smraw + LY::sc_off);
   float2* tw = reinterpret_cast<float2*>(smraw + LY::tw_off);
+  float2* dci = reinterpret_cast<float2*>(smraw + LY::dc_off);
+  float2* dck = dci + N;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smraw + LY::bar_off);
   const BulkDev<float>& I = insts[0];
   if (t > I.ns) return;
   const bool init = t == 0;
   const bool more = init || t < I.ns;
   const int gz = I.gz;
+  int it = 0, issued = 0, done = 0;
+  auto issue_plane = [&](int z) {
+    tmak::mbar_expect_tx(bar, LY::plane_bytes);
+    for (int b = 0; b < LY::NB; ++b)
+      tmak::tma_load_3d(plane + b * LY::box_elems, &tmap, bar, b * tmak::kBoxCols, 0, z);
+    ++issued;
+  };
+  // the first plane's load is issued at once; its latency overlaps the
+  // twiddle loads below
   if (threadIdx.x == 0) {
     tmak::mbar_init(bar, 1);
     tmak::fence_mbar_init();
+    if (!init && (int)blockIdx.x < gz) issue_plane(blockIdx.x);
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[I.px.tw_off + i];
+  // (0, 0) pencil: this step's z pass left it in FP32; the float-float
+  // convolution of the pencil as the previous plane pass wrote it
+  // (dcin[t mod 2]) replaces it, plane by plane
+  if (!init) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      dci[i] = dcin[(t & 1) * N + i];
+      const double c = g64[I.g64_off + i];
+      const float h = (float)c;
+      dck[i] = make_float2(h, (float)(c - (double)h));
+    }
+  }
   __syncthreads();
   const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
   const bool active = line < N;          // N = 64 leaves no idle line; kept for clarity
@@ -319,23 +377,23 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   const bool fA = chain_type_fwd(I, tt) == 0, bA = chain_type_bwd(I, tt) == 0;
   const bool fA2 = chain_type_fwd(I, t + 1) == 0, bA2 = chain_type_bwd(I, t + 1) == 0;
   float2* sl = I.slices + (size_t)t * I.npts;
-  int it = 0, issued = 0, done = 0;
   for (int z = blockIdx.x; z < gz; z += gridDim.x, ++it) {
     const size_t pbase = (size_t)z * N * N;
     if (!init) {
-      if (threadIdx.x == 0) {
+      if (threadIdx.x == 0 && it > 0) {
         tmak::bulk_wait_read0();          // the previous plane's stores have read the buffer
-        tmak::mbar_expect_tx(bar, LY::plane_bytes);
-        for (int b = 0; b < LY::NB; ++b)
-          tmak::tma_load_3d(plane + b * LY::box_elems, &tmap, bar, b * tmak::kBoxCols, 0, z);
-        ++issued;
+        issue_plane(z);
       }
+      float2 dco = make_float2(0.f, 0.f);
+      if (threadIdx.x < 32) dco = tmak::dc_point(dci, dck, N, z);   // while the plane is in flight
       const bool got = tmak::mbar_wait_bounded(bar, (uint32_t)(it & 1), tmak::kWaitPolls);
       if (!__syncthreads_and(got)) {
         if (threadIdx.x == 0) atomicOr(err, 8);
         break;
       }
       ++done;
+      if (threadIdx.x == 0) plane[tmak::plane_at<N>(0, 0)] = dco;
+      __syncthreads();
       // phase 1: inverse y, columns x
       for (int c0 = 0; c0 < N; c0 += LINES) {
         const int x = c0 + line;
@@ -409,6 +467,7 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       for (int b = 0; b < LY::NB; ++b)
         tmak::tma_store_3d(&tmap, plane + b * LY::box_elems, b * tmak::kBoxCols, 0, z);
       tmak::bulk_commit();
+      dcin[((t + 1) & 1) * N + z] = plane[tmak::plane_at<N>(0, 0)];   // the next z pass's pencil
     }
   }
   if (threadIdx.x == 0) {
