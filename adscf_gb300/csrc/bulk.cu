@@ -352,13 +352,32 @@ int create_t(adscf_ctx* ctx) {
 template <typename T>
 int expfield_t(adscf_ctx* ctx, const double* d_w);
 
+// Launch with programmatic stream serialisation: the kernel may start while
+// the previous kernel on the stream finishes; the TMA passes wait for it
+// (griddepcontrol.wait) before they touch its output.
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 // fused XY plane pass of step t (t = 0: the initial plane)
 template <int NN>
 void xy_pass(adscf_ctx* ctx, int t) {
   const BulkDev<float>* df = static_cast<const BulkDev<float>*>(ctx->d_inst);
   const float2* twf = static_cast<const float2*>(ctx->d_tw);
-  k_xy_tma<NN><<<ctx->xy_grid, tmak::XYLayout<NN>::THREADS, ctx->xy_smem, ctx->stream>>>(
-      df, ctx->tmap_y, twf, ctx->d_g64, ctx->d_dcin, t, ctx->d_flags);
+  launch_pdl(k_xy_tma<NN>, ctx->xy_grid, tmak::XYLayout<NN>::THREADS, ctx->xy_smem, ctx->stream,
+             df, ctx->tmap_y, twf, (const double*)ctx->d_g64, ctx->d_dcin, t, ctx->d_flags);
 }
 
 template <typename T, int NN>
@@ -382,9 +401,9 @@ void step_nn(adscf_ctx* ctx, int t) {
         const int tiles = z ? ctx->tma_tiles_z : ctx->tma_tiles_y;
         const int grid = std::min(ctx->tma_grid, tiles);
         const CUtensorMap& map = z ? ctx->tmap_z : ctx->tmap_y;
-        if (kind == 0) k_rs_tma<NN, 0><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
-        else if (kind == 1) k_rs_tma<NN, 1><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
-        else k_rs_tma<NN, 2><<<grid, BULK_THREADS, ctx->tma_smem, s>>>(df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
+        if (kind == 0) launch_pdl(k_rs_tma<NN, 0>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
+        else if (kind == 1) launch_pdl(k_rs_tma<NN, 1>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
+        else launch_pdl(k_rs_tma<NN, 2>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
         return;
       }
     }

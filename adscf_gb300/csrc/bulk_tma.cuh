@@ -73,6 +73,15 @@ __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_
 __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// Programmatic dependent launch: the two passes of a double step are launched
+// with programmatic stream serialisation, so the next pass's CTAs may start
+// (and load their constant tables) while this one finishes.  launch_dependents
+// lets them start; wait blocks until the previous grid has completed and its
+// memory is visible.  Without such a launch both return at once.
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // element offset of (row j, column c) in a 16-column box with 128-byte swizzle
 __device__ __forceinline__ int swz(int j, int c) {
@@ -145,10 +154,14 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
     }
   };
   int issued[2] = {0, 0}, done[2] = {0, 0};
+  tmak::pdl_launch_dependents();
+  // the first tile's load is issued as soon as the previous pass is complete;
+  // the other threads load the constant tables meanwhile
   if (threadIdx.x == 0) {
     tmak::mbar_init(&bar[0], 1);
     tmak::mbar_init(&bar[1], 1);
     tmak::fence_mbar_init();
+    tmak::pdl_wait();
     if (blockIdx.x < ntiles) { issue_load(blockIdx.x, 0); issued[0] = 1; }
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
@@ -156,6 +169,7 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
     const float* gzt = fk + I.gz_off;
     for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) gzs[i] = gzt[i];
   }
+  tmak::pdl_wait();
   const size_t es = zdir ? (size_t)gx * gy : (size_t)gx;
   float2* spec = I.spec;
   // (0, 0) pencil in float-float (CTA 0 handles tile 0 first); with dc = 0
@@ -349,11 +363,13 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       tmak::tma_load_3d(plane + b * LY::box_elems, &tmap, bar, b * tmak::kBoxCols, 0, z);
     ++issued;
   };
-  // the first plane's load is issued at once; its latency overlaps the
-  // twiddle loads below
+  tmak::pdl_launch_dependents();
+  // the first plane's load is issued as soon as the previous pass is
+  // complete; the other threads load the constant tables meanwhile
   if (threadIdx.x == 0) {
     tmak::mbar_init(bar, 1);
     tmak::fence_mbar_init();
+    tmak::pdl_wait();
     if (!init && (int)blockIdx.x < gz) issue_plane(blockIdx.x);
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[I.px.tw_off + i];
@@ -362,12 +378,14 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   // (dcin[t mod 2]) replaces it, plane by plane
   if (!init) {
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      dci[i] = dcin[(t & 1) * N + i];
       const double c = g64[I.g64_off + i];
       const float h = (float)c;
       dck[i] = make_float2(h, (float)(c - (double)h));
     }
   }
+  tmak::pdl_wait();
+  if (!init)
+    for (int i = threadIdx.x; i < N; i += blockDim.x) dci[i] = dcin[(t & 1) * N + i];
   __syncthreads();
   const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
   const bool active = line < N;          // N = 64 leaves no idle line; kept for clarity
