@@ -189,9 +189,9 @@ int setup_tma(adscf_ctx* ctx, void* spec) {
     CK(cudaMalloc(&ctx->d_flags, sizeof(int)));
     CK(cudaMemset(ctx->d_flags, 0, sizeof(int)));
   }
-  if (!ctx->d_dcin) {
-    CK(cudaMalloc(&ctx->d_dcin, 2 * (size_t)NN * sizeof(float2)));
-    CK(cudaMemset(ctx->d_dcin, 0, 2 * (size_t)NN * sizeof(float2)));
+  if (!ctx->d_dcin) {   // [2][NN] pencils kept by the plane pass | [NN] convolved by the z pass
+    CK(cudaMalloc(&ctx->d_dcin, 3 * (size_t)NN * sizeof(float2)));
+    CK(cudaMemset(ctx->d_dcin, 0, 3 * (size_t)NN * sizeof(float2)));
   }
   ctx->tma = NN;
   return ADSCF_OK;
@@ -377,7 +377,9 @@ void xy_pass(adscf_ctx* ctx, int t) {
   const BulkDev<float>* df = static_cast<const BulkDev<float>*>(ctx->d_inst);
   const float2* twf = static_cast<const float2*>(ctx->d_tw);
   launch_pdl(k_xy_tma<NN>, ctx->xy_grid, tmak::XYLayout<NN>::THREADS, ctx->xy_smem, ctx->stream,
-             df, ctx->tmap_y, twf, (const double*)ctx->d_g64, ctx->d_dcin, t, ctx->d_flags);
+             df, ctx->tmap_y, twf,
+             ctx->plan_z == PK_TMA ? (const float2*)(ctx->d_dcin + 2 * NN) : nullptr,
+             ctx->d_dcin, t, ctx->d_flags);
 }
 
 template <typename T, int NN>
@@ -401,9 +403,12 @@ void step_nn(adscf_ctx* ctx, int t) {
         const int tiles = z ? ctx->tma_tiles_z : ctx->tma_tiles_y;
         const int grid = std::min(ctx->tma_grid, tiles);
         const CUtensorMap& map = z ? ctx->tmap_z : ctx->tmap_y;
-        if (kind == 0) launch_pdl(k_rs_tma<NN, 0>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
-        else if (kind == 1) launch_pdl(k_rs_tma<NN, 1>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
-        else launch_pdl(k_rs_tma<NN, 2>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc, ctx->d_flags);
+        if (kind == 0) launch_pdl(k_rs_tma<NN, 0>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc,
+                   (const float2*)ctx->d_dcin, ctx->d_dcin + 2 * NN, ctx->d_flags);
+        else if (kind == 1) launch_pdl(k_rs_tma<NN, 1>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc,
+                   (const float2*)ctx->d_dcin, ctx->d_dcin + 2 * NN, ctx->d_flags);
+        else launch_pdl(k_rs_tma<NN, 2>, grid, BULK_THREADS, ctx->tma_smem, s, df, map, tiles, twf, fkf, g64, t, dc,
+                   (const float2*)ctx->d_dcin, ctx->d_dcin + 2 * NN, ctx->d_flags);
         return;
       }
     }

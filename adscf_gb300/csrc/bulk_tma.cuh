@@ -88,6 +88,39 @@ __device__ __forceinline__ int swz(int j, int c) {
   return j * 16 + ((((c >> 1) ^ (j & 7)) << 1) | (c & 1));
 }
 
+// One output z of the float-float (0, 0) pencil convolution
+// sum_d c[d] in[z - d mod n] that a z pass's pencil CTA evaluates for all z
+// (dc_pencil_apply).  Lanes 0-7 of the calling
+// warp run the eight real-part chains ((d mod 8) = lane), lanes 8-15 the
+// imaginary ones, each summing its terms in increasing d; the chains are then
+// combined pairwise as ((0+1) + (2+3)) + ((4+5) + (6+7)) -- the operations
+// of the pencil CTA in the same order, so the result is bit for bit the
+// same.  Every lane of the warp calls it; the value is returned in lane 0.
+__device__ __forceinline__ float2 dc_point(const float2* in, const float2* c, int n, int z) {
+  const int lane = threadIdx.x & 31;
+  const int u = lane & (kDcChains - 1);
+  const bool im = lane & kDcChains;
+  float sh = 0.f, sl = 0.f;
+  if (lane < 2 * kDcChains) {
+    for (int d = u; d < n; d += kDcChains) {
+      int zz = z - d;
+      if (zz < 0) zz += n;
+      const float2 p = in[zz];
+      const float2 cc = c[d];
+      ff_fma(sh, sl, cc.x, cc.y, im ? p.y : p.x);
+    }
+  }
+#pragma unroll
+  for (int st = 1; st < kDcChains; st *= 2) {
+    const float oh = __shfl_down_sync(0xffffffffu, sh, st);
+    const float ol = __shfl_down_sync(0xffffffffu, sl, st);
+    if ((u & (2 * st - 1)) == 0) ff_add(sh, sl, oh, ol);
+  }
+  const float r = sh + sl;
+  const float ri = __shfl_down_sync(0xffffffffu, r, kDcChains);
+  return make_float2(r, ri);
+}
+
 constexpr int kBoxCols = 16;           // 16 x 8 B = 128 B inner box
 constexpr int kWaitPolls = 1 << 22;    // bound of one mbarrier wait
 
@@ -118,7 +151,8 @@ template <int N, int KIND>
 __global__ void __launch_bounds__(BULK_THREADS, 2)
 k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUtensorMap tmap,
          int ntiles, const float2* __restrict__ gtw, const float* __restrict__ fk,
-         const double* __restrict__ g64, int t, int dc, int* __restrict__ err) {
+         const double* __restrict__ g64, int t, int dc, const float2* __restrict__ dcin,
+         float2* __restrict__ dcout, int* __restrict__ err) {
   using LY = tmak::TmaLayout<N>;
   using F = typename LY::F;
   constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
@@ -172,11 +206,27 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   tmak::pdl_wait();
   const size_t es = zdir ? (size_t)gx * gy : (size_t)gx;
   float2* spec = I.spec;
-  // (0, 0) pencil in float-float (CTA 0 handles tile 0 first); with dc = 0
-  // the fused XY pass that follows applies it instead
+  // (0, 0) pencil in float-float.  dc = 1: CTA 0 convolves the whole pencil
+  // before its first tile (tile 0, which holds the pencil) and stores it with
+  // that tile.  dc = 0 (fused plan): the CTAs with the fewest tiles each
+  // convolve outputs z = k, k + nlight, ... after their tiles, from the pencil
+  // the previous plane pass kept (dcin), into dcout; the plane pass that
+  // follows puts dcout[z] into its plane.
   const bool dcblk = zdir && dc && blockIdx.x == 0;
+  const int G = gridDim.x;
+  const int nlight = ntiles % G == 0 ? G : G - ntiles % G;
+  const int klight = (int)blockIdx.x - (G - nlight);
+  const bool dcsplit = zdir && !dc && klight >= 0 && klight < N;
   float2* dcf = reinterpret_cast<float2*>(smraw + LY::dc_off);
   const DcPencil dcp{dcf, dcf + N, dcf + 2 * N};
+  if (dcsplit) {
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      dcp.in[i] = dcin[(t & 1) * N + i];
+      const double c = g64[I.g64_off + i];
+      const float h = (float)c;
+      dcp.c[i] = make_float2(h, (float)(c - (double)h));
+    }
+  }
   __syncthreads();
   if (dcblk) {
     dc_pencil_load<float>(spec, es, N, g64 + I.g64_off, dcp);
@@ -248,6 +298,12 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       tmak::bulk_commit();
     }
   }
+  if (dcsplit && (threadIdx.x >> 5) == 1) {   // warp 1, while thread 0 drains the stores
+    for (int z = klight; z < N; z += nlight) {
+      const float2 o = tmak::dc_point(dcp.in, dcp.c, N, z);
+      if ((threadIdx.x & 31) == 0) dcout[z] = o;
+    }
+  }
   if (threadIdx.x == 0) {
     // loads still in flight after an early exit land before shared memory is released
     for (int st = 0; st < 2; ++st)
@@ -287,44 +343,10 @@ struct XYLayout {
   static constexpr uint32_t plane_bytes = (uint32_t)N * N * 8;
   static constexpr size_t sc_off = plane_bytes;             // plane at 0 (1024-aligned)
   static constexpr size_t tw_off = sc_off + (size_t)LINES * F::LS * sizeof(float2);
-  static constexpr size_t dc_off = tw_off + N * sizeof(float2);     // (0,0) pencil in [N], kernel [N]
-  static constexpr size_t bar_off = ((dc_off + 2 * N * sizeof(float2) + 15) / 16) * 16;
+  static constexpr size_t bar_off = ((tw_off + N * sizeof(float2) + 15) / 16) * 16;
   static constexpr size_t bytes = bar_off + sizeof(uint64_t) + 1024;   // + alignment slack
   static_assert(N % LINES == 0 || LINES % N == 0, "rounds of whole lines");
 };
-
-// (0, 0) entry of plane z after the z pass, in float-float: the circular
-// convolution sum_d c[d] in[z - d mod n] that the z pass's pencil CTA
-// evaluates (dc_pencil_apply), for one output.  Lanes 0-7 of the calling
-// warp run the eight real-part chains ((d mod 8) = lane), lanes 8-15 the
-// imaginary ones, each summing its terms in increasing d; the chains are then
-// combined pairwise as ((0+1) + (2+3)) + ((4+5) + (6+7)) -- the operations
-// of the pencil CTA in the same order, so the result is bit for bit the
-// same.  Every lane of the warp calls it; the value is returned in lane 0.
-__device__ __forceinline__ float2 dc_point(const float2* in, const float2* c, int n, int z) {
-  const int lane = threadIdx.x & 31;
-  const int u = lane & (kDcChains - 1);
-  const bool im = lane & kDcChains;
-  float sh = 0.f, sl = 0.f;
-  if (lane < 2 * kDcChains) {
-    for (int d = u; d < n; d += kDcChains) {
-      int zz = z - d;
-      if (zz < 0) zz += n;
-      const float2 p = in[zz];
-      const float2 cc = c[d];
-      ff_fma(sh, sl, cc.x, cc.y, im ? p.y : p.x);
-    }
-  }
-#pragma unroll
-  for (int st = 1; st < kDcChains; st *= 2) {
-    const float oh = __shfl_down_sync(0xffffffffu, sh, st);
-    const float ol = __shfl_down_sync(0xffffffffu, sl, st);
-    if ((u & (2 * st - 1)) == 0) ff_add(sh, sl, oh, ol);
-  }
-  const float r = sh + sl;
-  const float ri = __shfl_down_sync(0xffffffffu, r, kDcChains);
-  return make_float2(r, ri);
-}
 
 // element (row j, column x) of a plane held as N/16 swizzled 16-column boxes
 template <int N>
@@ -337,7 +359,7 @@ __device__ __forceinline__ int plane_at(int j, int x) {
 template <int N>
 __global__ void __launch_bounds__(512, 1)
 k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUtensorMap tmap,
-         const float2* __restrict__ gtw, const double* __restrict__ g64,
+         const float2* __restrict__ gtw, const float2* __restrict__ dcout,
          float2* __restrict__ dcin, int t, int* __restrict__ err) {
   using LY = tmak::XYLayout<N>;
   using F = typename LY::F;
@@ -348,8 +370,6 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   float2* plane = reinterpret_cast<float2*>(smraw);
   float2* scr = reinterpret_cast<float2*>(smraw + LY::sc_off);
   float2* tw = reinterpret_cast<float2*>(smraw + LY::tw_off);
-  float2* dci = reinterpret_cast<float2*>(smraw + LY::dc_off);
-  float2* dck = dci + N;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smraw + LY::bar_off);
   const BulkDev<float>& I = insts[0];
   if (t > I.ns) return;
@@ -373,19 +393,7 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
     if (!init && (int)blockIdx.x < gz) issue_plane(blockIdx.x);
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[I.px.tw_off + i];
-  // (0, 0) pencil: this step's z pass left it in FP32; the float-float
-  // convolution of the pencil as the previous plane pass wrote it
-  // (dcin[t mod 2]) replaces it, plane by plane
-  if (!init) {
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      const double c = g64[I.g64_off + i];
-      const float h = (float)c;
-      dck[i] = make_float2(h, (float)(c - (double)h));
-    }
-  }
   tmak::pdl_wait();
-  if (!init)
-    for (int i = threadIdx.x; i < N; i += blockDim.x) dci[i] = dcin[(t & 1) * N + i];
   __syncthreads();
   const int line = threadIdx.x / TPL, lt = threadIdx.x % TPL;
   const bool active = line < N;          // N = 64 leaves no idle line; kept for clarity
@@ -402,16 +410,21 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
         tmak::bulk_wait_read0();          // the previous plane's stores have read the buffer
         issue_plane(z);
       }
+      // (0, 0) entry: after the TMA z pass of the fused plan (dcout set) it is
+      // in FP32, and its float-float value comes from dcout (read while the
+      // plane is in flight); the other z kernels store the float-float value
+      // themselves.  Column 0 is read in phase 1 by lanes 0-7 of warp 0 only,
+      // so a warp barrier orders the write.
       float2 dco = make_float2(0.f, 0.f);
-      if (threadIdx.x < 32) dco = tmak::dc_point(dci, dck, N, z);   // while the plane is in flight
+      if (dcout && threadIdx.x == 0) dco = dcout[z];
       const bool got = tmak::mbar_wait_bounded(bar, (uint32_t)(it & 1), tmak::kWaitPolls);
       if (!__syncthreads_and(got)) {
         if (threadIdx.x == 0) atomicOr(err, 8);
         break;
       }
       ++done;
-      if (threadIdx.x == 0) plane[tmak::plane_at<N>(0, 0)] = dco;
-      __syncthreads();
+      if (dcout && threadIdx.x == 0) plane[tmak::plane_at<N>(0, 0)] = dco;
+      __syncwarp();
       // phase 1: inverse y, columns x
       for (int c0 = 0; c0 < N; c0 += LINES) {
         const int x = c0 + line;

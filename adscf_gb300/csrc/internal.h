@@ -62,7 +62,7 @@ struct adscf_ctx {
   size_t xy_smem = 0;                 // fused XY plane pass (FP32, gx = gy = 64/128)
   int xy_grid = 0;
   int* d_flags = nullptr;             // device error flags (bounded-wait expiry)
-  float2* d_dcin = nullptr;           // [2][gz] (0,0) pencil entering the z pass (fused XY plan)
+  float2* d_dcin = nullptr;           // fused XY plan: [2][gz] (0,0) pencils entering the z pass, [gz] convolved
   // kernel per pass of a double step (PK_*), chosen by the autotuner
   int plan_y = PK_PLAIN, plan_z = PK_PLAIN, plan_x = PK_PLAIN;
   int autotune = 1;
