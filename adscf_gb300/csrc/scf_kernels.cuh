@@ -502,12 +502,23 @@ __global__ void k_solve_b(const ScfDev* __restrict__ Ss, int have_closure, int d
 template <typename T>
 __device__ __forceinline__ void mix_body(const ScfDev& S, T* E, double ds, int bid, int nb) {
   __shared__ double ca[SCF_MAX_SLOTS], cb[SCF_MAX_SLOTS];
+  __shared__ int nzj[SCF_MAX_SLOTS], nnz;
   const int kn = *S.iter;               // already advanced to k+1
   const int nxt = kn % S.slots;
   const int cur = (kn - 1) % S.slots;
   if (threadIdx.x < S.slots) {
     ca[threadIdx.x] = S.coef[threadIdx.x];
     cb[threadIdx.x] = S.coef[S.slots + threadIdx.x];
+  }
+  __syncthreads();
+  // the slots with a nonzero a_j, in increasing j: the sum below skips the
+  // others without a per-point FP64 comparison (GB300's FP64 pipe bounds
+  // this kernel)
+  if (threadIdx.x == 0) {
+    int k = 0;
+    for (int j = 0; j < S.slots; ++j)
+      if (ca[j] != 0.0) nzj[k++] = j;
+    nnz = k;
   }
   __syncthreads();
   const size_t nv = (size_t)S.ntypes * S.npts;
@@ -520,8 +531,10 @@ __device__ __forceinline__ void mix_body(const ScfDev& S, T* E, double ds, int b
       x = S.hx[(size_t)cur * nv + i];
     } else if (use_y) {
       x = 0.0;
-      for (int j = 0; j < S.slots; ++j)
-        if (ca[j] != 0.0) x += ca[j] * S.hy[(size_t)j * nv + i];
+      for (int k = 0; k < nnz; ++k) {
+        const int j = nzj[k];
+        x += ca[j] * S.hy[(size_t)j * nv + i];
+      }
     } else {
       x = 0.0;
       for (int j = 0; j < S.slots; ++j) {
