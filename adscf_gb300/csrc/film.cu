@@ -75,10 +75,10 @@ AdiLaunch adi_launch(const FilmState* F, const FilmDev<T>& D, int chains) {
     return W;
   };
   A.wx = lanes(D.gx, 3, D.gy * (D.gz - 1));
-  A.wy = lanes(D.gy, 3, D.gx * (D.gz - 1));
+  A.wy = lanes(D.gy, 4, D.gx * (D.gz - 1));
   A.wz = lanes(D.gz + 1, 2, D.nlines);
   A.sx = adi_smem(D.gx, A.wx, sizeof(T));
-  A.sy = adi_smem(D.gy, A.wy, sizeof(T));
+  A.sy = adi_smem_y(D.gy, A.wy, sizeof(T));
   A.sz = 2 * (size_t)(D.gz + 1) * A.wz * sizeof(T);
   A.gx = dim3((D.gy * (D.gz - 1) + A.wx - 1) / A.wx, chains);
   A.gy = dim3((D.gx * (D.gz - 1) + A.wy - 1) / A.wy, chains);
@@ -264,7 +264,7 @@ int film_create(adscf_ctx* ctx, const adscf_params* p) {
   if (ctx->geometry == ADSCF_FILM_3D) {
     const size_t es = F->t64 ? sizeof(double) : sizeof(float);
     const int nmax = std::max(ctx->gx, std::max(ctx->gy, gz + 1));
-    if (adi_smem(nmax, 1, es) > (size_t)F->optin) return set_err(ctx, ADSCF_E_ARG, "ADI line too long for shared memory");
+    if (adi_smem_y(nmax, 1, es) > (size_t)F->optin) return set_err(ctx, ADSCF_E_ARG, "ADI line too long for shared memory");
     // shared memory is a per-function limit set in the launching file
     CK(cudaFuncSetAttribute(k_adi_x<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, F->optin));
     CK(cudaFuncSetAttribute(k_adi_y<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, F->optin));

@@ -308,8 +308,14 @@ __device__ __forceinline__ void cyclic_solve(const T a, const T b, const T c, in
 // [point][lane] (blockDim.x = W lanes, conflict-free): the right-hand side
 // is formed there, solved in place, and written out once, so the serial
 // recurrences wait on shared-memory latency instead of on global loads of
-// their own stores.  Shared memory per block: adi_smem(n, W, sizeof(T)).
+// their own stores.  The slices and q* that a sweep only reads go through
+// the non-coherent path (__ldg), and the write-back loops load nothing they
+// store: otherwise the compiler keeps every load behind the previous
+// point's store (it cannot prove them disjoint) and a line's write-back
+// waits on one memory latency per point.  Shared memory per block: adi_smem(n, W, sizeof(T)).
 __host__ __device__ __forceinline__ size_t adi_smem(int n, int W, size_t es) { return 3 * (size_t)n * W * es; }
+// the y sweep also keeps q* of its line (write-back without reloads)
+__host__ __device__ __forceinline__ size_t adi_smem_y(int n, int W, size_t es) { return 4 * (size_t)n * W * es; }
 
 // FP32 sweeps read the FP32 field copy; FP64 sweeps the field
 template <typename T>
@@ -345,10 +351,12 @@ k_adi_x(FilmDev<T> F, FieldRef fr, int s) {
   const size_t row = (size_t)z * L + (size_t)y * gx;
   for (int x = 0; x < gx; ++x) {
     const int xm = (x + gx - 1) % gx, xp = (x + 1) % gx;
-    const T c0 = p0[row + x];
-    const T qxm = p0[row + xm], qxp = p0[row + xp];
-    const T qym = p0[(size_t)z * L + (size_t)ym * gx + x], qyp = p0[(size_t)z * L + (size_t)yp * gx + x];
-    const T qzm = p0[(size_t)(z - 1) * L + (size_t)y * gx + x], qzp = p0[(size_t)(z + 1) * L + (size_t)y * gx + x];
+    const T c0 = __ldg(p0 + row + x);
+    const T qxm = __ldg(p0 + row + xm), qxp = __ldg(p0 + row + xp);
+    const T qym = __ldg(p0 + (size_t)z * L + (size_t)ym * gx + x);
+    const T qyp = __ldg(p0 + (size_t)z * L + (size_t)yp * gx + x);
+    const T qzm = __ldg(p0 + (size_t)(z - 1) * L + (size_t)y * gx + x);
+    const T qzp = __ldg(p0 + (size_t)(z + 1) * L + (size_t)y * gx + x);
     const T dsw = adi_dsw<T>(F, st, w, ty, row + x);
     if constexpr (sizeof(T) == 4)   // increment q* - q (b = -(a + c) on every axis; see cn_rhs)
       r[x * W] = (T)-2 * (ax * (qxm - c0) + cx * (qxp - c0) + ay * (qym - c0) + cy * (qyp - c0) +
@@ -358,7 +366,7 @@ k_adi_x(FilmDev<T> F, FieldRef fr, int s) {
                  ((T)1 - bx - by * (T)2 - bz * (T)2 - dsw) * c0;
   }
   cyclic_solve<T>(ax, (T)1 + bx, cx, gx, r, W, r, W, gs, zs, W, F.err);
-  for (int x = 0; x < gx; ++x) out[row + x] = sizeof(T) == 4 ? p0[row + x] + r[x * W] : r[x * W];
+  for (int x = 0; x < gx; ++x) out[row + x] = sizeof(T) == 4 ? __ldg(p0 + row + x) + r[x * W] : r[x * W];
 }
 
 // y sweep: (1 - ds Dyy/2) q** = q* - ds Dyy q / 2  (:108-119); one thread
@@ -374,6 +382,7 @@ k_adi_y(FilmDev<T> F, int s) {
   T* r = reinterpret_cast<T*>(smraw) + threadIdx.x;
   T* gs = r + (size_t)gy * W;
   T* zs = gs + (size_t)gy * W;
+  T* ws = zs + (size_t)gy * W;      // q* of the line, for the write-back
   const int x = id % gx, z = 1 + id / gx;
   const double ds = film_ds(F.dss, dir, s, F.ns);
   const T* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;
@@ -384,16 +393,18 @@ k_adi_y(FilmDev<T> F, int s) {
     const int ym = (y + gy - 1) % gy, yp = (y + 1) % gy;
     const size_t i = col + (size_t)y * gx, im = col + (size_t)ym * gx, ip = col + (size_t)yp * gx;
     if constexpr (sizeof(T) == 4) {   // increment q** - q* from e = q - q*
-      const T e0 = p0[i] - w1[i];
-      r[y * W] = ay * ((p0[im] - w1[im]) - e0) + cy * ((p0[ip] - w1[ip]) - e0);
+      const T w1i = w1[i];
+      ws[y * W] = w1i;
+      const T e0 = __ldg(p0 + i) - w1i;
+      r[y * W] = ay * ((__ldg(p0 + im) - w1[im]) - e0) + cy * ((__ldg(p0 + ip) - w1[ip]) - e0);
     } else {
-      r[y * W] = ay * p0[im] + w1[i] + by * p0[i] + cy * p0[ip];
+      r[y * W] = ay * __ldg(p0 + im) + w1[i] + by * __ldg(p0 + i) + cy * __ldg(p0 + ip);
     }
   }
   cyclic_solve<T>(ay, (T)1 + by, cy, gy, r, W, r, W, gs, zs, W, F.err);
   for (int y = 0; y < gy; ++y) {
     const size_t i = col + (size_t)y * gx;
-    w1[i] = sizeof(T) == 4 ? w1[i] + r[y * W] : r[y * W];
+    w1[i] = sizeof(T) == 4 ? ws[y * W] + r[y * W] : r[y * W];
   }
 }
 
@@ -419,7 +430,7 @@ k_adi_z(FilmDev<T> F, FieldRef fr, int s) {
   // FP32: increment q' - q** from f = q - q** (q** = 0 on the walls)
   constexpr bool inc = sizeof(T) == 4;
   T bet = (T)1, uprev = (T)0, cprev = (T)0;
-  T f_jm1 = p0[line], f_j = inc && gz > 1 ? p0[(size_t)L + line] - w1[(size_t)L + line] : (T)0;
+  T f_jm1 = __ldg(p0 + line), f_j = inc && gz > 1 ? __ldg(p0 + (size_t)L + line) - __ldg(w1 + (size_t)L + line) : (T)0;
   us[0] = (T)0;
   for (int j = 1; j <= gz; ++j) {
     T a, c, diag, rhs;
@@ -429,12 +440,12 @@ k_adi_z(FilmDev<T> F, FieldRef fr, int s) {
       cn_row<T>(F, st, j, sizeof(T) == 4 ? 0.0 : w[i], sizeof(T) == 4 ? wl[i] : 0.f, a, c, bz, hw);
       diag = (T)1 + bz + hw;
       if constexpr (inc) {
-        const T f_jp1 = j + 1 < gz ? p0[i + L] - w1[i + L] : p0[i + L];
+        const T f_jp1 = j + 1 < gz ? __ldg(p0 + i + L) - __ldg(w1 + i + L) : __ldg(p0 + i + L);
         rhs = a * (f_jm1 - f_j) + c * (f_jp1 - f_j) + hw * f_j;
         f_jm1 = f_j;
         f_j = f_jp1;
       } else {
-        rhs = a * p0[i - L] + w1[i] + (bz + hw) * p0[i] + c * p0[i + L];
+        rhs = a * __ldg(p0 + i - L) + __ldg(w1 + i) + (bz + hw) * __ldg(p0 + i) + c * __ldg(p0 + i + L);
       }
     } else {
       a = (T)0; c = (T)0; diag = (T)1; rhs = (T)0;
@@ -447,7 +458,7 @@ k_adi_z(FilmDev<T> F, FieldRef fr, int s) {
   for (int j = gz - 1; j >= 0; --j) {
     const size_t i = (size_t)j * L + line;
     const T u = us[j * W] - gs[(j + 1) * W] * unext;
-    qn[i] = inc && j > 0 ? w1[i] + u : u;
+    qn[i] = inc && j > 0 ? __ldg(w1 + i) + u : u;
     unext = u;
   }
 }
