@@ -187,6 +187,7 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       tmak::tma_load_3d(buf + (size_t)s * LY::tile_elems + b * LY::box_elems, &tmap, &bar[s], cx, cy, cz);
     }
   };
+  // loads issued / completed per stage (thread 0), to drain on an early exit
   int issued[2] = {0, 0}, done[2] = {0, 0};
   tmak::pdl_launch_dependents();
   // the first tile's load is issued as soon as the previous pass is complete;
