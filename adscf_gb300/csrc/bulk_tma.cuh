@@ -450,13 +450,20 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       const size_t rbase = pbase + (size_t)j * N;
       float2 v[R1];
       if (!init) {
+        // the Boltzmann factors of the first half of the row's points are
+        // loaded before its inverse x transform, so their latency overlaps
+        // it (all sixteen would leave too few registers for the transform)
+        constexpr int HP = R1 / 2;
+        EPt<float> epre[HP];
+#pragma unroll
+        for (int m = 0; m < HP; ++m) epre[m] = load_ept(I.E, rbase + F::in_index(lt, m));
 #pragma unroll
         for (int r = 0; r < R1; ++r) v[r] = plane[tmak::plane_at<N>(j, F::out_index(lt, r))];
         F::inverse(v, sc, tw, lt);
 #pragma unroll
         for (int m = 0; m < R1; ++m) {
           const size_t g = rbase + F::in_index(lt, m);
-          const EPt<float> ev = load_ept(I.E, g);
+          const EPt<float> ev = m < HP ? epre[m % HP] : load_ept(I.E, g);
           const float2 q = make_float2(emul(v[m].x, fA ? ev.a : ev.b, fA ? ev.al : ev.bl),
                                        emul(v[m].y, bA ? ev.a : ev.b, bA ? ev.al : ev.bl));
           sl[g] = q;
