@@ -242,8 +242,11 @@ __device__ __forceinline__ void closure_body(const ScfDev& S, int flags, int bid
 
 // one kernel per slot capacity (3: lambda/simple or m <= 2, 11: m <= 10,
 // SCF_MAX_SLOTS), so the partial sums held per thread fit the history
+// Up to 11 slots the closure is held to 64 registers, so the 4 x 152 blocks
+// of a bulk context run as one wave (at 80 registers, three blocks per SM
+// left a second wave of a third of the blocks).
 template <int NS>
-__global__ void __launch_bounds__(SCF_THREADS)
+__global__ void __launch_bounds__(SCF_THREADS, NS <= 11 ? 4 : 3)
 k_closure(ScfDev S, int flags) { closure_body<NS>(S, flags, blockIdx.x, gridDim.x); }
 
 template <int NS>
