@@ -159,8 +159,9 @@ __device__ __forceinline__ void ff_add(float& ah, float& al, float bh, float bl)
 // CTA's extra work in its pass, so its serial chain sets that CTA's finish:
 // eight interleaved partial sums per output (chain u = d mod 8, each in
 // increasing d) shorten the dependent chain eightfold, and are combined
-// pairwise: ((0+1) + (2+3)) + ((4+5) + (6+7)).  The fused XY pass evaluates
-// the same sums with one lane per chain (dc_point) and gets the same bits.
+// pairwise: ((0+1) + (2+3)) + ((4+5) + (6+7)).  In the fused plan the z
+// pass's light CTAs evaluate the same sums with one lane per chain
+// (dc_point) and get the same bits.
 constexpr int kDcChains = 8;
 __device__ __forceinline__ void dc_pencil_apply(int n, DcPencil D) {
   for (int z = threadIdx.x; z < n; z += blockDim.x) {
