@@ -103,6 +103,7 @@ SIGNATURES = {
     "adscf_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "adscf_enqueue": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "adscf_stage_launches": (C.c_int, [C.c_void_p, C.c_int]),
+    "adscf_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int]),
     "adscf_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
     "adscf_set_pass_plan": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "adscf_forward": (C.c_int, [C.c_void_p, _dp, _dp]),

@@ -335,6 +335,7 @@ int create_t(adscf_ctx* ctx) {
     if (rc) return rc;
   }
 
+  I.wait_polls = tmak::kWaitPolls;
   CK(cudaMalloc(&ctx->d_inst, sizeof(BulkDev<T>)));
   CK(cudaMemcpy(ctx->d_inst, &I, sizeof(I), cudaMemcpyHostToDevice));
   hb<T>(ctx) = I;
@@ -785,6 +786,18 @@ int bulk_hold_slices(adscf_ctx* ctx, bool full) {
   // captured graphs replay the full chains: capture again on next use
   if (ctx->g_iter) { cudaGraphExecDestroy(ctx->g_iter); ctx->g_iter = nullptr; }
   if (ctx->g_prop) { cudaGraphExecDestroy(ctx->g_prop); ctx->g_prop = nullptr; }
+  return ADSCF_OK;
+}
+// bound of the TMA passes' pipeline waits (0: every wait gives up at once)
+int bulk_set_wait_polls(adscf_ctx* ctx, int polls) {
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->prec == ADSCF_SPLIT) {
+    ctx->hb32.wait_polls = polls;
+    CK(cudaMemcpy(ctx->d_inst, &ctx->hb32, sizeof(ctx->hb32), cudaMemcpyHostToDevice));
+  } else {
+    ctx->hb64.wait_polls = polls;
+    CK(cudaMemcpy(ctx->d_inst, &ctx->hb64, sizeof(ctx->hb64), cudaMemcpyHostToDevice));
+  }
   return ADSCF_OK;
 }
 int bulk_enqueue_expfield(adscf_ctx* ctx, const double* d_w) {

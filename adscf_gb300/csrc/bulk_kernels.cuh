@@ -49,6 +49,7 @@ struct BulkDev {
   double* dist;              // [2][npts] contour integrals (block A, block B)
   double* qpart;             // [gridDim] partial sums of q_N
   double ds;                 // contour step
+  int wait_polls;            // polls of one pipeline mbarrier wait of the TMA passes
 };
 
 // X-pass modes (XM_FROM: start a chain segment at node t from a stored

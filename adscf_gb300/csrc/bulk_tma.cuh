@@ -122,7 +122,9 @@ __device__ __forceinline__ float2 dc_point(const float2* in, const float2* c, in
 }
 
 constexpr int kBoxCols = 16;           // 16 x 8 B = 128 B inner box
-constexpr int kWaitPolls = 1 << 22;    // bound of one mbarrier wait
+// default bound of one pipeline mbarrier wait (BulkDev::wait_polls, settable
+// per context) and the fixed bound of the drain waits at kernel exit
+constexpr int kWaitPolls = 1 << 22;
 
 template <int N>
 struct TmaLayout {
@@ -247,7 +249,7 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       issue_load(nxt, s ^ 1);
       ++issued[s ^ 1];
     }
-    const bool got = tmak::mbar_wait_bounded(&bar[s], (it >> 1) & 1, tmak::kWaitPolls);
+    const bool got = tmak::mbar_wait_bounded(&bar[s], (it >> 1) & 1, I.wait_polls);
     if (!__syncthreads_and(got)) {
       if (threadIdx.x == 0) atomicOr(err, 2);
       break;
@@ -418,7 +420,7 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       // so a warp barrier orders the write.
       float2 dco = make_float2(0.f, 0.f);
       if (dcout && threadIdx.x == 0) dco = dcout[z];
-      const bool got = tmak::mbar_wait_bounded(bar, (uint32_t)(it & 1), tmak::kWaitPolls);
+      const bool got = tmak::mbar_wait_bounded(bar, (uint32_t)(it & 1), I.wait_polls);
       if (!__syncthreads_and(got)) {
         if (threadIdx.x == 0) atomicOr(err, 8);
         break;

@@ -653,6 +653,12 @@ int adscf_set_stream(adscf_ctx* ctx, void* stream) {
   return ADSCF_OK;
 }
 
+int adscf_set_wait_limit(adscf_ctx* ctx, int polls) {
+  if (!ctx) return ADSCF_E_ARG;
+  if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "bulk contexts only");
+  return bulk_set_wait_polls(ctx, polls < 0 ? (1 << 22) : polls);
+}
+
 int adscf_set_box(adscf_ctx* ctx, double sizex, double sizey, double sizez) {
   if (!ctx || !(sizex > 0 && sizey > 0 && sizez > 0)) return ADSCF_E_ARG;
   if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "box updates are for bulk contexts");

@@ -127,7 +127,8 @@ int bulk_r2c(adscf_ctx* ctx, const double* d_prop, double* h_half);
 int bulk_c2r(adscf_ctx* ctx, const double* h_half, double* d_prop);
 int bulk_mix_e(adscf_ctx* ctx);                 // k_mix with E update
 int bulk_set_box(adscf_ctx* ctx);               // k-space tables for new side lengths
-int bulk_hold_slices(adscf_ctx* ctx, bool full);   // all Ns + 1 slices, or two of scratch (FP64)
+int bulk_hold_slices(adscf_ctx* ctx, bool full);
+int bulk_set_wait_polls(adscf_ctx* ctx, int polls);  // pipeline wait bound of the TMA passes   // all Ns + 1 slices, or two of scratch (FP64)
 void adj_set_box(adscf_ctx* ctx);               // adjoint's copy of the side lengths
 // adjoint (adjoint.cu)
 void adj_destroy(adscf_ctx* ctx);

@@ -9,22 +9,31 @@
 // tables, work lists, spectrum) from one file-scope static device array of
 // fixed size.
 //
-// The array is a property of the loaded library: every GPU that loads it
-// holds ADSCF_NOALLOC_SCRATCH_BYTES of device memory until the process
-// exits.  All calls on one device share it and it keeps the last call's
-// contents, so two calls whose kernels overlap on the GPU (different streams
-// without ordering, or different host threads) race and corrupt each other.
-// Calls must be ordered on the device, e.g. issued to one stream.
+// The array belongs to the loaded library: it is reserved on a device when
+// the library's device code is loaded there -- with CUDA's default lazy
+// module loading, at the first call on that device -- and held until the
+// process exits.  A caller on a tightly budgeted GPU should therefore make
+// one call during its set-up (or run with CUDA_MODULE_LOADING=EAGER); when
+// the reservation fails the call returns ADSCF_E_OOM.  All calls on one
+// device share the array and it keeps the last call's contents, so two calls
+// whose kernels overlap on the GPU (different streams without ordering, or
+// different host threads) race and corrupt each other.  Calls must be
+// ordered on the device, e.g. issued to one stream.
 //
-// Set-up: the first call on each device takes the array's device address
-// with cudaGetSymbolAddress (with that device current) and raises the
-// shared-memory limit of the FFT kernels; make that first call before any
-// stream capture.
+// Set-up and table rebuilds: the first call on each device takes the array's
+// device address with cudaGetSymbolAddress (with that device current) and
+// raises the shared-memory limit of the FFT kernels; a call with a new grid,
+// box or ds rewrites the plan, tables and work lists in the array and
+// synchronises its stream.  Both return ADSCF_E_STATE instead when the
+// stream is capturing, so make the first call, and every call with new
+// parameters, before any stream capture.  A rewrite replaces the tables that
+// work enqueued or recorded earlier will read when it runs.
 #include <cmath>
 #include <cstring>
 #include <mutex>
 
 #include "internal.h"
+#include "bulk_host.h"
 
 // sizes the static scratch is laid out for
 #define NOALLOC_MAX_POINTS 262144   // e.g. 64^3
@@ -44,6 +53,10 @@ constexpr size_t kOffTw = kOffWork + kWorkBytes;
 constexpr size_t kOffFk = kOffTw + kTwBytes;
 constexpr size_t kOffSpec = ((kOffFk + kFkBytes + 255) / 256) * 256;
 constexpr size_t kTotal = kOffSpec + kSpecBytes;
+// the instance header sits in front of the work lists
+static_assert(sizeof(BulkDev<double>) <= kInstBytes, "BulkDev<double> outgrew its scratch slot");
+static_assert(kInstBytes % alignof(int2) == 0 && kInstBytes % alignof(BulkDev<double>) == 0,
+              "work lists and header must stay aligned");
 
 }  // namespace
 
@@ -73,40 +86,6 @@ double2 h_tw[3 * NOALLOC_MAX_LINE];
 double h_fk[2 * (size_t)NOALLOC_MAX_PLANE + 2 * NOALLOC_MAX_LINE];
 int2 h_work[3 * (size_t)NOALLOC_MAX_TILES];
 
-int pow2_floor_na(int v) {
-  int p = 1;
-  while (p * 2 <= v) p *= 2;
-  return p;
-}
-
-bool plan_na(int n, Plan1D& P) {
-  std::memset(&P, 0, sizeof(P));
-  P.n = n;
-  int m = n;
-  while (m % 8 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 8; m /= 8; }
-  while (m % 4 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 4; m /= 4; }
-  while (m % 2 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 2; m /= 2; }
-  while (m % 3 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 3; m /= 3; }
-  while (m % 5 == 0 && P.nst < ADSCF_MAX_STAGES) { P.rad[P.nst++] = 5; m /= 5; }
-  if (m != 1) return false;
-  int tpl = pow2_floor_na(n / 8 > 0 ? n / 8 : 1);
-  if (tpl > 64) tpl = 64;
-  P.tpl = tpl;
-  P.lpc = BULK_THREADS / tpl;
-  P.ld = n + 1;
-  return true;
-}
-
-double wavenum_na(int i, int n, double L) {
-  const double m = (i > n / 2) ? double(i - n) : double(i);
-  return 2.0 * M_PI * m / L;
-}
-
-size_t smem_na(const Plan1D& P) {
-  const size_t twn = (P.n + 1) & ~1;
-  return (twn + 2 * (size_t)P.lpc * P.ld) * sizeof(double2);
-}
-
 // (re)build plan, tables and work lists inside the scratch for this problem
 int build_tables(DevState& D, int gx, int gy, int gz, double lx, double ly, double lz,
                  double ds, cudaStream_t s) {
@@ -114,7 +93,7 @@ int build_tables(DevState& D, int gx, int gy, int gz, double lx, double ly, doub
   I.gx = gx; I.gy = gy; I.gz = gz;
   I.npts = gx * gy * gz;
   I.ns = 0; I.na = 0; I.nb = 0;
-  if (!plan_na(gx, I.px) || !plan_na(gy, I.py) || !plan_na(gz, I.pz)) return ADSCF_E_ARG;
+  if (!bulkhost::make_plan(gx, I.px) || !bulkhost::make_plan(gy, I.py) || !bulkhost::make_plan(gz, I.pz)) return ADSCF_E_ARG;
   const int ns3[3] = {gx, gy, gz};
   int offs[3];
   int ntw = 0;
@@ -133,15 +112,15 @@ int build_tables(DevState& D, int gx, int gy, int gz, double lx, double ly, doub
   I.gxy_off = 0;
   I.gz_off = 2 * nxy;
   for (int y = 0; y < gy; ++y) {
-    const double ky = wavenum_na(y, gy, ly);
+    const double ky = bulkhost::wavenum(y, gy, ly);
     for (int x = 0; x < gx; ++x) {
-      const double kx = wavenum_na(x, gx, lx);
+      const double kx = bulkhost::wavenum(x, gx, lx);
       fk[(size_t)y * gx + x] = std::exp(-ds * kx * kx) * std::exp(-ds * ky * ky);
     }
   }
   const double invn = 1.0 / ((double)gx * gy * gz);
   for (int z = 0; z < gz; ++z) {
-    const double kz = wavenum_na(z, gz, lz);
+    const double kz = bulkhost::wavenum(z, gz, lz);
     fk[I.gz_off + z] = std::exp(-ds * kz * kz) * invn;
   }
   I.tw64_off = 0;
@@ -165,7 +144,9 @@ int build_tables(DevState& D, int gx, int gy, int gz, double lx, double ly, doub
     return ADSCF_E_CUDA;
   D.gx = gx; D.gy = gy; D.gz = gz; D.lx = lx; D.ly = ly; D.lz = lz; D.ds = ds;
   D.nwx = nwx; D.nwy = nwy; D.nwz = nwz;
-  D.smx = smem_na(I.px); D.smy = smem_na(I.py); D.smz = smem_na(I.pz);
+  D.smx = bulkhost::plan_smem<double>(I.px);
+  D.smy = bulkhost::plan_smem<double>(I.py);
+  D.smz = bulkhost::plan_smem<double>(I.pz);
   return ADSCF_OK;
 }
 
@@ -185,16 +166,29 @@ extern "C" int adscf_propagate_step_noalloc(int gx, int gy, int gz, double sizex
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   std::lock_guard<std::mutex> lock(g_mu);
   DevState& D = g_dev[dev];
+  const bool rebuild = D.gx != gx || D.gy != gy || D.gz != gz || D.lx != sizex ||
+                       D.ly != sizey || D.lz != sizez || D.ds != ds;
+  if (!D.ready || rebuild) {
+    // set-up and table rebuilds synchronise the stream: not while it captures
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return ADSCF_E_CUDA;
+    if (cs != cudaStreamCaptureStatusNone) return ADSCF_E_STATE;
+  }
   if (!D.ready) {
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return ADSCF_E_CUDA;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      return ADSCF_E_OOM;   // the array could not be reserved on this device
+    }
+    if (e != cudaSuccess || !p) return ADSCF_E_CUDA;
     D.base = static_cast<unsigned char*>(p);
     if (cudaFuncSetAttribute(k_bulk_xpass<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess ||
         cudaFuncSetAttribute(k_bulk_strided<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess)
       return ADSCF_E_CUDA;
     D.ready = true;
   }
-  if (D.gx != gx || D.gy != gy || D.gz != gz || D.lx != sizex || D.ly != sizey || D.lz != sizez || D.ds != ds) {
+  if (rebuild) {
     D.gx = 0;  // tables invalid until rebuilt
     const int rc = build_tables(D, gx, gy, gz, sizex, sizey, sizez, ds, s);
     if (rc) return rc;

@@ -232,6 +232,10 @@ class Context:
         self._ck(self.lib.adscf_tuning(self.h, buf, len(buf)))
         return buf.value.decode()
 
+    def set_wait_limit(self, polls):
+        """Pipeline-wait bound of the TMA passes (polls; < 0 restores the default)."""
+        self._ck(self.lib.adscf_set_wait_limit(self.h, int(polls)))
+
     def set_pass_plan(self, y, z, x):
         """Pin the kernel of the Y, Z and X passes (0 plain, 1 persistent, 2 TMA)."""
         self._ck(self.lib.adscf_set_pass_plan(self.h, int(y), int(z), int(x)))

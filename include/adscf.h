@@ -226,6 +226,14 @@ enum { ADSCF_STAGE_ITERATION = 0, ADSCF_STAGE_PROPAGATE = 1,
 ADSCF_API int adscf_enqueue(adscf_ctx *ctx, int stage, int repeats);
 /* kernel launches one run of a stage makes (for launch accounting) */
 ADSCF_API int adscf_stage_launches(const adscf_ctx *ctx, int stage);
+/* Bound of one pipeline wait of the TMA-fed bulk passes, in polls of its
+ * mbarrier (default 2^22, restored by polls < 0; 0 makes every wait give up
+ * at once).  A wait that runs out sets a device flag; the kernel drains its
+ * copies in flight and returns, and the next result-reading call returns
+ * ADSCF_E_TIMEOUT.  No reference counterpart (failure detection of the
+ * device pipeline; the reference's only failure stops are the tridiagonal
+ * pivot and the non-finite accuracy checks).                              */
+ADSCF_API int adscf_set_wait_limit(adscf_ctx *ctx, int polls);
 
 /* ---- pass-kernel autotuner (bulk) ----------------------------------------
  * No reference counterpart.  At context creation every available kernel for
@@ -366,17 +374,22 @@ ADSCF_API int adscf_batch_backward(adscf_batch *b, double *grad);
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (a pre-partitioned or quota-limited GPU, a driver that owns every
  * device buffer, code paths where cudaMalloc's implicit synchronisation is
- * not allowed): one FP64 bulk Propagate_Step, prop <- E IFFT(exp(-k^2 ds)
- * FFT(E prop)) with E = expfield (mod_propagate.f90:40-68), on caller-owned
- * device buffers d_prop [gz][gy][gx] (in/out) and d_expfield, enqueued on
- * `stream` (cudaStream_t as void*).  It calls no allocator: plan, tables and
- * spectrum live in one file-scope static device array of about 6.6 MB that
- * every GPU loading the library holds until exit.  Limits: gx*gy*gz <=
- * 262144, each axis <= 512 and a product of 2, 3 and 5, gx*gy <= 65536;
- * larger problems return ADSCF_E_TOO_LARGE.  The first call on a device
- * sets the array up (cudaGetSymbolAddress, kernel attributes): make it
- * before any stream capture.  All calls share the array, so calls whose
- * kernels overlap on the GPU race; order them on one stream.               */
+ * not allowed): one FP64 bulk propagator step, prop <- E IFFT(exp(-k^2 ds)
+ * FFT(E prop)) with E = expfield, on caller-owned device buffers d_prop
+ * [gz][gy][gx] (in/out) and d_expfield, enqueued on `stream` (cudaStream_t
+ * as void*).  It calls no allocator: plan, tables and spectrum live in one
+ * file-scope static device array of about 6.6 MB, reserved on a device when
+ * the library's device code loads there (under CUDA's default lazy loading,
+ * at the first call on that device; ADSCF_E_OOM if that fails) and held
+ * until exit.  Limits: gx*gy*gz <= 262144, each axis <= 512 and a product of
+ * 2, 3 and 5, gx*gy <= 65536; larger problems return ADSCF_E_TOO_LARGE.  The
+ * first call on a device sets the array up (cudaGetSymbolAddress, kernel
+ * attributes), and a call with a new grid, box or ds rebuilds the tables in
+ * the array with a stream synchronisation; both return ADSCF_E_STATE while
+ * the stream is capturing, so make them before any stream capture.  All
+ * calls share the array: calls whose kernels overlap on the GPU race, and a
+ * rebuild replaces the tables that earlier enqueued or recorded work reads.
+ * Order the calls on one stream.                                           */
 ADSCF_API int adscf_propagate_step_noalloc(int gx, int gy, int gz, double sizex,
                                            double sizey, double sizez, double ds,
                                            double *d_prop, const double *d_expfield,

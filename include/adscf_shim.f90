@@ -1,0 +1,363 @@
+! adscf_shim.f90 -- drop-in replacements for ADSCF's compute modules.
+!
+! Each module below has the name, public types and procedure signatures of
+! the reference module it replaces, so the reference's Main_* programs
+! compile unchanged against it; the bodies call the GB300 library through
+! the `adscf` binding module (adscf.f90).  Build: list this file (after
+! mod_global.f90 and adscf.f90) in place of the replaced source files and
+! link -ladscf_gb300.
+!
+!   replaced file (Bulk_3D_FFT)                      module here
+!   General_Routines/mod_propagate.f90               Propagate
+!   Polymer_Modules/mod_diblock.f90                  Molecule_Diblock_Copolymer
+!   General_Routines/mod_iterate.f90 (Mixing_*)      Iterate
+!   Film_CK_AD/Film_3D/Geometry_Modules/mod_realspace.f90
+!     Propagate_Step, integrator                     RealSpace_adscf (used
+!     beside RealSpace, whose generate_mesh and calculate_Volume stay)
+!
+! Every module shares one library context per geometry (adscf_shim_state),
+! created on first use from the Global module's grid, box and ds.  A
+! non-zero library status prints the library's message and stops, as the
+! reference's routines do on their own errors.
+module adscf_shim_state
+  use iso_c_binding
+  use adscf
+  use Global
+  implicit none
+  private
+  type(c_ptr), save :: bulk_ctx = c_null_ptr    ! propagation (Propagate, Molecule_*)
+  type(c_ptr), save :: mix_ctx = c_null_ptr     ! mixing (Iterate)
+  type(c_ptr), save :: film_ctx = c_null_ptr    ! film steps and integrator
+  ! the chain the bulk context was created for
+  real(c_double), save :: cur_len(2) = -1d0, cur_rho = -1d0, cur_mu = 0d0
+  integer(c_int), save :: cur_types(2) = -1, cur_ens = -1
+  integer, save :: cur_mix = -1
+  real(c_double), save :: cur_lam = -1d0
+  public :: shim_bulk_context, shim_mix_context, shim_film_context
+contains
+
+  subroutine base_params(p)
+    type(adscf_params), intent(out) :: p
+    p%geometry = ADSCF_BULK
+    p%gx = gridx; p%gy = gridy; p%gz = gridz
+    p%sizex = sizex; p%sizey = sizey; p%sizez = sizez
+    p%ds = ds
+    p%dss = c_null_ptr; p%ns = 0; p%n_a = 0
+    p%block_length = [0.5d0, 0.5d0]
+    p%ensemble = 1
+    p%rho = 1d0; p%mu = 0d0
+    p%kappa = 0d0; p%chi = 0d0
+    p%monomer_volume = [1d0, 1d0]
+    p%precision = ADSCF_FP64
+    p%mixing_type = ADSCF_MIX_LAMBDA
+    p%mixing_dim = 2
+    p%lambda = 0.1d0
+    p%lam_warm = 1d-3
+    p%warm_iters = 2
+    p%dz = c_null_ptr
+    p%int_scheme = 1; p%int_span = 0
+    p%ext_potential = c_null_ptr
+    p%ww = 0d0
+    p%graft = c_null_ptr
+    p%nblocks = 0
+    p%blocks = c_null_ptr
+    p%block_types = c_null_ptr
+  end subroutine base_params
+
+  ! bulk context for a two-block chain of the given block lengths, monomer
+  ! types (1-based, as the reference's monomer_type) and ensemble; made
+  ! again when the chain changes
+  function shim_bulk_context(block_length, monomer_type, ensemble, rho, mu) result(ctx)
+    real(c_double), intent(in) :: block_length(2), rho, mu
+    integer, intent(in) :: monomer_type(2), ensemble
+    type(c_ptr) :: ctx
+    type(adscf_params) :: p
+    real(c_double), target, save :: blocks(2)
+    integer(c_int), target, save :: types(2)
+    integer(c_int) :: rc
+    if (c_associated(bulk_ctx)) then
+      if (all(cur_len == block_length) .and. all(cur_types == monomer_type) .and. &
+          cur_ens == ensemble .and. cur_rho == rho .and. cur_mu == mu) then
+        ctx = bulk_ctx
+        return
+      end if
+      rc = adscf_ctx_destroy(bulk_ctx)
+      bulk_ctx = c_null_ptr
+    end if
+    call base_params(p)
+    blocks = block_length
+    types = monomer_type - 1
+    p%nblocks = 2
+    p%blocks = c_loc(blocks)
+    p%block_types = c_loc(types)
+    p%block_length = block_length
+    p%ensemble = ensemble
+    p%rho = rho; p%mu = mu
+    rc = adscf_ctx_create(p, bulk_ctx)
+    call adscf_check(bulk_ctx, rc, 'adscf_ctx_create (bulk)')
+    cur_len = block_length; cur_types = monomer_type
+    cur_ens = ensemble; cur_rho = rho; cur_mu = mu
+    ctx = bulk_ctx
+  end function shim_bulk_context
+
+  ! bulk context that holds the mixing history of one mixing scheme
+  function shim_mix_context(mixing_type, lambda) result(ctx)
+    integer, intent(in) :: mixing_type
+    real(c_double), intent(in) :: lambda
+    type(c_ptr) :: ctx
+    type(adscf_params) :: p
+    integer(c_int) :: rc
+    if (c_associated(mix_ctx)) then
+      if (cur_mix == mixing_type .and. cur_lam == lambda) then
+        ctx = mix_ctx
+        return
+      end if
+      rc = adscf_ctx_destroy(mix_ctx)
+      mix_ctx = c_null_ptr
+    end if
+    call base_params(p)
+    p%ds = 0.5d0            ! two contour steps: the context only mixes
+    p%mixing_type = mixing_type
+    p%lambda = lambda
+    rc = adscf_ctx_create(p, mix_ctx)
+    call adscf_check(mix_ctx, rc, 'adscf_ctx_create (mixing)')
+    cur_mix = mixing_type; cur_lam = lambda
+    ctx = mix_ctx
+  end function shim_mix_context
+
+  ! Film_3D context on the Global mesh dz(0:gridz)
+  function shim_film_context(zmesh, scheme) result(ctx)
+    real(c_double), intent(in) :: zmesh(0:)
+    integer, intent(in) :: scheme
+    type(c_ptr) :: ctx
+    type(adscf_params) :: p
+    real(c_double), allocatable, target, save :: dzc(:)
+    integer(c_int) :: rc
+    if (c_associated(film_ctx)) then
+      ctx = film_ctx
+      return
+    end if
+    call base_params(p)
+    allocate(dzc(0:size(zmesh) - 1))
+    dzc = zmesh
+    p%geometry = ADSCF_FILM_3D
+    p%dz = c_loc(dzc)
+    p%int_scheme = scheme
+    p%int_span = 0
+    rc = adscf_ctx_create(p, film_ctx)
+    call adscf_check(film_ctx, rc, 'adscf_ctx_create (film)')
+    ctx = film_ctx
+  end function shim_film_context
+
+end module adscf_shim_state
+
+! ---------------------------------------------------------------------------
+! Propagate (Bulk_3D_FFT/General_Routines/mod_propagate.f90:22-68)
+module Propagate
+  use iso_c_binding
+  use adscf
+  use adscf_shim_state
+  use Global
+  implicit none
+contains
+
+  ! expfield = exp(-ds w / 2), on the host as in the reference (:22-32)
+  subroutine Calculate_Expfield(field, expfield)
+    double precision, dimension(gridx, gridy, gridz, monomer_types), intent(in) :: field
+    double precision, dimension(gridx, gridy, gridz, monomer_types), intent(out) :: expfield
+    expfield = exp(-0.5d0 * ds * field)
+  end subroutine Calculate_Expfield
+
+  ! prop <- E IFFT(exp(-ds k^2) FFT(E prop)) on the GPU (:40-68)
+  subroutine Propagate_Step(prop, expfield)
+    double precision, dimension(gridx, gridy, gridz), intent(in) :: expfield
+    double precision, dimension(gridx, gridy, gridz), intent(inout) :: prop
+    type(c_ptr) :: ctx
+    integer(c_int) :: rc
+    ctx = shim_bulk_context([0.5d0, 0.5d0], [1, 2], 1, 1d0, 0d0)
+    rc = adscf_propagate_step(ctx, prop, expfield, 0d0)
+    call adscf_check(ctx, rc, 'Propagate_Step')
+  end subroutine Propagate_Step
+
+end module Propagate
+
+! ---------------------------------------------------------------------------
+! Molecule_Diblock_Copolymer (Bulk_3D_FFT/Polymer_Modules/mod_diblock.f90)
+module Molecule_Diblock_Copolymer
+  use iso_c_binding
+  use adscf
+  use adscf_shim_state
+  use Global
+  implicit none
+  private
+  integer, parameter :: block_number = 2
+
+  ! same members as the reference's type (mod_diblock.f90:19-33)
+  type diblock_copolymer
+    integer :: label
+    integer, dimension(block_number) :: monomer_type
+    double precision, dimension(block_number) :: block_length
+    integer :: ensemble
+    double precision :: rho
+    double precision :: mu
+    double precision :: energy
+    integer, dimension(block_number) :: block_segments
+    integer :: segments
+    double precision :: Qsum
+    double precision, dimension(gridx, gridy, gridz, block_number) :: distribution
+    double precision, dimension(gridx, gridy, gridz, block_number) :: density
+  end type diblock_copolymer
+
+  public :: diblock_copolymer, Initialize_Diblock, Propagate_Diblock
+contains
+
+  ! chain set-up with the reference's semantics (mod_diblock.f90:46-88):
+  ! nint(f/ds) segments per block and the flat initial block densities
+  subroutine Initialize_Diblock(copolymer, label, monomer_type, block_length, ensemble, rho, mu)
+    integer, intent(in) :: label, ensemble
+    double precision, intent(in) :: rho, mu
+    double precision, dimension(block_number), intent(in) :: block_length
+    integer, dimension(block_number), intent(in) :: monomer_type
+    type(diblock_copolymer), intent(out) :: copolymer
+    integer :: b
+    if (ensemble /= 1 .and. ensemble /= 2) print *, 'Invalid Ensemble'
+    copolymer%label = label
+    copolymer%monomer_type = monomer_type
+    copolymer%block_length = block_length
+    copolymer%ensemble = ensemble
+    copolymer%rho = rho
+    copolymer%mu = mu
+    copolymer%block_segments = nint(block_length / ds)
+    copolymer%segments = sum(copolymer%block_segments)
+    copolymer%energy = 0d0
+    copolymer%Qsum = 0d0
+    copolymer%distribution = 0d0
+    do b = 1, block_number
+      copolymer%density(:, :, :, b) = rho * copolymer%block_segments(b) * ds * volume / dvol &
+                                      / dble(gridx * gridy * gridz)
+    end do
+  end subroutine Initialize_Diblock
+
+  ! both chains, Q, the block densities and the ensemble closure on the GPU
+  ! (mod_diblock.f90:100-173).  The library takes the field w, recovered
+  ! here from expfield = exp(-ds w / 2) (relative error ~1e-15).
+  subroutine Propagate_Diblock(copolymer, expfield)
+    type(diblock_copolymer), intent(inout) :: copolymer
+    double precision, dimension(gridx, gridy, gridz, monomer_types), intent(in) :: expfield
+    double precision, dimension(gridx, gridy, gridz, monomer_types) :: field, dens
+    type(adscf_chain_result) :: res
+    type(c_ptr) :: ctx
+    integer(c_int) :: rc
+    integer :: b
+    if (copolymer%monomer_type(1) == copolymer%monomer_type(2)) then
+      print *, 'Propagate_Diblock: the blocks must have distinct monomer types'
+      stop 1
+    end if
+    field = -2d0 * log(expfield) / ds
+    ctx = shim_bulk_context(copolymer%block_length, copolymer%monomer_type, &
+                            copolymer%ensemble, copolymer%rho, copolymer%mu)
+    rc = adscf_propagate_diblock(ctx, field, dens, res)
+    call adscf_check(ctx, rc, 'Propagate_Diblock')
+    do b = 1, block_number
+      copolymer%density(:, :, :, b) = dens(:, :, :, copolymer%monomer_type(b))
+    end do
+    copolymer%Qsum = res%Qsum
+    copolymer%mu = res%mu
+    copolymer%rho = res%rho
+    copolymer%energy = res%energy
+    if (copolymer%ensemble == 1) then
+      copolymer%distribution = copolymer%density * copolymer%Qsum / (copolymer%rho * volume)
+    else
+      copolymer%distribution = copolymer%density * exp(-copolymer%mu)
+    end if
+  end subroutine Propagate_Diblock
+
+end module Molecule_Diblock_Copolymer
+
+! ---------------------------------------------------------------------------
+! Iterate (Bulk_3D_FFT/General_Routines/mod_iterate.f90:13,27-150): the
+! mixing history lives on the GPU, so only column 0 of field/dfield is read
+! (x_k, r_k) and column 0 of field receives x_{k+1}.
+module Iterate
+  use iso_c_binding
+  use adscf
+  use adscf_shim_state
+  use Global
+  implicit none
+  integer, parameter :: mixing_dim = 2
+contains
+
+  subroutine mix_on_device(mixing_type, field, dfield, fieldsize, lambda, iter)
+    integer, intent(in) :: mixing_type, fieldsize, iter
+    double precision, intent(in) :: lambda
+    double precision, dimension(fieldsize, 0:mixing_dim), intent(inout) :: field, dfield
+    double precision, dimension(fieldsize) :: x
+    type(c_ptr) :: ctx
+    integer(c_int) :: rc
+    if (fieldsize /= 2 * gridx * gridy * gridz) then
+      print *, 'Mixing: fieldsize must be 2*gridx*gridy*gridz'
+      stop 1
+    end if
+    ctx = shim_mix_context(mixing_type, lambda)
+    x = field(:, 0)
+    rc = adscf_mix(ctx, x, dfield(:, 0), iter)
+    call adscf_check(ctx, rc, 'Mixing')
+    field(:, 0) = x
+  end subroutine mix_on_device
+
+  subroutine Mixing_Simple(field, dfield, fieldsize, lambda, iter)
+    double precision, intent(in) :: lambda
+    integer, intent(in) :: fieldsize, iter
+    double precision, dimension(fieldsize, 0:mixing_dim), intent(inout) :: field, dfield
+    call mix_on_device(ADSCF_MIX_SIMPLE, field, dfield, fieldsize, lambda, iter)
+  end subroutine Mixing_Simple
+
+  subroutine Mixing_Lambda(field, dfield, fieldsize, lambda, iter)
+    double precision, intent(in) :: lambda
+    integer, intent(in) :: fieldsize, iter
+    double precision, dimension(fieldsize, 0:mixing_dim), intent(inout) :: field, dfield
+    call mix_on_device(ADSCF_MIX_LAMBDA, field, dfield, fieldsize, lambda, iter)
+  end subroutine Mixing_Lambda
+
+  subroutine Mixing_Anderson(field, dfield, fieldsize, lam_mix, iter)
+    double precision, intent(in) :: lam_mix
+    integer, intent(in) :: fieldsize, iter
+    double precision, dimension(fieldsize, 0:mixing_dim), intent(inout) :: field, dfield
+    call mix_on_device(ADSCF_MIX_ANDERSON, field, dfield, fieldsize, lam_mix, iter)
+  end subroutine Mixing_Anderson
+
+end module Iterate
+
+! ---------------------------------------------------------------------------
+! RealSpace_adscf: the Film_3D step and integrator of
+! Film_CK_AD/Film_3D/Geometry_Modules/mod_realspace.f90:22-140,267-281 on
+! the GPU, for a driver compiled against the Film_3D Global module.
+module RealSpace_adscf
+  use iso_c_binding
+  use adscf
+  use adscf_shim_state
+  use Global
+  implicit none
+contains
+
+  subroutine Propagate_Step(prop, field)
+    double precision, dimension(gridx, gridy, 0:gridz), intent(inout) :: prop
+    double precision, dimension(gridx, gridy, 0:gridz), intent(in) :: field
+    type(c_ptr) :: ctx
+    integer(c_int) :: rc
+    ctx = shim_film_context(dz, int_scheme)
+    rc = adscf_propagate_step(ctx, prop, field, ds)
+    call adscf_check(ctx, rc, 'Propagate_Step (film)')
+  end subroutine Propagate_Step
+
+  subroutine integrator(integrand, integral)
+    double precision, dimension(gridx, gridy, 0:gridz), intent(in) :: integrand
+    double precision, intent(out) :: integral
+    type(c_ptr) :: ctx
+    integer(c_int) :: rc
+    ctx = shim_film_context(dz, int_scheme)
+    rc = adscf_integrator(ctx, integrand, integral)
+    call adscf_check(ctx, rc, 'integrator')
+  end subroutine integrator
+
+end module RealSpace_adscf

@@ -49,6 +49,84 @@ def test_struct_layout_matches_c(tmp_path):
                                      ctypes.sizeof(_lib.IterResult)]
 
 
+def _c_struct_members(name):
+    """Member names, in order, of `typedef struct name {...} name;` in adscf.h."""
+    text = (ROOT / "include" / "adscf.h").read_text()
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), text, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = []
+    for decl in body.split(";"):
+        decl = " ".join(decl.split())
+        if not decl:
+            continue
+        decl = re.sub(r"^(const )?(unsigned )?\w+ \*?", "", decl)
+        for d in decl.split(","):
+            names.append(re.sub(r"[\s*]|\[.*\]", "", d))
+    return names
+
+
+def _fortran_members(tname):
+    text = (ROOT / "include" / "adscf.f90").read_text()
+    body = re.search(r"type, bind\(C\) :: %s\n(.*?)end type" % tname, text, re.S).group(1)
+    names = []
+    for line in body.splitlines():
+        line = line.split("!")[0]
+        if "::" not in line:
+            continue
+        for d in line.split("::")[1].split(","):
+            names.append(re.sub(r"\(.*\)", "", d).strip())
+    return names
+
+
+CTYPES_NAME = {"lambda": "lam"}   # `lambda` is a Python keyword
+
+
+@pytest.mark.parametrize("cname,pyname", [("adscf_params", "Params"),
+                                          ("adscf_chain_result", "ChainResult"),
+                                          ("adscf_iter_result", "IterResult")])
+def test_struct_field_offsets_match_c(tmp_path, cname, pyname):
+    """offsetof of every member seen by gcc equals the ctypes mirror's offset,
+    and the Fortran bind(C) type lists the same members in the same order."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    members = _c_struct_members(cname)
+    prog = ['#include <stdio.h>', '#include <stddef.h>', '#include "adscf.h"', "int main(){"]
+    prog += ['printf("%%zu\\n", offsetof(%s, %s));' % (cname, m) for m in members]
+    prog += ["return 0;}"]
+    src = tmp_path / "off.c"
+    src.write_text("\n".join(prog))
+    exe = tmp_path / "off"
+    subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    offs = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                           check=True).stdout.split()]
+    from adscf_gb300 import _lib
+    cls = getattr(_lib, pyname)
+    py = [getattr(cls, CTYPES_NAME.get(m, m)).offset for m in members]
+    assert offs == py, list(zip(members, offs, py))
+    assert [f[0] for f in cls._fields_] == [CTYPES_NAME.get(m, m) for m in members]
+    assert _fortran_members(cname) == members
+
+
+def test_fortran_binding_names_declared_symbols():
+    """Every bind(C) name of the Fortran binding is an entry point of the
+    header, and the shim keeps the reference's module procedure names."""
+    decl = set(declared_symbols())
+    f90 = (ROOT / "include" / "adscf.f90").read_text()
+    bound = re.findall(r'bind\(C, name="(\w+)"\)', f90)
+    assert bound and set(bound) <= decl
+    shim = (ROOT / "include" / "adscf_shim.f90").read_text()
+    for mod in ("Propagate", "Molecule_Diblock_Copolymer", "Iterate", "RealSpace_adscf"):
+        assert re.search(r"^module %s$" % mod, shim, re.M), mod
+    for proc in ("Calculate_Expfield", "Propagate_Step", "Initialize_Diblock", "Propagate_Diblock",
+                 "Mixing_Simple", "Mixing_Lambda", "Mixing_Anderson", "integrator"):
+        assert re.search(r"^\s*subroutine %s\(" % proc, shim, re.M), proc
+    called = set(re.findall(r"\b(adscf_\w+)\(", shim)) - {"adscf_check", "adscf_error_text"}
+    assert called <= set(bound), called - set(bound)
+
+
 def test_status_strings_without_gpu(lib):
     assert lib.adscf_abi_version() == 2
     assert lib.adscf_status_string(3).decode() == "zero tridiagonal pivot"

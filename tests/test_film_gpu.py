@@ -248,3 +248,28 @@ def test_brush_gradient_wrt_wall_potential(rng):
     with make(ext, 1.0 + 1e-4) as a, make(ext, 1.0 - 1e-4) as b:
         fd = (a.forward(field) - b.forward(field)) / 2e-4
     assert abs(dww - fd) < 1e-8 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("geom,grid,scheme,span", [(FILM_3D, (6, 4, 20), 1, 0), (FILM_3D, (6, 4, 20), 0, 0),
+                                                   (FILM_1D, (1, 1, 30), 1, 1), (FILM_1D, (1, 1, 30), 0, 1)])
+def test_integrator_entry_point_vs_oracle(geom, grid, scheme, span, rng):
+    """adscf_integrator (integrator, Film_3D/.../mod_realspace.f90:267-281;
+    Film_1D/Brush interior form) on a host integrand against the oracle."""
+    gx, gy, gz = grid
+    dz, zr = of.tanh_mesh(gz, 3.0)
+    size = (3.0, 2.0, 3.0) if geom == FILM_3D else (1.0, 1.0, 3.0)
+    f = rng.random((gz + 1, gy, gx))
+    with film_ctx(geom, grid, dz, size, int_scheme=scheme, int_span=span) as c:
+        got = c.integrator(f)
+    want = of.integrator(f, dz, size[0] / gx, size[1] / gy, int_scheme=scheme,
+                         span="full" if span == 0 else "interior")
+    assert abs(got - want) <= 1e-13 * abs(want)
+
+
+def test_integrator_entry_point_bulk(rng):
+    """Bulk: dvol * sum (the reference's dvol * sum(...) reductions)."""
+    from adscf_gb300 import BULK
+    f = rng.random((12, 10, 8))
+    with Context(BULK, grid=(8, 10, 12), size=(2.0, 2.5, 3.0), ds=0.05, block_length=(0.5, 0.5)) as c:
+        got = c.integrator(f)
+    assert abs(got - f.sum() * (2.0 * 2.5 * 3.0) / f.size) <= 1e-13 * abs(got)
