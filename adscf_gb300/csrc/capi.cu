@@ -390,6 +390,9 @@ int adscf_propagate_diblock_dev(adscf_ctx* ctx, const double* d_field, double* d
   }
   ScfDev S2 = ctx->S;
   S2.dens = d_density;
+  // the closure's accuracy term compares with what the output holds: start
+  // from zero, so the status reflects this call's Q and densities only
+  CK(cudaMemsetAsync(d_density, 0, nvar(ctx) * sizeof(double), ctx->stream));
   launch_closure(S2, 0, ctx->closure_blocks, ctx->stream);
   k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(S2, 1, 0);
   CK(cudaGetLastError());
@@ -423,6 +426,7 @@ int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* den
   if ((rc = film_check_pivot(ctx))) return rc;
   ScfDev S2 = ctx->S;
   S2.dens = d_out;
+  CK(cudaMemsetAsync(d_out, 0, nv * sizeof(double), ctx->stream));   // see adscf_propagate_diblock_dev
   launch_closure(S2, 0, ctx->closure_blocks, ctx->stream);
   k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(S2, 1, 0);
   CK(cudaGetLastError());

@@ -54,6 +54,47 @@ def gather_instances(local: list, rng: range, n: int, group=None) -> list | None
     return out
 
 
+def instance_cost(kw) -> float:
+    """Work of one batch instance: grid points x contour steps."""
+    gx, gy, gz = kw.get("grid", (32, 32, 32))
+    planes = gz if kw.get("geometry", 0) == 0 else gz + 1
+    if kw.get("dss") is not None:
+        steps = len(kw["dss"]) - 1
+    else:
+        f = kw.get("block_length", (0.5, 0.5))
+        ds = kw.get("ds", 0.01)
+        steps = round(f[0] / ds) + round(f[1] / ds)
+    return float(gx * gy * planes) * float(steps)
+
+
+def run_batch(instances, fields, n_iter, tol=-1.0):
+    """One rank's share: a Batch (adscf_batch_*) over `instances`, n_iter SCF
+    iterations; per-instance (free energy, accuracy, log Q, status, iter)."""
+    from .scf import Batch
+    if not instances:
+        return []
+    with Batch(instances) as b:
+        b.set_fields(fields)
+        res = b.scf_run(n_iter, tol)
+    return [dict(free_energy=r.free_energy, accuracy=r.accuracy, logQ=r.logQ,
+                 status=r.status, iter=r.iter) for r in res]
+
+
+def run_batch_sharded(instances, fields, n_iter, tol=-1.0, runner=None, group=None):
+    """Run a batch split across the ranks of `group`: rank r takes the
+    contiguous, cost-balanced range shard(costs, r, world), runs it with
+    `runner(instances, fields, n_iter, tol)` (default: run_batch on this
+    rank's GPU) with no collective on the data path, and rank 0 receives
+    every instance's result in instance order (other ranks: None)."""
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    rg = shard([instance_cost(k) for k in instances], rank, world)
+    run = runner or run_batch
+    local = run([instances[i] for i in rg], [fields[i] for i in rg], n_iter, tol)
+    return gather_instances(local, rg, len(instances), group=group)
+
+
 def max_over_ranks(value: float, group=None, device=None) -> float:
     """Maximum of a per-rank scalar (the benchmark's timed region)."""
     import torch

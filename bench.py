@@ -154,80 +154,107 @@ def time_stage(torch, ctx, stream, stage, reps):
 
 
 # --------------------------------------------------------------------------
-# CPU legs (oracle restatement of the reference, bounded samples)
+# CPU legs: the C++17/OpenMP FP64 restatement of the reference's iteration
+# (oracle/scf_cpu.cpp; gfortran and FFTW, which the reference needs, are on
+# neither machine), timed over whole SCF iterations of the same workload
 # --------------------------------------------------------------------------
-def cpu_sample(nsteps, workers):
-    """Time `nsteps` Propagate_Step calls, `nsteps` contour-slice products and
-    one closure + Anderson mix at 128^3 on the host; return seconds per whole
-    iteration (2 Ns steps, Ns+1 slices) extrapolated from the sample."""
-    from oracle import bulk as ob, interactions as oi, iterate as oit
-    grid = (GRID, GRID, GRID)
-    w = c3_fields()
-    e = ob.calculate_expfield(w, DS)
-    lap = ob.calculate_laplace(grid, (L, L, L), DS)
-    if workers and workers > 1:
-        import scipy.fft as sf
-        fwd = lambda a: sf.rfftn(a, workers=workers) / a.size
-        inv = lambda f, s: sf.irfftn(f, s=s, workers=workers) * float(np.prod(s))
-    else:
-        fwd = ob.real2fourier
-        inv = ob.fourier2real
-    q = np.ones(grid)
+def cpu_model():
+    """CPU model string and logical core count of this host."""
+    model = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        try:
+            for line in Path("/proc/cpuinfo").read_text().splitlines():
+                if line.startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    return model or "unknown", os.cpu_count() or 1
+
+
+def cpu_context():
+    from oracle import cbuild
+    return cbuild.ScfCpu((GRID, GRID, GRID), (L, L, L), DS, F_A, KAPPA, CHI, m=M_HIST, lam=LAM,
+                         lam_warm=LAM, warm_iters=M_HIST)
+
+
+def cpu_iterations(c, n):
+    """Seconds per whole SCF iteration over n iterations of context c."""
     t0 = time.perf_counter()
-    for s in range(nsteps):
-        t = 0 if s % 2 == 0 else 1
-        q = e[t] * q
-        q = inv(lap * fwd(q), q.shape)
-        q = e[t] * q
-    t1 = time.perf_counter()
-    acc = np.zeros(grid)
-    for s in range(nsteps):
-        acc += DS * q * q
-    t2 = time.perf_counter()
-    dens = np.stack([acc, acc])
-    nf = oi.mean_fields(dens, KAPPA, CHI)
-    hist = np.zeros((M_HIST + 1, dens.size))
-    dh = np.zeros_like(hist)
-    hist[:] = w.reshape(1, -1)
-    dh[:] = (nf - w).reshape(1, -1) * (1 + 0.01 * np.arange(M_HIST + 1))[:, None]
-    oit.mixing_anderson(hist, dh, LAM, it=M_HIST + 1)
-    t3 = time.perf_counter()
-    ns = int(round(F_A / DS)) + int(round((1 - F_A) / DS))
-    per_step = (t1 - t0) / nsteps
-    per_slice = (t2 - t1) / nsteps
-    return 2 * ns * per_step + (ns + 1) * per_slice + (t3 - t2), t3 - t0
+    c.iterate(n)
+    return (time.perf_counter() - t0) / n
+
+
+def config(world):
+    return {"workload": "bulk diblock 128^3 Ns=200 f_A=0.40 chiN=20 kappa=25 L=3.8 "
+                        "canonical, Anderson m=10, {211} fields + noise",
+            "grid": [GRID, GRID, GRID], "ns": 200, "parallelism": f"replicas{world}",
+            "l2": "working set 3.4 GB > L2 (no flush needed)"}
 
 
 def run_reference(args):
+    """Whole SCF iterations of the workload on all host cores: W untimed,
+    then K timed, each a full iteration (both chains over 200 contour
+    steps, contour integral, mean fields, Anderson mix)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    cores = os.cpu_count() or 1
-    per_iter = []
-    for _ in range(args.warmup):
-        cpu_sample(4, cores)
-    wall = 0.0
-    for _ in range(args.steps):
-        t_iter, t_wall = cpu_sample(8, cores)
-        per_iter.append(t_iter)
-        wall += t_wall
-    v = 1.0 / statistics.mean(per_iter)
-    sample = (f"each step: 8 Propagate_Step (r2c/c2r via scipy.fft, {cores} workers) + 8 contour "
-              f"slice products + one closure/Anderson mix at 128^3, extrapolated to 400 steps and "
-              f"201 slices; FP64 restatement of the reference (gfortran absent)")
+    from oracle import cbuild
+    lib = cbuild.load()
+    model, ncpu = cpu_model()
+    threads = lib.scfcpu_threads()
+    t_start = time.perf_counter()
+    with cpu_context() as c:
+        c.set_field(c3_fields())
+        c.iterate(args.warmup)
+        sec = cpu_iterations(c, args.steps)
+    v = 1.0 / sec
+    sample = (f"{args.steps} whole SCF iterations after {args.warmup} untimed, C++17/OpenMP FP64 "
+              f"restatement of the reference (oracle/scf_cpu.cpp; its own FFT; gfortran/FFTW "
+              f"absent), {threads} threads on {ncpu} logical cores, {model}")
     out = {
         "metric": METRIC, "value": v, "unit": "iter/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "bulk diblock 128^3 Ns=200 f_A=0.40 chiN=20 L=3.8 Anderson m=10",
-                   "grid": [GRID, GRID, GRID], "ns": 200, "l2": "n/a (host)"},
-        "cpu_baseline": {"value": v, "unit": "iter/s", "cores": cores, "kind": "port",
-                         "sample": sample},
+        "ms_per_step": 1000.0 * sec, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config(args.gpus),
+        "cpu_baseline": {"value": v, "unit": "iter/s", "cores": threads, "kind": "port",
+                         "sample": sample, "cpu_model": model, "nproc": ncpu},
         "e2e": {"value": v, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_start,
     }
     print(json.dumps(out))
     return 0
+
+
+def cpu_baseline_leg():
+    """The restatement on all host cores (2 iterations after 1 untimed) and
+    on one core (1 iteration), same workload and start field."""
+    from oracle import cbuild
+    lib = cbuild.load()
+    model, ncpu = cpu_model()
+    threads = lib.scfcpu_threads()
+    with cpu_context() as c:
+        c.set_field(c3_fields())
+        c.iterate(1)
+        s_all = cpu_iterations(c, 2)
+        lib.scfcpu_set_threads(1)
+        try:
+            s_one = cpu_iterations(c, 1)
+        finally:
+            lib.scfcpu_set_threads(threads)
+    return {"value": 1.0 / s_all, "unit": "iter/s", "cores": threads, "kind": "port",
+            "sample": f"whole SCF iterations of the same workload (2 timed after 1 untimed) on "
+                      f"{threads} threads; C++17/OpenMP FP64 restatement of the reference "
+                      f"(oracle/scf_cpu.cpp), {model}, nproc {ncpu}",
+            "single_core_iter_s": 1.0 / s_one, "cpu_model": model, "nproc": ncpu}
 
 
 # --------------------------------------------------------------------------
@@ -396,10 +423,28 @@ def time_batch(torch, A, inst, fields, stream, steps, warmup):
     return ms, launches, bad
 
 
-def batch_legs(torch, A, stream, args):
+def sharded_time(torch, A, inst, fields, stream, steps, world, rank):
+    """Time this rank's share of a batch (contiguous, cost-balanced instance
+    range, no collective on the data path); the batch time is the maximum
+    over ranks."""
+    from adscf_gb300 import parallel
+    if world == 1:
+        return time_batch(torch, A, inst, fields, stream, steps, 3)
+    rg = parallel.shard([parallel.instance_cost(k) for k in inst], rank, world)
+    ms, launches, bad = 0.0, 0, 0
+    if len(rg):
+        ms, launches, bad = time_batch(torch, A, [inst[i] for i in rg], [fields[i] for i in rg],
+                                       stream, steps, 3)
+    ms = parallel.max_over_ranks(ms, device="cuda")
+    return ms, launches, bad
+
+
+def batch_legs(torch, A, stream, args, world=1, rank=0):
+    """C2 and C5 batches; with several ranks each rank runs its instance
+    range and the figures are whole-batch throughputs."""
     out = {}
     inst, fields = c2_films(A)
-    ms, launches, bad = time_batch(torch, A, inst, fields, stream, args.batch_steps, 3)
+    ms, launches, bad = sharded_time(torch, A, inst, fields, stream, args.batch_steps, world, rank)
     pts_steps = sum(2 * len(k["dss"]) * (k["grid"][2] + 1) for k in inst)   # both chains
     out["film_batch"] = {
         "workload": "C2: 4096 Film_1D diblock films, nz 64-192 tanh meshes, D 2-8, Ns 100-300 "
@@ -409,16 +454,18 @@ def batch_legs(torch, A, stream, args):
         "film_iter_s": len(inst) * 1000.0 / ms,
         "line_solves_s": 2 * len(inst) * sum(len(k["dss"]) - 1 for k in inst) / len(inst) * 1000.0 / ms,
         "point_steps_s": pts_steps * 1000.0 / ms,
-        "launches_per_iter": launches, "nonfinite_instances": bad}
+        "launches_per_iter": launches, "nonfinite_instances": bad,
+        "sharding": f"{world} rank(s), contiguous cost-balanced instance ranges"}
     inst, fields = c5_bulk(A)
-    ms, launches, bad = time_batch(torch, A, inst, fields, stream, args.batch_steps, 3)
+    ms, launches, bad = sharded_time(torch, A, inst, fields, stream, args.batch_steps, world, rank)
     steps = sum(2 * round(1.0 / k["ds"]) for k in inst)
     out["bulk_batch"] = {
         "workload": "C5: 256 bulk diblock instances, grids {24,32,40,48,64}^3, f_A 0.25-0.45, "
                     "chiN 15-30, L 3-5, Ns 100-200, split precision, Anderson m=10",
         "instances": len(inst), "ms_per_iter": ms, "iter_s": 1000.0 / ms,
         "instance_iter_s": len(inst) * 1000.0 / ms, "contour_steps_s": steps * 1000.0 / ms,
-        "launches_per_iter": launches, "nonfinite_instances": bad}
+        "launches_per_iter": launches, "nonfinite_instances": bad,
+        "sharding": f"{world} rank(s), contiguous cost-balanced instance ranges"}
     return out
 
 
@@ -587,10 +634,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32/f64-split", "data": "synthetic",
-        "config": {"workload": "bulk diblock 128^3 Ns=200 f_A=0.40 chiN=20 kappa=25 L=3.8 "
-                               "canonical, Anderson m=10, {211} fields + noise",
-                   "grid": [GRID, GRID, GRID], "ns": ns, "parallelism": f"replicas{world}",
-                   "l2": "working set 3.4 GB > L2 (no flush needed)"},
+        "config": config(world),
         "fp64_gpu_iter_s": world * fp64_iter_s,
         "split_over_fp64": fp64_iter_s and (1000.0 / ms_step) / fp64_iter_s,
         "contour_steps_per_s": world * 2 * ns * 1000.0 / ms_step,
@@ -617,16 +661,12 @@ def main():
     }
     if world == 1:
         out["parity_c1"] = c1_parity(A)
-    if not args.no_batches and world == 1:
-        out["film3d"] = film3d_leg(torch, A, stream, args.batch_steps)
-        out.update(batch_legs(torch, A, stream, args))
+    if not args.no_batches:
+        if world == 1:
+            out["film3d"] = film3d_leg(torch, A, stream, args.batch_steps)
+        out.update(batch_legs(torch, A, stream, args, world, rank))
     if rank == 0 and world == 1 and not args.no_cpu:
-        t_iter, t_wall = cpu_sample(24, 1)
-        out["cpu_baseline"] = {
-            "value": 1.0 / t_iter, "unit": "iter/s", "cores": 1, "kind": "port",
-            "sample": f"24 Propagate_Step + 24 contour slice products + one closure/Anderson mix "
-                      f"at 128^3 (numpy FP64 oracle, {t_wall:.1f} s), extrapolated to 400 steps "
-                      f"and 201 slices"}
+        out["cpu_baseline"] = cpu_baseline_leg()
     if dist:
         dist.destroy_process_group()
     if rank == 0:
