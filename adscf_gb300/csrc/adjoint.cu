@@ -258,6 +258,7 @@ int forward_core(adscf_ctx* ctx, double* free_energy, double* sc_out) {
 extern "C" {
 
 int adscf_forward(adscf_ctx* ctx, const double* field, double* free_energy) {
+  ADSCF_RANGE("adscf_forward");
   if (!ctx || !field) return ADSCF_E_ARG;
   int rc;
   if (ctx->geometry != ADSCF_BULK) {   // films and brushes: F and its wall-potential gradient
@@ -275,6 +276,7 @@ int adscf_forward(adscf_ctx* ctx, const double* field, double* free_energy) {
 }
 
 int adscf_forward_dev(adscf_ctx* ctx, const double* d_field, double* free_energy) {
+  ADSCF_RANGE("adscf_forward_dev");
   if (!ctx || !d_field) return ADSCF_E_ARG;
   int rc;
   if ((rc = check_ctx(ctx)) || (rc = adj_setup(ctx))) return rc;
@@ -286,6 +288,7 @@ int adscf_forward_dev(adscf_ctx* ctx, const double* d_field, double* free_energy
 // FP64 free energy at the context's current (device-resident) SCF field.  A
 // split context evaluates it on an FP64 sibling context created on first use.
 int adscf_free_energy_fp64(adscf_ctx* ctx, adscf_iter_result* out) {
+  ADSCF_RANGE("adscf_free_energy_fp64");
   if (!ctx || !out) return ADSCF_E_ARG;
   if (ctx->geometry != ADSCF_BULK || ctx->p.ensemble != 1)
     return set_err(ctx, ADSCF_E_STATE, "FP64 free energy: bulk contexts, canonical ensemble");
@@ -338,12 +341,14 @@ int adscf_set_adjoint_checkpoint(adscf_ctx* ctx, int every) {
 }
 
 int adscf_backward_surface(adscf_ctx* ctx, double* dF_dchi, double* dF_dU) {
+  ADSCF_RANGE("adscf_backward_surface");
   if (!ctx) return ADSCF_E_ARG;
   if (ctx->geometry == ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "wall-potential gradients are for films and brushes");
   return film_backward(ctx, dF_dchi, dF_dU);
 }
 
 int adscf_backward(adscf_ctx* ctx, double* grad) {
+  ADSCF_RANGE("adscf_backward");
   if (!ctx || !grad) return ADSCF_E_ARG;
   if (ctx->geometry != ADSCF_BULK)
     return set_err(ctx, ADSCF_E_STATE, "films and brushes: use adscf_backward_surface");

@@ -36,6 +36,7 @@
 #include "bulk_reg.cuh"
 #include "film_host.h"
 #include "film_kernels.cuh"
+#include "film_warp.cuh"
 #include "adjoint_kernels.cuh"
 
 struct adscf_batch {
@@ -75,6 +76,7 @@ struct adscf_batch {
   void* d_f32 = nullptr;                // FilmDev<float>[n]
   void* d_f64 = nullptr;                // FilmDev<double>[n]
   int* d_list32 = nullptr;              // films sweeping in FP32 / FP64, by contour length
+  int* d_items32 = nullptr;             // (film << 1) | chain of the FP32 films, same order
   int* d_list64 = nullptr;
   int n32 = 0, n64 = 0;
   // shared-memory line sweeps: rows per line (max gz + 1 of the list) and
@@ -572,6 +574,13 @@ int build_film(adscf_batch* b) {
   BK(cudaMalloc(&b->d_list64, std::max<size_t>(1, l64.size()) * sizeof(int)));
   if (!l32.empty())
     BK(cudaMemcpyAsync(b->d_list32, l32.data(), l32.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  {  // (film, chain) items of the warp sweep, in the order of l32
+    std::vector<int> items;
+    for (int f : l32) { items.push_back(f << 1); items.push_back((f << 1) | 1); }
+    BK(cudaMalloc(&b->d_items32, std::max<size_t>(1, items.size()) * sizeof(int)));
+    if (!items.empty())
+      BK(cudaMemcpyAsync(b->d_items32, items.data(), items.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  }
   if (!l64.empty())
     BK(cudaMemcpyAsync(b->d_list64, l64.data(), l64.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   BK(cudaMalloc(&b->d_S, n * sizeof(ScfDev)));
@@ -589,7 +598,10 @@ int enqueue_film(adscf_batch* b) {
   const FilmDev<float>* f32 = static_cast<const FilmDev<float>*>(b->d_f32);
   const FilmDev<double>* f64 = static_cast<const FilmDev<double>*>(b->d_f64);
   const int pw = b->film_per_warp;
-  if (b->n32 && b->lanes32) {
+  if (b->n32 && b->zcap32 <= 32 * kFilmWarpM) {
+    // one warp per (film, chain), longest contours first
+    k_film1d_warp_b<<<(2 * b->n32 + 3) / 4, 128, 0, s>>>(f32, b->d_S, b->d_items32, 2 * b->n32);
+  } else if (b->n32 && b->lanes32) {
     const int W = b->lanes32;
     k_film1d_chains_sm<float><<<dim3((b->n32 + W - 1) / W, 2), 32 * (W / pw),
                                 film_sweep_smem(b->zcap32, W, sizeof(float)), s>>>(
@@ -925,6 +937,7 @@ int batch_adj_check(adscf_batch* b) {
 extern "C" {
 
 int adscf_batch_forward(adscf_batch* b, const double* fields, double* free_energy) {
+  ADSCF_RANGE("adscf_batch_forward");
   if (!b || !fields || !free_energy) return ADSCF_E_ARG;
   int rc;
   if ((rc = batch_adj_check(b)) || (rc = batch_adj_setup(b))) return rc;
@@ -954,6 +967,7 @@ int adscf_batch_forward(adscf_batch* b, const double* fields, double* free_energ
 }
 
 int adscf_batch_backward(adscf_batch* b, double* grad) {
+  ADSCF_RANGE("adscf_batch_backward");
   if (!b || !grad) return ADSCF_E_ARG;
   int rc;
   if ((rc = batch_adj_check(b))) return rc;
@@ -991,6 +1005,7 @@ int adscf_batch_backward(adscf_batch* b, double* grad) {
 }
 
 int adscf_batch_create(const adscf_params* params, int n, adscf_batch** out) {
+  ADSCF_RANGE("adscf_batch_create");
   if (!out) return ADSCF_E_ARG;
   *out = nullptr;
   if (!params || n < 1) return ADSCF_E_ARG;
@@ -1031,7 +1046,7 @@ int adscf_batch_destroy(adscf_batch* b) {
   cudaFree(b->pool); cudaFree(b->d_inst); cudaFree(b->d_S);
   cudaFree(b->d_tw); cudaFree(b->d_fk); cudaFree(b->d_g64);
   for (auto& C : b->cls) { cudaFree(C.wx); cudaFree(C.wy); cudaFree(C.wz); }
-  cudaFree(b->d_f32); cudaFree(b->d_f64); cudaFree(b->d_list32); cudaFree(b->d_list64);
+  cudaFree(b->d_f32); cudaFree(b->d_f64); cudaFree(b->d_list32); cudaFree(b->d_list64); cudaFree(b->d_items32);
   cudaFree(b->d_tabf);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
@@ -1062,6 +1077,7 @@ int adscf_batch_get_densities(adscf_batch* b, double* densities) {
 }
 
 int adscf_batch_scf_run(adscf_batch* b, int n_iter, double tol, adscf_iter_result* out) {
+  ADSCF_RANGE("adscf_batch_scf_run");
   if (!b || n_iter < 0) return ADSCF_E_ARG;
   ++b->prop_gen;
   int rc = build_graph(b);
@@ -1086,6 +1102,7 @@ int adscf_batch_set_stream(adscf_batch* b, void* cuda_stream) {
 }
 
 int adscf_batch_enqueue(adscf_batch* b, int repeats) {
+  ADSCF_RANGE("adscf_batch_enqueue");
   if (!b || repeats < 0) return ADSCF_E_ARG;
   ++b->prop_gen;
   int rc = build_graph(b);

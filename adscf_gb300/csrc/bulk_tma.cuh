@@ -189,8 +189,9 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       tmak::tma_load_3d(buf + (size_t)s * LY::tile_elems + b * LY::box_elems, &tmap, &bar[s], cx, cy, cz);
     }
   };
-  // loads issued / completed per stage (thread 0), to drain on an early exit
-  int issued[2] = {0, 0}, done[2] = {0, 0};
+  // loads issued / completed, in issue order (load k uses stage k & 1 with
+  // phase (k >> 1) & 1), to drain on an early exit
+  int issued = 0, done = 0;
   tmak::pdl_launch_dependents();
   // the first tile's load is issued as soon as the previous pass is complete;
   // the other threads load the constant tables meanwhile
@@ -199,7 +200,7 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
     tmak::mbar_init(&bar[1], 1);
     tmak::fence_mbar_init();
     tmak::pdl_wait();
-    if (blockIdx.x < ntiles) { issue_load(blockIdx.x, 0); issued[0] = 1; }
+    if (blockIdx.x < ntiles) { issue_load(blockIdx.x, 0); issued = 1; }
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = gtw[tw_off + i];
   if constexpr (KIND == 2) {
@@ -247,14 +248,21 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
     if (threadIdx.x == 0 && nxt < ntiles) {
       tmak::bulk_wait_read0();  // the store of the tile last held in stage s^1 has read it
       issue_load(nxt, s ^ 1);
-      ++issued[s ^ 1];
+      ++issued;
+    }
+    // this line's k-space factor is read while the tile is in flight
+    float ah = 0.f, al = 0.f;
+    if constexpr (KIND == 2) {
+      const int L = tile * LPC + line;
+      ah = gxy[L];
+      al = gxy[gx * gy + L];
     }
     const bool got = tmak::mbar_wait_bounded(&bar[s], (it >> 1) & 1, I.wait_polls);
     if (!__syncthreads_and(got)) {
       if (threadIdx.x == 0) atomicOr(err, 2);
       break;
     }
-    ++done[s];
+    ++done;
     float2* tb = buf + (size_t)s * LY::tile_elems + box * LY::box_elems;
     float2 v[R1];
 #pragma unroll
@@ -268,8 +276,6 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       F::forward(v, sc, tw, lt);
     } else {
       F::forward(v, sc, tw, lt);
-      const int L = tile * LPC + line;
-      const float ah = gxy[L], al = gxy[gx * gy + L];
 #pragma unroll
       for (int r = 0; r < R1; ++r) {
         const int kz = F::out_index(lt, r);
@@ -309,9 +315,8 @@ k_rs_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   }
   if (threadIdx.x == 0) {
     // loads still in flight after an early exit land before shared memory is released
-    for (int st = 0; st < 2; ++st)
-      for (int k = done[st]; k < issued[st]; ++k)
-        tmak::mbar_wait_bounded(&bar[st], k & 1, tmak::kWaitPolls);
+    for (int k = done; k < issued; ++k)
+      tmak::mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, tmak::kWaitPolls);
     tmak::bulk_wait0();
   }
 }
@@ -347,7 +352,15 @@ struct XYLayout {
   static constexpr size_t sc_off = plane_bytes;             // plane at 0 (1024-aligned)
   static constexpr size_t tw_off = sc_off + (size_t)LINES * F::LS * sizeof(float2);
   static constexpr size_t bar_off = ((tw_off + N * sizeof(float2) + 15) / 16) * 16;
-  static constexpr size_t bytes = bar_off + sizeof(uint64_t) + 1024;   // + alignment slack
+  static constexpr size_t bytes = bar_off + 2 * sizeof(uint64_t) + 1024;   // + alignment slack
+  // the plane arrives and leaves as two halves of NB / 2 boxes (columns
+  // [0, N/2) and [N/2, N)), one mbarrier each, so that phase 1 starts on the
+  // first half while the second is in flight and the first half is stored
+  // while phase 3 transforms the second
+  static constexpr int HB = NB / 2;
+  static constexpr uint32_t half_bytes = plane_bytes / 2;
+  static constexpr bool split = LINES < N;   // rounds of phases 1 and 3 cover one half each
+  static_assert(!split || LINES == N / 2, "a round covers one half of the plane");
   static_assert(N % LINES == 0 || LINES % N == 0, "rounds of whole lines");
 };
 
@@ -379,18 +392,37 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
   const bool init = t == 0;
   const bool more = init || t < I.ns;
   const int gz = I.gz;
-  int it = 0, issued = 0, done = 0;
+  int it = 0, issued = 0, done0 = 0, done1 = 0;
   auto issue_plane = [&](int z) {
-    tmak::mbar_expect_tx(bar, LY::plane_bytes);
-    for (int b = 0; b < LY::NB; ++b)
-      tmak::tma_load_3d(plane + b * LY::box_elems, &tmap, bar, b * tmak::kBoxCols, 0, z);
+    for (int h = 0; h < 2; ++h) {
+      tmak::mbar_expect_tx(&bar[h], LY::half_bytes);
+      for (int b = h * LY::HB; b < (h + 1) * LY::HB; ++b)
+        tmak::tma_load_3d(plane + b * LY::box_elems, &tmap, &bar[h], b * tmak::kBoxCols, 0, z);
+    }
     ++issued;
+  };
+  auto store_half = [&](int h, int z) {
+    for (int b = h * LY::HB; b < (h + 1) * LY::HB; ++b)
+      tmak::tma_store_3d(&tmap, plane + b * LY::box_elems, b * tmak::kBoxCols, 0, z);
+    tmak::bulk_commit();
+  };
+  // bounded wait for half h of plane iteration `it`; false (flag 8 set) when
+  // it expired in any thread of the CTA
+  auto wait_half = [&](int h) {
+    const bool got = tmak::mbar_wait_bounded(&bar[h], (uint32_t)(it & 1), I.wait_polls);
+    if (!__syncthreads_and(got)) {
+      if (threadIdx.x == 0) atomicOr(err, 8);
+      return false;
+    }
+    if (h == 0) ++done0; else ++done1;
+    return true;
   };
   tmak::pdl_launch_dependents();
   // the first plane's load is issued as soon as the previous pass is
   // complete; the other threads load the constant tables meanwhile
   if (threadIdx.x == 0) {
-    tmak::mbar_init(bar, 1);
+    tmak::mbar_init(&bar[0], 1);
+    tmak::mbar_init(&bar[1], 1);
     tmak::fence_mbar_init();
     tmak::pdl_wait();
     if (!init && (int)blockIdx.x < gz) issue_plane(blockIdx.x);
@@ -420,16 +452,15 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       // so a warp barrier orders the write.
       float2 dco = make_float2(0.f, 0.f);
       if (dcout && threadIdx.x == 0) dco = dcout[z];
-      const bool got = tmak::mbar_wait_bounded(bar, (uint32_t)(it & 1), I.wait_polls);
-      if (!__syncthreads_and(got)) {
-        if (threadIdx.x == 0) atomicOr(err, 8);
-        break;
-      }
-      ++done;
+      if (!wait_half(0)) break;
+      if (!LY::split && !wait_half(1)) break;
       if (dcout && threadIdx.x == 0) plane[tmak::plane_at<N>(0, 0)] = dco;
       __syncwarp();
-      // phase 1: inverse y, columns x
+      // phase 1: inverse y, columns x (with split halves, the round of the
+      // second half waits for its boxes)
+      bool ok = true;
       for (int c0 = 0; c0 < N; c0 += LINES) {
+        if (LY::split && c0 > 0 && !(ok = wait_half(1))) break;
         const int x = c0 + line;
         if (active && x < N) {
           float2 v[R1];
@@ -440,6 +471,7 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
           for (int r = 0; r < R1; ++r) plane[tmak::plane_at<N>(F::in_index(lt, r), x)] = v[r];
         }
       }
+      if (!ok) break;
       __syncthreads();
     } else {
       if (threadIdx.x == 0) tmak::bulk_wait_read0();
@@ -490,7 +522,8 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
     }
     __syncthreads();
     if (!more) continue;                  // last step: nothing goes back to the spectrum
-    // phase 3: forward y, columns x
+    // phase 3: forward y, columns x; each half leaves as soon as its columns
+    // are done
     for (int c0 = 0; c0 < N; c0 += LINES) {
       const int x = c0 + line;
       if (active && x < N) {
@@ -501,19 +534,24 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
 #pragma unroll
         for (int r = 0; r < R1; ++r) plane[tmak::plane_at<N>(F::out_index(lt, r), x)] = v[r];
       }
+      if (LY::split) {
+        tmak::fence_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) store_half(c0 == 0 ? 0 : 1, z);
+      }
     }
-    tmak::fence_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      for (int b = 0; b < LY::NB; ++b)
-        tmak::tma_store_3d(&tmap, plane + b * LY::box_elems, b * tmak::kBoxCols, 0, z);
-      tmak::bulk_commit();
+    if (!LY::split) {
+      tmak::fence_async_smem();
+      __syncthreads();
+      if (threadIdx.x == 0) { store_half(0, z); store_half(1, z); }
+    }
+    if (threadIdx.x == 0)
       dcin[((t + 1) & 1) * N + z] = plane[tmak::plane_at<N>(0, 0)];   // the next z pass's pencil
-    }
   }
   if (threadIdx.x == 0) {
-    // a load still in flight after an early exit lands before shared memory is released
-    for (int k = done; k < issued; ++k) tmak::mbar_wait_bounded(bar, (uint32_t)(k & 1), tmak::kWaitPolls);
+    // loads still in flight after an early exit land before shared memory is released
+    for (int k = done0; k < issued; ++k) tmak::mbar_wait_bounded(&bar[0], (uint32_t)(k & 1), tmak::kWaitPolls);
+    for (int k = done1; k < issued; ++k) tmak::mbar_wait_bounded(&bar[1], (uint32_t)(k & 1), tmak::kWaitPolls);
     tmak::bulk_wait0();
   }
 }

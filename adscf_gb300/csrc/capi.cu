@@ -212,6 +212,7 @@ int adscf_contour_info(const adscf_ctx* ctx, int* ns, int* n_a) {
 }
 
 int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
+  ADSCF_RANGE("adscf_ctx_create");
   if (!out) return ADSCF_E_ARG;
   *out = nullptr;
   std::string why;
@@ -377,6 +378,7 @@ int adscf_ctx_destroy(adscf_ctx* ctx) {
 // ---- propagator ----------------------------------------------------------
 int adscf_propagate_diblock_dev(adscf_ctx* ctx, const double* d_field, double* d_density,
                                 adscf_chain_result* out) {
+  ADSCF_RANGE("adscf_propagate_diblock_dev");
   if (!ctx || !d_field || !d_density) return ADSCF_E_ARG;
   ++ctx->prop_gen;
   if (ctx->geometry == ADSCF_BRUSH) return set_err(ctx, ADSCF_E_STATE, "brush context: use adscf_propagate_homopolymer");
@@ -401,6 +403,7 @@ int adscf_propagate_diblock_dev(adscf_ctx* ctx, const double* d_field, double* d
 
 int adscf_propagate_diblock(adscf_ctx* ctx, const double* field, double* density,
                             adscf_chain_result* out) {
+  ADSCF_RANGE("adscf_propagate_diblock");
   if (!ctx || !field || !density) return ADSCF_E_ARG;
   const size_t nv = nvar(ctx);
   double* d_w = ctx->d_tmp;
@@ -414,6 +417,7 @@ int adscf_propagate_diblock(adscf_ctx* ctx, const double* field, double* density
 
 int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* density,
                                 adscf_chain_result* out) {
+  ADSCF_RANGE("adscf_propagate_homopolymer");
   if (!ctx || !field || !density) return ADSCF_E_ARG;
   ++ctx->prop_gen;
   if (ctx->geometry != ADSCF_BRUSH) return set_err(ctx, ADSCF_E_STATE, "not a brush context");
@@ -435,6 +439,7 @@ int adscf_propagate_homopolymer(adscf_ctx* ctx, const double* field, double* den
 }
 
 int adscf_propagate_step(adscf_ctx* ctx, double* prop, const double* aux, double ds) {
+  ADSCF_RANGE("adscf_propagate_step");
   if (!ctx || !prop || !aux) return ADSCF_E_ARG;
   ++ctx->prop_gen;
   const size_t n = ctx->npts;
@@ -450,6 +455,7 @@ int adscf_propagate_step(adscf_ctx* ctx, double* prop, const double* aux, double
 }
 
 int adscf_real2fourier(adscf_ctx* ctx, const double* prop, double* spectrum) {
+  ADSCF_RANGE("adscf_real2fourier");
   if (!ctx || !prop || !spectrum) return ADSCF_E_ARG;
   ++ctx->prop_gen;
   if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "bulk only");
@@ -460,6 +466,7 @@ int adscf_real2fourier(adscf_ctx* ctx, const double* prop, double* spectrum) {
 }
 
 int adscf_fourier2real(adscf_ctx* ctx, const double* spectrum, double* prop) {
+  ADSCF_RANGE("adscf_fourier2real");
   if (!ctx || !prop || !spectrum) return ADSCF_E_ARG;
   ++ctx->prop_gen;
   if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "bulk only");
@@ -470,6 +477,7 @@ int adscf_fourier2real(adscf_ctx* ctx, const double* spectrum, double* prop) {
 
 // ---- interactions -------------------------------------------------------
 int adscf_mean_fields(adscf_ctx* ctx, const double* density, double* field) {
+  ADSCF_RANGE("adscf_mean_fields");
   if (!ctx || !density || !field) return ADSCF_E_ARG;
   const size_t nv = nvar(ctx);
   int rc = h2d(ctx, ctx->d_tmp, density, nv);
@@ -523,6 +531,7 @@ int adscf_integrator(adscf_ctx* ctx, const double* integrand, double* integral) 
 
 // ---- mixing ---------------------------------------------------------------
 int adscf_mix_dev(adscf_ctx* ctx, double* d_field, const double* d_dfield, int iter) {
+  ADSCF_RANGE("adscf_mix_dev");
   if (!ctx || !d_field || !d_dfield || iter < 1) return ADSCF_E_ARG;
   const size_t nv = nvar(ctx);
   const int cur = iter % ctx->hist_slots;
@@ -542,6 +551,7 @@ int adscf_mix_dev(adscf_ctx* ctx, double* d_field, const double* d_dfield, int i
 }
 
 int adscf_mix(adscf_ctx* ctx, double* field, const double* dfield, int iter) {
+  ADSCF_RANGE("adscf_mix");
   if (!ctx || !field || !dfield) return ADSCF_E_ARG;
   const size_t nv = nvar(ctx);
   int rc;
@@ -596,6 +606,7 @@ int adscf_get_density(adscf_ctx* ctx, double* density) {
 }
 
 int adscf_scf_run(adscf_ctx* ctx, int n_iter, double tol, adscf_iter_result* out) {
+  ADSCF_RANGE("adscf_scf_run");
   if (!ctx || n_iter < 0) return ADSCF_E_ARG;
   ++ctx->prop_gen;
   int rc = build_iteration_graph(ctx);
@@ -617,6 +628,7 @@ int adscf_scf_run(adscf_ctx* ctx, int n_iter, double tol, adscf_iter_result* out
 }
 
 int adscf_scf_iteration(adscf_ctx* ctx, double* field, double* density, adscf_iter_result* out) {
+  ADSCF_RANGE("adscf_scf_iteration");
   if (!ctx || !field || !density) return ADSCF_E_ARG;
   ++ctx->prop_gen;
   int rc = build_iteration_graph(ctx);
@@ -664,6 +676,7 @@ int adscf_set_wait_limit(adscf_ctx* ctx, int polls) {
 }
 
 int adscf_set_box(adscf_ctx* ctx, double sizex, double sizey, double sizez) {
+  ADSCF_RANGE("adscf_set_box");
   if (!ctx || !(sizex > 0 && sizey > 0 && sizez > 0)) return ADSCF_E_ARG;
   if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "box updates are for bulk contexts");
   ++ctx->prop_gen;
@@ -723,6 +736,7 @@ int adscf_stage_launches(const adscf_ctx* ctx, int stage) {
 }
 
 int adscf_enqueue(adscf_ctx* ctx, int stage, int repeats) {
+  ADSCF_RANGE("adscf_enqueue");
   if (!ctx || repeats < 0) return ADSCF_E_ARG;
   ++ctx->prop_gen;
   int rc;

@@ -294,6 +294,7 @@ int adscf_ddft_rhs(adscf_ctx* ctx, const double* mu, double* ddensity) {
 
 int adscf_conjugate_fields(adscf_ctx* ctx, const double* density, double accuracy, int itermax, int* status,
                            int* iterations) {
+  ADSCF_RANGE("adscf_conjugate_fields");
   if (!ctx || !density || !status || itermax < 1) return ADSCF_E_ARG;
   int rc;
   if ((rc = need_bulk(ctx)) || (rc = ddft_alloc(ctx))) return rc;
@@ -305,6 +306,7 @@ int adscf_conjugate_fields(adscf_ctx* ctx, const double* density, double accurac
 
 int adscf_ddft_step(adscf_ctx* ctx, double* density, double timestep, int floor_density, double accuracy,
                     int itermax, int* status) {
+  ADSCF_RANGE("adscf_ddft_step");
   if (!ctx || !density || !status || itermax < 1) return ADSCF_E_ARG;
   int rc;
   if ((rc = need_bulk(ctx)) || (rc = ddft_alloc(ctx))) return rc;

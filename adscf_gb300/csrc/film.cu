@@ -6,6 +6,7 @@
 
 #include "film_host.h"
 #include "film_kernels.cuh"
+#include "film_warp.cuh"
 #include "internal.h"
 
 struct FilmState {
@@ -34,6 +35,12 @@ struct FilmState {
   double* d_fe_out = nullptr;   // [2 + ntypes*nplanes]
   long long fe_gen = -1;
 };
+
+// warp-cooperative FP32 ADI sweeps (film_adi.cu)
+int adi_warp_mask(const FilmDev<float>& D);
+void adi_x_warp(const FilmDev<float>& D, int step, int chains, cudaStream_t s);
+void adi_y_warp(const FilmDev<float>& D, int step, int chains, cudaStream_t s);
+void adi_z_warp(const FilmDev<float>& D, int step, int chains, cudaStream_t s);
 
 namespace {
 
@@ -86,6 +93,37 @@ AdiLaunch adi_launch(const FilmState* F, const FilmDev<T>& D, int chains) {
   return A;
 }
 
+// One Douglas ADI step (three sweeps) of `chains` chains: FP32 sweeps whose
+// lines fit run on the warp solver (film_adi.cu), the rest one thread per
+// line.
+template <typename T>
+void adi_step(const AdiLaunch& A, const FilmDev<T>& D, const FieldRef& fr, int st, int chains, cudaStream_t s) {
+  int m = 0;
+  if constexpr (sizeof(T) == 4) m = adi_warp_mask(D);
+  if constexpr (sizeof(T) == 4) { if (m & 1) adi_x_warp(D, st, chains, s); }
+  if (!(m & 1)) k_adi_x<T><<<A.gx, A.wx, A.sx, s>>>(D, fr, st);
+  if constexpr (sizeof(T) == 4) { if (m & 2) adi_y_warp(D, st, chains, s); }
+  if (!(m & 2)) k_adi_y<T><<<A.gy, A.wy, A.sy, s>>>(D, st);
+  if constexpr (sizeof(T) == 4) { if (m & 4) adi_z_warp(D, st, chains, s); }
+  if (!(m & 4)) k_adi_z<T><<<A.gz, A.wz, A.sz, s>>>(D, fr, st);
+}
+
+// 1D chains of every line: FP32 sweeps on lines of up to 32 * kFilmWarpM
+// planes with one warp per (line, chain) (film_warp.cuh); FP64 sweeps (the
+// reference's serial Thomas) and longer lines with one thread per (line,
+// chain).
+template <typename T>
+void launch_chains_1d(const FilmDev<T>& D, const FieldRef& fr, int chains, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (D.gz + 1 <= 32 * kFilmWarpM) {
+      k_film1d_warp<<<dim3((D.nlines + 3) / 4, chains), 128, 0, s>>>(D);
+      return;
+    }
+  }
+  const dim3 g((D.nlines + FILM_THREADS - 1) / FILM_THREADS, chains);
+  k_film1d_chains<T><<<g, FILM_THREADS, 0, s>>>(D, fr);
+}
+
 template <typename T>
 int chains_t(adscf_ctx* ctx, const double* d_w) {
   FilmState* F = ctx->film;
@@ -100,18 +138,13 @@ int chains_t(adscf_ctx* ctx, const double* d_w) {
       k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
     }
     const AdiLaunch A = adi_launch<T>(F, D, 2);
-    for (int st = 1; st <= D.ns; ++st) {
-      k_adi_x<T><<<A.gx, A.wx, A.sx, s>>>(D, fr, st);
-      k_adi_y<T><<<A.gy, A.wy, A.sy, s>>>(D, st);
-      k_adi_z<T><<<A.gz, A.wz, A.sz, s>>>(D, fr, st);
-    }
+    for (int st = 1; st <= D.ns; ++st) adi_step<T>(A, D, fr, st, 2, s);
   } else {
     if (sizeof(T) == 4) {
       const size_t n = (size_t)ctx->ntypes * D.npts;
       k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
     }
-    const dim3 g((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 2);
-    k_film1d_chains<T><<<g, FILM_THREADS, 0, s>>>(D, fr);
+    launch_chains_1d<T>(D, fr, 2, s);
   }
   CK(cudaGetLastError());
   return ADSCF_OK;
@@ -148,14 +181,11 @@ int step_single_t(adscf_ctx* ctx, double* d_prop, const double* d_w, double ds) 
     if (sizeof(T) == 4)   // one field (type 0) of npts values
       k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
     const AdiLaunch A = adi_launch<T>(F, D, 1);
-    k_adi_x<T><<<A.gx, A.wx, A.sx, s>>>(D, fr, 1);
-    k_adi_y<T><<<A.gy, A.wy, A.sy, s>>>(D, 1);
-    k_adi_z<T><<<A.gz, A.wz, A.sz, s>>>(D, fr, 1);
+    adi_step<T>(A, D, fr, 1, 1, s);
   } else {
     if (sizeof(T) == 4)   // one field (type 0) of npts values
       k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
-    const dim3 g((D.nlines + FILM_THREADS - 1) / FILM_THREADS, 1);
-    k_film1d_chains<T><<<g, FILM_THREADS, 0, s>>>(D, fr);
+    launch_chains_1d<T>(D, fr, 1, s);
   }
   k_convert<double, T><<<std::max<size_t>(1, (n + 255) / 256), 256, 0, s>>>(D.q + n, d_prop, n);
   CK(cudaGetLastError());

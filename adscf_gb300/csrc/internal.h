@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <string>
 #include <vector>
 
@@ -105,6 +106,16 @@ struct adscf_ctx {
   int adj_ckpt = 0;             // adjoint checkpoint interval (0: every slice stored, < 0: ceil(sqrt(Ns)))
   bool slices_full = true;      // all Ns + 1 propagator slices held (bulk_hold_slices)
 };
+
+// NVTX range over an entry point (header-only NVTX v3: without a profiler
+// attached each push / pop is a cheap no-op)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define ADSCF_RANGE(name) NvtxRange adscf_nvtx_range_(name)
 
 // errors
 int set_err(adscf_ctx* c, int code, const std::string& msg);
