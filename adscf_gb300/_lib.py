@@ -104,6 +104,7 @@ SIGNATURES = {
     "adscf_enqueue": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "adscf_stage_launches": (C.c_int, [C.c_void_p, C.c_int]),
     "adscf_set_wait_limit": (C.c_int, [C.c_void_p, C.c_int]),
+    "adscf_probe_l2_copy": (C.c_int, [C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     "adscf_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
     "adscf_set_pass_plan": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "adscf_forward": (C.c_int, [C.c_void_p, _dp, _dp]),
@@ -173,6 +174,13 @@ def check(lib, ctx, rc: int):
     if rc != ADSCF_OK:
         detail = lib.adscf_last_error(ctx).decode() if ctx else ""
         raise AdscfError(rc, f"{lib.adscf_status_string(rc).decode()} ({detail})")
+
+
+def c_double_out(fn, *args):
+    """Call fn(*args, &out) for an entry point with a trailing double*
+    result; None when it returns a non-zero status."""
+    out = C.c_double()
+    return out.value if fn(*args, C.byref(out)) == ADSCF_OK else None
 
 
 def dptr(a):

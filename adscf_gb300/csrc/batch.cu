@@ -67,6 +67,14 @@ struct adscf_batch {
   };
   std::vector<PassClass> cls;
   int maxns = 0, cont_blocks = 64, clos_grid = 0, mix_grid = 0;
+  // persistent sweep: items of every pass of every instance in dependency
+  // order, control words [next item, error flag, done count per instance]
+  int4* d_items = nullptr;
+  int nitems = 0;
+  int* d_ctl = nullptr;
+  int sweep_grid = 0;
+  size_t sweep_smem = 0;
+  bool sweep = true;                    // persistent sweep (ADSCF_BATCH_SWEEP=0: one launch per pass)
   cudaGraphExec_t g_iter = nullptr;
   double* h_pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -124,7 +132,10 @@ int nint_b(double x) { return x >= 0 ? (int)std::floor(x + 0.5) : -(int)std::flo
 
 int reg_tpl(int n) {
   switch (n) {
+    case 24: return regk::Cfg<24>::TPL;
     case 32: return regk::Cfg<32>::TPL;
+    case 40: return regk::Cfg<40>::TPL;
+    case 48: return regk::Cfg<48>::TPL;
     case 64: return regk::Cfg<64>::TPL;
     case 128: return regk::Cfg<128>::TPL;
     default: return regk::Cfg<256>::TPL;
@@ -133,11 +144,18 @@ int reg_tpl(int n) {
 template <typename T>
 size_t reg_smem(int n) {
   switch (n) {
+    case 24: return regk::Layout<T, 24>::bytes;
     case 32: return regk::Layout<T, 32>::bytes;
+    case 40: return regk::Layout<T, 40>::bytes;
+    case 48: return regk::Layout<T, 48>::bytes;
     case 64: return regk::Layout<T, 64>::bytes;
     case 128: return regk::Layout<T, 128>::bytes;
     default: return regk::Layout<T, 256>::bytes;
   }
+}
+// cubic grids whose lines run on the register FFT kernels in batches
+__host__ __device__ inline bool batch_reg_size(int g) {
+  return g == 24 || g == 32 || g == 40 || g == 48 || g == 64 || g == 128 || g == 256;
 }
 
 struct Carve {
@@ -159,6 +177,131 @@ int check_params(const adscf_params& q, int prec, std::string& why) {
   if (q.mixing_type == 3 && (q.mixing_dim < 1 || q.mixing_dim > SCF_MAX_HIST)) { why = "mixing_dim"; return ADSCF_E_ARG; }
   if (q.ensemble != 1 && q.ensemble != 2) { why = "ensemble"; return ADSCF_E_ARG; }
   return ADSCF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent sweep of a bulk batch: every line pass of every contour step of
+// every instance in one launch.  The host lists work items in dependency
+// order -- X of node 0, then per step t the Yf, Z, Yi and X passes -- with
+// the instances interleaved within each pass; an item is up to kSweepTiles
+// tiles of one pass of one instance and carries the number of items of that
+// instance listed before it.  Resident CTAs take items in list order from an
+// atomic counter, wait (bounded) until their instance has completed that many
+// items, run the pass's tile function, and count the item done with release
+// semantics.  Every item an item waits for was taken earlier by a resident
+// CTA that waits only on earlier items, so the sweep cannot deadlock; a wait
+// that runs out sets the error flag and ends its CTA, and the CTAs waiting on
+// it run out in turn.  The tile functions are those of the per-pass kernels,
+// so results are bit for bit those of the launch-per-pass schedule.
+// item: x instance, y first tile | ntiles << 20, z t << 3 | pass, w items before
+// ---------------------------------------------------------------------------
+enum { SW_XINIT = 0, SW_YF = 1, SW_Z = 2, SW_YI = 3, SW_X = 4 };
+constexpr int kSweepTiles = 8;
+constexpr int kSweepPolls = 1 << 22;
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// One tile of a pass, each (kernel class, pass) in a function of its own
+// (not inlined), so that every pass gets the kernel's whole register budget.
+template <typename T, int N, int KIND>
+__device__ __noinline__ void sweep_rs(const BulkDev<T>* insts, int2 w, int t, const cplx<T>* tw, const T* fk,
+                                      const double* g64, unsigned char* sm) {
+  rs_tile<T, N, KIND>(insts, w, tw, fk, nullptr, g64, t, sm);
+}
+template <typename T, int N>
+__device__ __noinline__ void sweep_rx(const BulkDev<T>* insts, int2 w, int t, int mode, const cplx<T>* tw,
+                                      unsigned char* sm) {
+  const XAux none{nullptr, nullptr, nullptr};
+  rx_tile<T, N>(insts, w, tw, t, mode, none, sm);
+}
+template <typename T, int N>
+__device__ __forceinline__ void sweep_reg(const BulkDev<T>* insts, int2 w, int pass, int t, const cplx<T>* tw,
+                                          const T* fk, const double* g64, unsigned char* sm) {
+  switch (pass) {
+    case SW_XINIT: sweep_rx<T, N>(insts, w, 0, XM_INIT, tw, sm); break;
+    case SW_YF: sweep_rs<T, N, 0>(insts, w, t, tw, fk, g64, sm); break;
+    case SW_Z: sweep_rs<T, N, 2>(insts, w, t, tw, fk, g64, sm); break;
+    case SW_YI: sweep_rs<T, N, 1>(insts, w, t, tw, fk, g64, sm); break;
+    default: sweep_rx<T, N>(insts, w, t, XM_STEP, tw, sm); break;
+  }
+}
+
+template <typename T>
+__device__ __noinline__ void sweep_gx(const BulkDev<T>* insts, int2 w, int t, int mode, const cplx<T>* tw,
+                                      unsigned char* sm) {
+  const XAux none{nullptr, nullptr, nullptr};
+  xpass_tile<T>(insts, w, tw, t, mode, none, sm);
+}
+template <typename T>
+__device__ __noinline__ void sweep_gs(const BulkDev<T>* insts, int2 w, int t, int kind, const cplx<T>* tw,
+                                      const T* fk, const double* g64, unsigned char* sm) {
+  strided_tile<T>(insts, w, tw, fk, nullptr, g64, t, kind, sm);
+}
+template <typename T>
+__device__ __forceinline__ void sweep_generic(const BulkDev<T>* insts, int2 w, int pass, int t, const cplx<T>* tw,
+                                              const T* fk, const double* g64, unsigned char* sm) {
+  if (pass == SW_XINIT) sweep_gx<T>(insts, w, 0, XM_INIT, tw, sm);
+  else if (pass == SW_X) sweep_gx<T>(insts, w, t, XM_STEP, tw, sm);
+  else sweep_gs<T>(insts, w, t, pass == SW_YF ? 0 : pass == SW_Z ? 2 : 1, tw, fk, g64, sm);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BULK_THREADS, 2)
+k_batch_sweep(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ items, int nitems,
+              int* __restrict__ ctl, const cplx<T>* __restrict__ tw, const T* __restrict__ fk,
+              const double* __restrict__ g64) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int s_k;
+  for (;;) {
+    __syncthreads();                     // the previous item is done with shared memory
+    if (threadIdx.x == 0) s_k = atomicAdd(&ctl[0], 1);
+    __syncthreads();
+    const int k = s_k;
+    if (k >= nitems) break;
+    const int4 it = items[k];
+    int* done = &ctl[2 + it.x];
+    bool ok = true;
+    if (threadIdx.x == 0) {
+      for (int i = 0; ld_acquire_gpu(done) < it.w; ++i) {
+        if (i >= kSweepPolls) { ok = false; break; }
+        __nanosleep(64);
+      }
+      if (!ok) atomicOr(&ctl[1], 1);
+    }
+    if (!__syncthreads_or(!ok)) {
+      ld_acquire_gpu(done);              // every thread's loads follow the producers' stores
+    } else {
+      break;
+    }
+    const int pass = it.z & 7, t = it.z >> 3;
+    const int tile0 = it.y & 0xfffff, nt = it.y >> 20;
+    const BulkDev<T>& I = insts[it.x];
+    const int n = I.gx;
+    const bool reg = I.gy == n && I.gz == n && batch_reg_size(n);
+    for (int j = 0; j < nt; ++j) {
+      if (j) __syncthreads();            // the tile function reuses shared memory
+      const int2 w = make_int2(it.x, tile0 + j);
+      switch (reg ? n : 0) {
+        case 24: sweep_reg<T, 24>(insts, w, pass, t, tw, fk, g64, smraw); break;
+        case 32: sweep_reg<T, 32>(insts, w, pass, t, tw, fk, g64, smraw); break;
+        case 40: sweep_reg<T, 40>(insts, w, pass, t, tw, fk, g64, smraw); break;
+        case 48: sweep_reg<T, 48>(insts, w, pass, t, tw, fk, g64, smraw); break;
+        case 64: sweep_reg<T, 64>(insts, w, pass, t, tw, fk, g64, smraw); break;
+        case 128: sweep_reg<T, 128>(insts, w, pass, t, tw, fk, g64, smraw); break;
+        case 256: sweep_reg<T, 256>(insts, w, pass, t, tw, fk, g64, smraw); break;
+        default: sweep_generic<T>(insts, w, pass, t, tw, fk, g64, smraw);
+      }
+    }
+    __syncthreads();                     // every thread's stores of the item are issued
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(done, 1);
+    }
+  }
 }
 
 template <typename T>
@@ -291,9 +434,9 @@ int build(adscf_batch* b) {
   auto class_of = [&](int i) {
     const BulkDev<T>& d = I[i];
     const int g = d.gx;
-    return (d.gy == g && d.gz == g && (g == 32 || g == 64 || g == 128 || g == 256)) ? g : 0;
+    return (d.gy == g && d.gz == g && batch_reg_size(g)) ? g : 0;
   };
-  for (int cn : {32, 64, 128, 256, 0}) {
+  for (int cn : {24, 32, 40, 48, 64, 128, 256, 0}) {
     adscf_batch::PassClass C;
     C.n = cn;
     std::vector<int2> wx, wy, wz;
@@ -331,6 +474,42 @@ int build(adscf_batch* b) {
     BK(cudaMemcpyAsync(C.wy, wy.data(), wy.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
     BK(cudaMemcpyAsync(C.wz, wz.data(), wz.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
   }
+  // items of the persistent sweep (k_batch_sweep): per step and pass, the
+  // instances still on their contour in the same order as the work lists
+  {
+    std::vector<int> tx(n), ty(n), tz(n), before(n, 0);
+    for (int i = 0; i < n; ++i) {
+      const BulkDev<T>& d = I[i];
+      const int cn = class_of(i);
+      const int lx = cn ? BULK_THREADS / reg_tpl(cn) : d.px.lpc;
+      const int ly = cn ? BULK_THREADS / reg_tpl(cn) : d.py.lpc;
+      const int lz = cn ? BULK_THREADS / reg_tpl(cn) : d.pz.lpc;
+      tx[i] = (d.gy * d.gz + lx - 1) / lx;
+      ty[i] = (d.gx * d.gz + ly - 1) / ly;
+      tz[i] = (d.gx * d.gy + lz - 1) / lz;
+    }
+    std::vector<int4> items;
+    auto add = [&](int i, int ntiles, int pass, int t) {
+      int k = 0;
+      for (int t0 = 0; t0 < ntiles; t0 += kSweepTiles, ++k) {
+        const int nt = std::min(kSweepTiles, ntiles - t0);
+        items.push_back(make_int4(i, t0 | (nt << 20), (t << 3) | pass, before[i]));
+      }
+      before[i] += k;
+    };
+    for (int i : ord) add(i, tx[i], SW_XINIT, 0);
+    for (int t = 1; t <= b->maxns; ++t) {
+      for (int pass : {SW_YF, SW_Z, SW_YI, SW_X})
+        for (int i : ord)
+          if (b->ns[i] >= t) add(i, pass == SW_X ? tx[i] : pass == SW_Z ? tz[i] : ty[i], pass, t);
+    }
+    b->nitems = (int)items.size();
+    BK(cudaMalloc(&b->d_items, items.size() * sizeof(int4)));
+    BK(cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
+    BK(cudaMalloc(&b->d_ctl, (2 + (size_t)n) * sizeof(int)));
+    BK(cudaMemsetAsync(b->d_ctl, 0, (2 + (size_t)n) * sizeof(int), b->stream));
+    if (const char* e = std::getenv("ADSCF_BATCH_SWEEP")) b->sweep = std::atoi(e) != 0;
+  }
   size_t smmax = 0;
   for (const auto& C : b->cls) smmax = std::max(smmax, std::max(C.smx, std::max(C.smy, C.smz)));
   int optin = 0;
@@ -344,8 +523,25 @@ int build(adscf_batch* b) {
   BK(cudaFuncSetAttribute(k_rs<T, NN, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));           \
   BK(cudaFuncSetAttribute(k_rs<T, NN, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));           \
   BK(cudaFuncSetAttribute(k_rs<T, NN, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  ADSCF_BATTR(32) ADSCF_BATTR(64) ADSCF_BATTR(128) ADSCF_BATTR(256)
+  ADSCF_BATTR(24) ADSCF_BATTR(32) ADSCF_BATTR(40) ADSCF_BATTR(48) ADSCF_BATTR(64) ADSCF_BATTR(128)
+  ADSCF_BATTR(256)
 #undef ADSCF_BATTR
+  {  // persistent sweep: resident CTAs with the largest tile layout of the batch
+     // (the kernel's static shared memory counts against the same limit)
+    cudaFuncAttributes fa{};
+    BK(cudaFuncGetAttributes(&fa, k_batch_sweep<T>));
+    b->sweep_smem = std::max<size_t>(smmax, 16);
+    int occ = 0, nsm = 0;
+    if (b->sweep_smem + fa.sharedSizeBytes > (size_t)optin) {
+      b->sweep = false;
+    } else {
+      BK(cudaFuncSetAttribute(k_batch_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->sweep_smem));
+      BK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_sweep<T>, BULK_THREADS, b->sweep_smem));
+    }
+    BK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev));
+    b->sweep_grid = std::max(1, occ) * nsm;
+    if (occ < 1) b->sweep = false;
+  }
   BK(cudaStreamSynchronize(b->stream));
   return ADSCF_OK;
 }
@@ -641,6 +837,9 @@ int enqueue_propagation(adscf_batch* b) {
   auto xpass = [&](const adscf_batch::PassClass& C, int grid, int t, int mode) {
     if (grid <= 0) return;
     switch (C.n) {
+      case 24: k_rx<T, 24><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
+      case 40: k_rx<T, 40><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
+      case 48: k_rx<T, 48><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
       case 32: k_rx<T, 32><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
       case 64: k_rx<T, 64><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
       case 128: k_rx<T, 128><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none); break;
@@ -648,6 +847,14 @@ int enqueue_propagation(adscf_batch* b) {
       default: k_bulk_xpass<T><<<grid, BULK_THREADS, C.smx, s>>>(d, C.wx, tw, t, mode, none);
     }
   };
+  if (b->sweep) {
+    BK(cudaMemsetAsync(b->d_ctl, 0, (2 + (size_t)b->n) * sizeof(int), s));
+    k_batch_sweep<T><<<b->sweep_grid, BULK_THREADS, b->sweep_smem, s>>>(d, b->d_items, b->nitems, b->d_ctl, tw,
+                                                                       fk, g64);
+    k_bulk_contour<T><<<dim3(b->cont_blocks, b->n), BULK_THREADS, 0, s>>>(d);
+    BK(cudaGetLastError());
+    return ADSCF_OK;
+  }
   auto spass = [&](const adscf_batch::PassClass& C, int t, int kind) {
     const bool z = kind == 2;
     const int grid = z ? C.pz[t] : C.py[t];
@@ -659,6 +866,9 @@ int enqueue_propagation(adscf_batch* b) {
   else if (kind == 1) k_rs<T, NN, 1><<<grid, BULK_THREADS, sm, s>>>(d, w, tw, fk, nullptr, g64, t); \
   else k_rs<T, NN, 2><<<grid, BULK_THREADS, sm, s>>>(d, w, tw, fk, nullptr, g64, t);
     switch (C.n) {
+      case 24: ADSCF_BS(24) break;
+      case 40: ADSCF_BS(40) break;
+      case 48: ADSCF_BS(48) break;
       case 32: ADSCF_BS(32) break;
       case 64: ADSCF_BS(64) break;
       case 128: ADSCF_BS(128) break;
@@ -728,6 +938,15 @@ int read_iters(adscf_batch* b, std::vector<int>& it) {
 }
 
 int read_results(adscf_batch* b, adscf_iter_result* out, double* max_acc) {
+  if (b->d_ctl) {   // a bounded wait of the persistent sweep expired
+    int f = 0;
+    BK(cudaMemcpyAsync(&f, b->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BK(cudaStreamSynchronize(b->stream));
+    if (f) {
+      BK(cudaMemsetAsync(b->d_ctl + 1, 0, sizeof(int), b->stream));
+      return berr(b, ADSCF_E_TIMEOUT, "a bounded wait of the persistent sweep expired");
+    }
+  }
   std::vector<double> r((size_t)b->n * R_COUNT);
   BK(cudaMemcpyAsync(r.data(), b->d_resall, r.size() * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
   BK(cudaStreamSynchronize(b->stream));
@@ -1047,6 +1266,7 @@ int adscf_batch_destroy(adscf_batch* b) {
   cudaFree(b->d_tw); cudaFree(b->d_fk); cudaFree(b->d_g64);
   for (auto& C : b->cls) { cudaFree(C.wx); cudaFree(C.wy); cudaFree(C.wz); }
   cudaFree(b->d_f32); cudaFree(b->d_f64); cudaFree(b->d_list32); cudaFree(b->d_list64); cudaFree(b->d_items32);
+  cudaFree(b->d_items); cudaFree(b->d_ctl);
   cudaFree(b->d_tabf);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
@@ -1119,6 +1339,7 @@ int adscf_batch_results(adscf_batch* b, adscf_iter_result* out) {
 int adscf_batch_launches(const adscf_batch* b) {
   if (!b) return -1;
   if (b->film) return 2 * ((b->n32 > 0) + (b->n64 > 0)) + 3;
+  if (b->sweep) return 5;   // sweep, contour, closure, solve, mix (and a memset of the counters)
   int k = 4;   // contour, closure, solve, mix
   for (const auto& C : b->cls) {
     k += C.px[0] > 0;

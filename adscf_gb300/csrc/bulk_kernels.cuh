@@ -218,12 +218,12 @@ __device__ __forceinline__ void load_twiddles(cplx<T>* tw, const cplx<T>* gtw, c
 // ---------------------------------------------------------------------------
 // X pass: lines along x (contiguous rows).  work.y = row tile.
 // ---------------------------------------------------------------------------
+// One tile (LPC x-rows of instance w.x, tile w.y) of the X pass; every
+// thread of the block calls it (shared memory `smraw` per plan_smem).
 template <typename T>
-__global__ void __launch_bounds__(BULK_THREADS)
-k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
-             const cplx<T>* __restrict__ gtw, int t, int mode, XAux aux) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int2 w = work[blockIdx.x];
+__device__ __forceinline__ void xpass_tile(const BulkDev<T>* __restrict__ insts, const int2 w,
+                                           const cplx<T>* __restrict__ gtw, int t, int mode, XAux aux,
+                                           unsigned char* smraw) {
   const BulkDev<T> I = insts[w.x];
   if (mode == XM_STEP && t > I.ns) return;
   const Plan1D P = I.px;
@@ -343,6 +343,14 @@ k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work
     I.spec[base + e] = r2[(e / N) * P.ld + (e % N)];
 }
 
+template <typename T>
+__global__ void __launch_bounds__(BULK_THREADS)
+k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
+             const cplx<T>* __restrict__ gtw, int t, int mode, XAux aux) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  xpass_tile<T>(insts, work[blockIdx.x], gtw, t, mode, aux, smraw);
+}
+
 // ---------------------------------------------------------------------------
 // Y / Z passes: lines along a strided axis.  Lines are flattened as
 // L = o*gx + x (o = z for Y passes, y for Z passes); a tile is LPC
@@ -351,13 +359,11 @@ k_bulk_xpass(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work
 //   3: forward z only, 4: inverse z only
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(BULK_THREADS)
-k_bulk_strided(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
-               const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
-               const double2* __restrict__ gtw64, const double* __restrict__ g64,
-               int t, int kind) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int2 w = work[blockIdx.x];
+__device__ __forceinline__ void strided_tile(const BulkDev<T>* __restrict__ insts, const int2 w,
+                                             const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
+                                             const double2* __restrict__ gtw64,
+                                             const double* __restrict__ g64, int t, int kind,
+                                             unsigned char* smraw) {
   const BulkDev<T> I = insts[w.x];
   if (t > I.ns) return;
   const bool zdir = kind >= 2;
@@ -438,6 +444,16 @@ k_bulk_strided(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ wo
     const size_t b = (size_t)(L / I.gx) * ostride + (L % I.gx);
     I.spec[b + (size_t)j * es] = r[l * P.ld + j];
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BULK_THREADS)
+k_bulk_strided(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
+               const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
+               const double2* __restrict__ gtw64, const double* __restrict__ g64,
+               int t, int kind) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  strided_tile<T>(insts, work[blockIdx.x], gtw, fk, gtw64, g64, t, kind, smraw);
 }
 
 // ---------------------------------------------------------------------------

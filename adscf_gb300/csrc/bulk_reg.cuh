@@ -12,7 +12,10 @@ namespace regk {
 
 template <int N>
 struct Cfg;
+template <> struct Cfg<24> { static constexpr int R1 = 12, TPL = 2; };
 template <> struct Cfg<32> { static constexpr int R1 = 8, TPL = 4; };
+template <> struct Cfg<40> { static constexpr int R1 = 20, TPL = 2; };
+template <> struct Cfg<48> { static constexpr int R1 = 12, TPL = 4; };
 template <> struct Cfg<64> { static constexpr int R1 = 8, TPL = 8; };
 template <> struct Cfg<128> { static constexpr int R1 = 16, TPL = 8; };
 template <> struct Cfg<256> { static constexpr int R1 = 16, TPL = 16; };
@@ -31,6 +34,19 @@ struct Layout {
 };
 
 __device__ __forceinline__ int ilog2(int v) { return __ffs(v) - 1; }
+constexpr bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// line L = o * gx + x of a strided pass -> offset of its first point:
+// shifts for power-of-two line lengths (with a power-of-two gx), a division
+// for the others (cubic grids, gx = N)
+template <int N>
+__device__ __forceinline__ size_t line_base(int L, int gx, int lgx, size_t ostride) {
+  if constexpr (pow2(N)) return (size_t)(L >> lgx) * ostride + (L & (gx - 1));
+  else {
+    const int o = L / gx;
+    return (size_t)o * ostride + (L - o * gx);
+  }
+}
 
 }  // namespace regk
 
@@ -38,16 +54,14 @@ __device__ __forceinline__ int ilog2(int v) { return __ffs(v) - 1; }
 // X pass (rows along x).  Modes as k_bulk_xpass.
 // ---------------------------------------------------------------------------
 template <typename T, int N>
-__global__ void __launch_bounds__(BULK_THREADS)
-k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
-     const cplx<T>* __restrict__ gtw, int t, int mode, XAux aux) {
+__device__ __forceinline__ void rx_tile(const BulkDev<T>* __restrict__ insts, const int2 w,
+                                        const cplx<T>* __restrict__ gtw, int t, int mode, XAux aux,
+                                        unsigned char* smraw) {
   using LY = regk::Layout<T, N>;
   using F = typename LY::F;
   constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
-  extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smraw);
   cplx<T>* scr = reinterpret_cast<cplx<T>*>(smraw + LY::sc_off);
-  const int2 w = work[blockIdx.x];
   const BulkDev<T>& I = insts[w.x];
   const int ns = I.ns;
   if (mode == XM_STEP && t > ns) return;
@@ -136,23 +150,29 @@ k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
   }
 }
 
+template <typename T, int N>
+__global__ void __launch_bounds__(BULK_THREADS)
+k_rx(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
+     const cplx<T>* __restrict__ gtw, int t, int mode, XAux aux) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  rx_tile<T, N>(insts, work[blockIdx.x], gtw, t, mode, aux, smraw);
+}
+
 // ---------------------------------------------------------------------------
 // Strided passes (Y: KIND 0 fwd / 1 inv; Z: KIND 2 fwd*G*inv, 3 fwd, 4 inv).
 // Flattened lines L = o*gx + x; LPC consecutive lines per CTA.
 // ---------------------------------------------------------------------------
 template <typename T, int N, int KIND>
-__global__ void __launch_bounds__(BULK_THREADS, KIND == 2 ? 2 : 3)
-k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
-     const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
-     const double2* __restrict__ gtw64, const double* __restrict__ g64, int t) {
+__device__ __forceinline__ void rs_tile(const BulkDev<T>* __restrict__ insts, const int2 w,
+                                        const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
+                                        const double2* __restrict__ gtw64,
+                                        const double* __restrict__ g64, int t, unsigned char* smraw) {
   using LY = regk::Layout<T, N>;
   using F = typename LY::F;
   constexpr int R1 = F::R1, TPL = F::TPL, LPC = LY::LPC;
-  extern __shared__ __align__(16) unsigned char smraw[];
   cplx<T>* tw = reinterpret_cast<cplx<T>*>(smraw);
   T* gzs = reinterpret_cast<T*>(smraw + LY::tw_bytes);
   cplx<T>* scr = reinterpret_cast<cplx<T>*>(smraw + LY::sc_off);
-  const int2 w = work[blockIdx.x];
   const BulkDev<T>& I = insts[w.x];
   if (t > I.ns) return;
   constexpr bool zdir = KIND >= 2;
@@ -173,7 +193,7 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
   const int L = valid ? Lr : nlines - 1;
   const size_t es = zdir ? (size_t)gx * gy : (size_t)gx;
   const size_t ostride = zdir ? (size_t)gx : (size_t)gx * gy;
-  const size_t base = (size_t)(L >> lgx) * ostride + (L & (gx - 1));
+  const size_t base = regk::line_base<N>(L, gx, lgx, ostride);
   cplx<T>* sc = scr + line * F::LS;
   cplx<T>* spec = I.spec;
   cplx<T> v[R1];
@@ -236,6 +256,15 @@ k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
     __syncthreads();
     dc_pencil_store<T>(spec, es, N, dcp);
   }
+}
+
+template <typename T, int N, int KIND>
+__global__ void __launch_bounds__(BULK_THREADS, KIND == 2 ? 2 : 3)
+k_rs(const BulkDev<T>* __restrict__ insts, const int2* __restrict__ work,
+     const cplx<T>* __restrict__ gtw, const T* __restrict__ fk,
+     const double2* __restrict__ gtw64, const double* __restrict__ g64, int t) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  rs_tile<T, N, KIND>(insts, work[blockIdx.x], gtw, fk, gtw64, g64, t, smraw);
 }
 
 // ---------------------------------------------------------------------------

@@ -57,12 +57,66 @@ __device__ __forceinline__ void dft16(cplx<T>* v, int sg) {
   }
 }
 
+
+// v * W_R^m, W_R = exp(-i sg 2 pi / R), for the composite DFTs of 12 and 20
+// points (m compile-time after unrolling; cos and sin of 2 pi m / R from
+// their closed forms)
+template <typename T, int R>
+__device__ __forceinline__ cplx<T> twr(cplx<T> v, int m, int sg) {
+  constexpr double h = K_SQRT3_2;
+  constexpr double c12[10] = {1.0, h, 0.5, 0.0, -0.5, -h, -1.0, -h, -0.5, 0.0};
+  constexpr double s12[10] = {0.0, 0.5, h, 1.0, h, 0.5, 0.0, -0.5, -h, -1.0};
+  // angles of 18 degrees: cos 18 = sin 72, cos 36 = -cos 144, ...
+  constexpr double c20[13] = {1.0, K_S5_1, -K_C5_2, K_S5_2, K_C5_1, 0.0, -K_C5_1,
+                              -K_S5_2, K_C5_2, -K_S5_1, -1.0, -K_S5_1, K_C5_2};
+  constexpr double s20[13] = {0.0, K_C5_1, K_S5_2, -K_C5_2, K_S5_1, 1.0, K_S5_1,
+                              -K_C5_2, K_S5_2, K_C5_1, 0.0, -K_C5_1, -K_S5_2};
+  if (m == 0) return v;
+  const T c = (T)(R == 12 ? c12[m] : c20[m]);
+  const T s = (T)(R == 12 ? s12[m] : s20[m]);
+  return mk<T>(v.x * c + sg * v.y * s, v.y * c - sg * v.x * s);
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void dft_c(cplx<T>* v, int sg);
+
+// R = P Q points, natural order in and out (Cooley-Tukey: n = n1 + P n2,
+// k = k2 + Q k1): Q-point DFTs over n2, twiddles W_R^(n1 k2), P-point DFTs
+// over n1
+template <typename T, int P, int Q>
+__device__ __forceinline__ void dft_pq(cplx<T>* v, int sg) {
+  cplx<T> a[P][Q];
+#pragma unroll
+  for (int n1 = 0; n1 < P; ++n1) {
+    cplx<T> t[Q];
+#pragma unroll
+    for (int n2 = 0; n2 < Q; ++n2) t[n2] = v[n1 + P * n2];
+    dft_c<T, Q>(t, sg);
+#pragma unroll
+    for (int k2 = 0; k2 < Q; ++k2) a[n1][k2] = twr<T, P * Q>(t[k2], n1 * k2, sg);
+  }
+#pragma unroll
+  for (int k2 = 0; k2 < Q; ++k2) {
+    cplx<T> t[P];
+#pragma unroll
+    for (int n1 = 0; n1 < P; ++n1) t[n1] = a[n1][k2];
+    dft_c<T, P>(t, sg);
+#pragma unroll
+    for (int k1 = 0; k1 < P; ++k1) v[k2 + Q * k1] = t[k1];
+  }
+}
+
 template <typename T, int R>
 __device__ __forceinline__ void dft_c(cplx<T>* v, int sg) {
   if constexpr (R == 4) dft4<T>(v, sg);
   else if constexpr (R == 8) dft8<T>(v, sg);
   else if constexpr (R == 16) dft16<T>(v, sg);
   else if constexpr (R == 2) dft2<T>(v);
+  else if constexpr (R == 3) dft3<T>(v, sg);
+  else if constexpr (R == 5) dft5<T>(v, sg);
+  else if constexpr (R == 12) dft_pq<T, 4, 3>(v, sg);
+  else if constexpr (R == 20) dft_pq<T, 4, 5>(v, sg);
+  else static_assert(R == 4, "no register DFT of this size");
 }
 
 template <typename T, int R1_, int TPL_>

@@ -478,25 +478,83 @@ __global__ void k_film_fill(T* __restrict__ q, T* __restrict__ qd, int n) {
 // mod_diblock.f90:154) or integrator(qdag_0 q_N) (brush, mod_homopolymer.f90:
 // 226), with the per-plane weights wz.
 // ---------------------------------------------------------------------------
+// FP32 slices: each product q_s qdag_{N-s} is exact as a float pair (TwoProd),
+// the weight is split into a float pair staged in shared memory, and the sum
+// over s is compensated (float-float, ~48 bits): FP32 units instead of
+// GB300's narrow FP64 pipe, which two FP64 multiply-adds per node and point
+// would wait on.  FP64 slices keep plain FP64 accumulation.
+constexpr int kFilmContourChunk = 256;   // contour nodes per staged weight chunk
+
+__device__ __forceinline__ void ffw_add(float& sh, float& sl, float x, float y, float2 w) {
+  const float p = x * y;
+  const float e = fmaf(x, y, -p);                // x y = p + e exactly
+  const float t = p * w.x;
+  const float te = fmaf(p, w.x, -t);             // p wh = t + te exactly
+  const float lo = fmaf(e, w.x, fmaf(p, w.y, te));
+  const float s = sh + t;                        // TwoSum(sh, t)
+  const float bp = s - sh;
+  const float err = (sh - (s - bp)) + (t - bp);
+  sl += err + lo;
+  sh = s;
+}
+
 template <typename T>
 __device__ __forceinline__ void film_contour_body(const FilmDev<T>& F, int bid, int nb) {
   __shared__ double red[32];
   const int N = F.ns;
   const size_t np = F.npts;
   double qs = 0.0;
-  for (int p = bid * blockDim.x + threadIdx.x; p < F.npts; p += nb * blockDim.x) {
-    double a0 = 0.0, a1 = 0.0;
-    for (int s = 0; s <= N; ++s) {
-      const double pr = (double)F.q[(size_t)s * np + p] * (double)F.qd[(size_t)(N - s) * np + p];
-      a0 += F.wA[s] * pr;
-      if (F.ntypes == 2) a1 += F.wB[s] * pr;
+  if constexpr (sizeof(T) == 4) {
+    __shared__ float2 wsh[2][kFilmContourChunk];
+    for (int pb = bid * blockDim.x; pb < F.npts; pb += nb * blockDim.x) {   // uniform per block
+      const int p = pb + threadIdx.x;
+      const bool ok = p < F.npts;
+      float ah = 0.f, al = 0.f, bh = 0.f, bl = 0.f;
+      for (int s0 = 0; s0 <= N; s0 += kFilmContourChunk) {
+        const int cn = min(kFilmContourChunk, N + 1 - s0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cn; k += blockDim.x) {
+          const double wa = F.wA[s0 + k];
+          const float wah = (float)wa;
+          wsh[0][k] = make_float2(wah, (float)(wa - (double)wah));
+          const double wb = F.ntypes == 2 ? F.wB[s0 + k] : 0.0;
+          const float wbh = (float)wb;
+          wsh[1][k] = make_float2(wbh, (float)(wb - (double)wbh));
+        }
+        __syncthreads();
+        if (ok) {
+          for (int k = 0; k < cn; ++k) {
+            const int s = s0 + k;
+            const float x = F.q[(size_t)s * np + p], y = F.qd[(size_t)(N - s) * np + p];
+            ffw_add(ah, al, x, y, wsh[0][k]);
+            if (F.ntypes == 2) ffw_add(bh, bl, x, y, wsh[1][k]);
+          }
+        }
+      }
+      if (ok) {
+        F.dist[p] = (double)ah + (double)al;
+        if (F.ntypes == 2) F.dist[np + p] = (double)bh + (double)bl;
+        const int z = p / F.nlines;
+        double qn = (double)F.q[(size_t)N * np + p];
+        if (F.brush) qn *= (double)F.qd[p];
+        qs += F.wz[z] * qn;
+      }
     }
-    F.dist[p] = a0;
-    if (F.ntypes == 2) F.dist[np + p] = a1;
-    const int z = p / F.nlines;
-    double qn = (double)F.q[(size_t)N * np + p];
-    if (F.brush) qn *= (double)F.qd[p];
-    qs += F.wz[z] * qn;
+  } else {
+    for (int p = bid * blockDim.x + threadIdx.x; p < F.npts; p += nb * blockDim.x) {
+      double a0 = 0.0, a1 = 0.0;
+      for (int s = 0; s <= N; ++s) {
+        const double pr = (double)F.q[(size_t)s * np + p] * (double)F.qd[(size_t)(N - s) * np + p];
+        a0 += F.wA[s] * pr;
+        if (F.ntypes == 2) a1 += F.wB[s] * pr;
+      }
+      F.dist[p] = a0;
+      if (F.ntypes == 2) F.dist[np + p] = a1;
+      const int z = p / F.nlines;
+      double qn = (double)F.q[(size_t)N * np + p];
+      if (F.brush) qn *= (double)F.qd[p];
+      qs += F.wz[z] * qn;
+    }
   }
   const double tot = block_reduce_1(qs, red);
   if (threadIdx.x == 0) F.qpart[bid] = tot;

@@ -275,6 +275,27 @@ k_film1d_warp_b(const FilmDev<float>* __restrict__ Fs, const ScfDev* __restrict_
 // x and y systems are the reference's periodic ones (cyclicTriDiag, :149-176)
 // solved with the reduced system closed cyclically.  blockIdx.y = chain.
 // ---------------------------------------------------------------------------
+// Per-chain FP32 coefficients of a step, formed once per block in FP64 (as
+// k_adi_x / k_adi_y form them per thread) and shared: every thread forming
+// them would keep GB300's narrow FP64 pipe busy for the whole sweep.
+struct AdiCoef {
+  float ax, bx, ay, by, dsf, hdsf;
+};
+__device__ __forceinline__ AdiCoef adi_coef(const FilmDev<float>& F, int dir, int s) {
+  __shared__ AdiCoef cs;
+  if (threadIdx.x == 0) {
+    const double ds = film_ds(F.dss, dir, s, F.ns);
+    cs.ax = (float)(-ds / F.dx / F.dx / 2.0);
+    cs.bx = (float)(ds / F.dx / F.dx);
+    cs.ay = (float)(-ds / F.dy / F.dy / 2.0);
+    cs.by = (float)(ds / F.dy / F.dy);
+    cs.dsf = (float)ds;
+    cs.hdsf = (float)(0.5 * ds);
+  }
+  __syncthreads();
+  return cs;
+}
+
 template <int G, int K>
 __global__ void __launch_bounds__(128)
 k_adi_x_w(FilmDev<float> F, int s) {
@@ -285,15 +306,15 @@ k_adi_x_w(FilmDev<float> F, int s) {
   const int dir = blockIdx.y;
   const bool live = id < gy * (gz - 1);
   const int y = live ? id % gy : 0, z = live ? 1 + id / gy : 1;
-  const double ds = film_ds(F.dss, dir, s, F.ns);
-  const CnStep st = cn_step(ds);
+  const AdiCoef cf = adi_coef(F, dir, s);
   const int ty = (F.brush || F.single) ? 0 : film_type(dir, s, F.ns, F.na);
   const float* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;
   float* out = F.w1 + (size_t)dir * F.npts;
   const float* wf = F.wf + (size_t)ty * F.npts;
-  const float ax = (float)(-ds / F.dx / F.dx / 2.0), bx = (float)(ds / F.dx / F.dx), cx = ax;
-  const float ay = (float)(-ds / F.dy / F.dy / 2.0), cy = ay;
-  const float az = (float)(-ds * F.alpha[z]), cz = (float)(-ds * F.gamma[z]);
+  const float ax = cf.ax, bx = cf.bx, cx = ax;
+  const float ay = cf.ay, cy = ay;
+  // z couplings as the z sweep forms them (cn_row, FP32 mesh factors)
+  const float az = __fmul_rn(-cf.dsf, F.alf[z]), cz = __fmul_rn(-cf.dsf, F.gaf[z]);
   const int ym = (y + gy - 1) % gy, yp = (y + 1) % gy;
   const size_t row = (size_t)z * L + (size_t)y * gx, rym = (size_t)z * L + (size_t)ym * gx,
                ryp = (size_t)z * L + (size_t)yp * gx, rzm = row - L, rzp = row + L;
@@ -314,7 +335,7 @@ k_adi_x_w(FilmDev<float> F, int s) {
     if (live) {
       qym = __ldg(p0 + rym + x); qyp = __ldg(p0 + ryp + x);
       qzm = __ldg(p0 + rzm + x); qzp = __ldg(p0 + rzp + x);
-      dsw = st.dsf * wf[row + x];
+      dsw = cf.dsf * wf[row + x];
     }
     const float q0 = c0[i];
     r[i] = -2.f * (ax * (qxm - q0) + cx * (qxp - q0) + ay * (qym - q0) + cy * (qyp - q0) +
@@ -338,10 +359,10 @@ k_adi_y_w(FilmDev<float> F, int s) {
   const int dir = blockIdx.y;
   const bool live = id < gx * (gz - 1);
   const int x = live ? id % gx : 0, z = live ? 1 + id / gx : 1;
-  const double ds = film_ds(F.dss, dir, s, F.ns);
+  const AdiCoef cf = adi_coef(F, dir, s);
   const float* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;
   float* w1 = F.w1 + (size_t)dir * F.npts;
-  const float ay = (float)(-ds / F.dy / F.dy / 2.0), by = (float)(ds / F.dy / F.dy), cy = ay;
+  const float ay = cf.ay, by = cf.by, cy = ay;
   const size_t col = (size_t)z * L + x;
   const int y0 = gl * K;
   // e = q - q* at the lane's points; q* kept for the write-back
@@ -380,7 +401,8 @@ k_adi_z_w(FilmDev<float> F, int s) {
   const int dir = blockIdx.y;
   const bool live = line0 < L;
   const int line = live ? line0 : 0;
-  const CnStep st = cn_step(film_ds(F.dss, dir, s, F.ns));
+  const AdiCoef cf = adi_coef(F, dir, s);
+  const CnStep st{0.0, cf.dsf, cf.hdsf};
   const int ty = (F.brush || F.single) ? 0 : film_type(dir, s, F.ns, F.na);
   const float* wl = F.wf + (size_t)ty * F.npts;
   const float* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;

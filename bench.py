@@ -44,6 +44,10 @@ SEED = 3
 # DRAM bytes of one 128^3 FP32 double step (Yf, Z, Yi, X launches), measured with
 # ncu on GB300: 17.53 MB, against 50.3 MB of algorithmic bytes (24 B per point)
 DSTEP_TRAFFIC = 17_531_648
+# L2 traffic of one 128^3 double step from the SM side, measured with ncu
+# (lts__t_sectors_srcunit_tex.sum x 32 B of one launch each of the fused XY
+# plane pass, 2,803,707 sectors, and of the TMA Z pass, 1,247,065 sectors)
+DSTEP_L2_BYTES = (2_803_707 + 1_247_065) * 32
 
 
 def c3_fields(n=GRID, length=L, seed=SEED):
@@ -469,6 +473,25 @@ def batch_legs(torch, A, stream, args, world=1, rank=0):
     return out
 
 
+def run_profile_workload(name):
+    """One SCF iteration of a film or batch workload for a launch list:
+    c4 (Film_3D, 64 x 64 x 65, ADI), c2 (4096 films), c5 (256 bulk
+    instances), after two untimed iterations."""
+    import adscf_gb300 as A
+    if name == "c4":
+        kw, w = c4_film3d(A)
+        with A.Context(A.FILM_3D, **kw) as c:
+            c.set_field(w)
+            c.scf_run(3)
+    else:
+        inst, fields = c2_films(A) if name == "c2" else c5_bulk(A)
+        with A.Batch(inst) as b:
+            b.set_fields(fields)
+            b.scf_run(3)
+    print(f"profile run {name} done")
+    return 0
+
+
 def run_profile(pass_plan=None):
     """One SCF iteration's stages at 128^3, ds = 0.05 (20 contour steps, 340 MB
     of slices) on the split path: the kernels of the bench, few launches.
@@ -505,14 +528,18 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--saddle-iters", type=int, default=800,
                     help="split-path iterations toward the saddle for the converged parity")
-    ap.add_argument("--profile", action="store_true",
-                    help="small run for ncu: one propagation, contour and update of the "
-                         "split path at 128^3 with 20 contour steps")
+    ap.add_argument("--profile", nargs="?", const="bulk", default=None,
+                    choices=["bulk", "c4", "c2", "c5"],
+                    help="small run for ncu: bulk (default) = one propagation, contour and "
+                         "update of the split path at 128^3 with 20 contour steps; c4 / c2 / c5 = "
+                         "three SCF iterations of that workload")
     ap.add_argument("--pass-plan", default=None,
                     help="with --profile: pin the Y, Z, X pass kernels, e.g. 2,2,3 "
                          "(0 plain, 1 persistent, 2 TMA, 3 fused XY)")
     args = ap.parse_args()
     if args.profile:
+        if args.profile != "bulk":
+            return run_profile_workload(args.profile)
         plan = tuple(int(v) for v in args.pass_plan.split(",")) if args.pass_plan else None
         return run_profile(plan)
     if args.warmup < 3:
@@ -596,6 +623,7 @@ def main():
     hbm, peak_kind = peaks()
     achieved = alg_dstep / (t_dstep * 1e-3) / 1e9
     alg_contour = 8 * (ns + 1) * npts + 16 * npts   # read all FP32 slices, write FP64 phi
+    l2_peak = L_.c_double_out(lib.adscf_probe_l2_copy, 24 << 20, 50)
 
     # ---- end to end through the C ABI with host buffers ---------------------
     # page-locked host buffers: the call copies them by DMA directly
@@ -651,7 +679,15 @@ def main():
                                        "over the four passes of one 128^3 double step "
                                        "(--cache-control none; Boltzmann factors and spectrum "
                                        "stay in L2, only the slice store reaches DRAM)",
-                     "contour_GBs": alg_contour / (t_cont * 1e-3) / 1e9},
+                     "contour_GBs": alg_contour / (t_cont * 1e-3) / 1e9,
+                     "l2": {"bytes_per_double_step": DSTEP_L2_BYTES,
+                            "achieved_gbs": DSTEP_L2_BYTES / (t_dstep * 1e-3) / 1e9,
+                            "peak_gbs": l2_peak,
+                            "frac": (DSTEP_L2_BYTES / (t_dstep * 1e-3) / 1e9) / l2_peak if l2_peak else None,
+                            "peak_source": "adscf_probe_l2_copy: copy of two 24 MiB buffers "
+                                           "(L2-resident), read + write bytes",
+                            "bytes_source": "ncu lts__t_sectors_srcunit_tex.sum x 32 B, one launch "
+                                            "each of the XY and Z passes at 128^3"}},
         "pass_plan": pass_plan,
         "clocks": clk,
         "gpu_launches": launches_per_step * args.steps,

@@ -370,6 +370,14 @@ ADSCF_API int adscf_batch_launches(const adscf_batch *b);
 ADSCF_API int adscf_batch_forward(adscf_batch *b, const double *fields, double *free_energy);
 ADSCF_API int adscf_batch_backward(adscf_batch *b, double *grad);
 
+/* Measurement helper of the benchmark, no reference counterpart: copy
+ * bandwidth (read + write bytes per second, in GB/s) of two buffers of
+ * `bytes` each (1 MiB .. 256 MiB) on the current device: one launch
+ * copies the buffer `reps` times after a launch that copies it twice;
+ * below half the L2 size both buffers stay L2-resident, so this is the L2
+ * bandwidth a streaming kernel sees.                                       */
+ADSCF_API int adscf_probe_l2_copy(long long bytes, int reps, double *gbs);
+
 /* ---- allocation-free propagator step ----------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (a pre-partitioned or quota-limited GPU, a driver that owns every

@@ -107,3 +107,25 @@ def test_batch_converges_every_instance(rng):
     assert all(r.accuracy <= 1e-8 for r in res)
     assert all(r.status == 0 for r in res)
     assert res[0].iter < 3000              # stopped once every instance was converged
+
+
+@pytest.mark.parametrize("prec", [SPLIT, FP64])
+def test_persistent_sweep_matches_launch_per_pass(rng, prec, monkeypatch):
+    """The persistent sweep (every pass of every instance in one launch) runs
+    the same tile functions as the launch-per-pass schedule, so three SCF
+    iterations give the same bits; it takes at most a handful of launches."""
+    w = start_fields(rng)
+    insts = [with_common(inst, prec, MIX_ANDERSON) for inst in INSTANCES]
+    out = {}
+    for sweep in ("1", "0"):
+        monkeypatch.setenv("ADSCF_BATCH_SWEEP", sweep)
+        with Batch(insts) as b:
+            b.set_fields(w)
+            res = b.scf_run(3)
+            out[sweep] = (b.get_fields(), [r.free_energy for r in res], b.lib.adscf_batch_launches(b.h))
+    f1, F1, l1 = out["1"]
+    f0, F0, l0 = out["0"]
+    assert l1 <= 10 < l0
+    assert F1 == F0
+    for a, c in zip(f1, f0):
+        assert np.array_equal(a, c)
