@@ -107,6 +107,7 @@ SIGNATURES = {
     "adscf_probe_l2_copy": (C.c_int, [C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     "adscf_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
     "adscf_set_pass_plan": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "adscf_set_adi_plan": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]),
     "adscf_forward": (C.c_int, [C.c_void_p, _dp, _dp]),
     "adscf_backward": (C.c_int, [C.c_void_p, _dp]),
     "adscf_forward_dev": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),

@@ -705,6 +705,17 @@ int adscf_tuning(const adscf_ctx* ctx, char* buf, int len) {
   return ADSCF_OK;
 }
 
+int adscf_set_adi_plan(adscf_ctx* ctx, int x_lanes, int y_lanes, int z_lanes, int staged) {
+  if (!ctx) return ADSCF_E_ARG;
+  const int lanes[3] = {x_lanes, y_lanes, z_lanes};
+  const int rc = ctx->film ? film_set_adi_plan(ctx, lanes, staged) : ADSCF_E_STATE;
+  if (rc == ADSCF_E_STATE) return set_err(ctx, rc, "ADI plans are for Film_3D contexts with FP32 sweeps");
+  if (rc) return set_err(ctx, rc, "no warp-solver shape with that many lanes for these lines");
+  if (ctx->g_iter) { cudaGraphExecDestroy(ctx->g_iter); ctx->g_iter = nullptr; }
+  if (ctx->g_prop) { cudaGraphExecDestroy(ctx->g_prop); ctx->g_prop = nullptr; }
+  return ADSCF_OK;
+}
+
 int adscf_set_pass_plan(adscf_ctx* ctx, int y, int z, int x) {
   if (!ctx) return ADSCF_E_ARG;
   if (ctx->geometry != ADSCF_BULK) return set_err(ctx, ADSCF_E_STATE, "pass plans are for bulk contexts");

@@ -1,7 +1,12 @@
 // film.cu -- film (Film_1D, Film_3D) and brush contexts: meshes, contour
 // schedules, weights and launch sequences.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
 #include <vector>
 
 #include "film_host.h"
@@ -20,6 +25,7 @@ struct FilmState {
   double* d_wA = nullptr;
   double* d_wB = nullptr;
   double* d_graft = nullptr;
+  float* d_adicf = nullptr;     // FP32 ADI coefficients per schedule entry [ns+3][6]
   float* d_alf = nullptr;       // FP32 mesh factors and field of FP32 line sweeps
   float* d_wf = nullptr;
   void* d_q = nullptr;
@@ -34,17 +40,35 @@ struct FilmState {
   double* d_fe_part = nullptr;  // [nplanes][FE_N]
   double* d_fe_out = nullptr;   // [2 + ntypes*nplanes]
   long long fe_gen = -1;
+  // FP32 ADI sweeps x, y, z: warp-solver shape of each (g = 0: one thread
+  // per line), from the autotuner or the defaults
+  AdiShape adi[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  bool adi_set = false;
 };
 
-// warp-cooperative FP32 ADI sweeps (film_adi.cu)
-int adi_warp_mask(const FilmDev<float>& D);
-void adi_x_warp(const FilmDev<float>& D, int step, int chains, cudaStream_t s);
-void adi_y_warp(const FilmDev<float>& D, int step, int chains, cudaStream_t s);
-void adi_z_warp(const FilmDev<float>& D, int step, int chains, cudaStream_t s);
+// warp-cooperative FP32 ADI sweeps (film_adi.cu); dim 0: x, 1: y, 2: z
+std::vector<AdiShape> adi_shapes(int dim, const FilmDev<float>& D);
+AdiShape adi_default_shape(int dim, const FilmDev<float>& D);
+void adi_warp_sweep(int dim, AdiShape sh, const FilmDev<float>& D, int step, int chains, cudaStream_t s);
 
 namespace {
 
 int nint_f(double x) { return x >= 0 ? (int)std::floor(x + 0.5) : -(int)std::floor(-x + 0.5); }
+
+// FP32 ADI coefficients of step sizes ds[0..n): ax, bx, ay, by, ds, ds/2 per
+// step, in the FP64 expressions of the per-thread sweeps
+void adi_coef_rows(const double* ds, int n, double dx, double dy, float* out) {
+  for (int k = 0; k < n; ++k) {
+    const double h = ds[k];
+    float* c = out + 6 * k;
+    c[0] = (float)(-h / dx / dx / 2.0);
+    c[1] = (float)(h / dx / dx);
+    c[2] = (float)(-h / dy / dy / 2.0);
+    c[3] = (float)(h / dy / dy);
+    c[4] = (float)h;
+    c[5] = (float)(0.5 * h);
+  }
+}
 
 template <typename T>
 FilmDev<T>& fdev(FilmState* F);
@@ -71,6 +95,7 @@ struct AdiLaunch {
   dim3 gx, gy, gz;
   int wx, wy, wz;
   size_t sx, sy, sz;
+  AdiShape sh[3];   // FP32 warp-solver shapes (g = 0: the kernels above)
 };
 template <typename T>
 AdiLaunch adi_launch(const FilmState* F, const FilmDev<T>& D, int chains) {
@@ -90,22 +115,121 @@ AdiLaunch adi_launch(const FilmState* F, const FilmDev<T>& D, int chains) {
   A.gx = dim3((D.gy * (D.gz - 1) + A.wx - 1) / A.wx, chains);
   A.gy = dim3((D.gx * (D.gz - 1) + A.wy - 1) / A.wy, chains);
   A.gz = dim3((D.nlines + A.wz - 1) / A.wz, chains);
+  for (int d = 0; d < 3; ++d) A.sh[d] = sizeof(T) == 4 ? F->adi[d] : AdiShape{0, 0, 0};
   return A;
 }
 
-// One Douglas ADI step (three sweeps) of `chains` chains: FP32 sweeps whose
-// lines fit run on the warp solver (film_adi.cu), the rest one thread per
-// line.
+// One sweep of a Douglas ADI step: the FP32 warp solver with the sweep's
+// shape, or the one-thread-per-line kernel.
+template <typename T>
+void adi_sweep(int dim, const AdiLaunch& A, const FilmDev<T>& D, const FieldRef& fr, int st, int chains,
+               cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (A.sh[dim].g) {
+      adi_warp_sweep(dim, A.sh[dim], D, st, chains, s);
+      return;
+    }
+  }
+  if (dim == 0) k_adi_x<T><<<A.gx, A.wx, A.sx, s>>>(D, fr, st);
+  else if (dim == 1) k_adi_y<T><<<A.gy, A.wy, A.sy, s>>>(D, st);
+  else k_adi_z<T><<<A.gz, A.wz, A.sz, s>>>(D, fr, st);
+}
+
+// One Douglas ADI step (three sweeps) of `chains` chains.
 template <typename T>
 void adi_step(const AdiLaunch& A, const FilmDev<T>& D, const FieldRef& fr, int st, int chains, cudaStream_t s) {
-  int m = 0;
-  if constexpr (sizeof(T) == 4) m = adi_warp_mask(D);
-  if constexpr (sizeof(T) == 4) { if (m & 1) adi_x_warp(D, st, chains, s); }
-  if (!(m & 1)) k_adi_x<T><<<A.gx, A.wx, A.sx, s>>>(D, fr, st);
-  if constexpr (sizeof(T) == 4) { if (m & 2) adi_y_warp(D, st, chains, s); }
-  if (!(m & 2)) k_adi_y<T><<<A.gy, A.wy, A.sy, s>>>(D, st);
-  if constexpr (sizeof(T) == 4) { if (m & 4) adi_z_warp(D, st, chains, s); }
-  if (!(m & 4)) k_adi_z<T><<<A.gz, A.wz, A.sz, s>>>(D, fr, st);
+  for (int d = 0; d < 3; ++d) adi_sweep<T>(d, A, D, fr, st, chains, s);
+}
+
+// Autotuner of the FP32 ADI sweeps, run once at context creation (outside
+// any stream capture): every warp-solver shape of each sweep and the
+// one-thread-per-line kernel are timed on this context's buffers (node 0
+// filled, a zero field) at step 1 with both chains, twice, four launches
+// each after one warm-up launch, with CUDA events on the context stream;
+// each sweep keeps its fastest.  The x sweep runs first and
+// the z sweep last, so every candidate reads finite values written by the
+// sweep before it.  Shapes are cached per (device, grid).  Shapes differ in
+// the order of the FP32 line-solve arithmetic (results agree to rounding);
+// ADSCF_AUTOTUNE=0 keeps the default shapes.
+struct AdiTuneKey {
+  int dev, gx, gy, gz;
+  bool operator<(const AdiTuneKey& o) const {
+    return std::tie(dev, gx, gy, gz) < std::tie(o.dev, o.gx, o.gy, o.gz);
+  }
+};
+struct AdiTuneVal {
+  AdiShape sh[3];
+  std::string report;
+};
+std::mutex g_adi_mu;
+std::map<AdiTuneKey, AdiTuneVal> g_adi_tune;
+
+void adi_defaults(FilmState* F, const FilmDev<float>& D) {
+  for (int d = 0; d < 3; ++d) F->adi[d] = adi_default_shape(d, D);
+  F->adi_set = true;
+}
+
+int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldRef& fr) {
+  const AdiTuneKey key{ctx->dev, D.gx, D.gy, D.gz};
+  {
+    std::lock_guard<std::mutex> lk(g_adi_mu);
+    auto it = g_adi_tune.find(key);
+    if (it != g_adi_tune.end()) {
+      for (int d = 0; d < 3; ++d) F->adi[d] = it->second.sh[d];
+      F->adi_set = true;
+      ctx->tune_report = it->second.report + " (cached)";
+      return ADSCF_OK;
+    }
+  }
+  cudaStream_t s = ctx->stream;
+  AdiLaunch A = adi_launch<float>(F, D, 2);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  std::string rep = "adi";
+  static const char* nm[3] = {"x", "y", "z"};
+  AdiTuneVal val;
+  for (int d = 0; d < 3; ++d) {
+    std::vector<AdiShape> cand = adi_shapes(d, D);
+    cand.push_back({0, 0, 0});
+    std::vector<float> us(cand.size(), 1e30f);
+    for (int round = 0; round < 2; ++round)
+      for (size_t c = 0; c < cand.size(); ++c) {
+        A.sh[d] = cand[c];
+        adi_sweep<float>(d, A, D, fr, 1, 2, s);
+        cudaEventRecord(e0, s);
+        for (int r = 0; r < 4; ++r) adi_sweep<float>(d, A, D, fr, 1, 2, s);
+        cudaEventRecord(e1, s);
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        us[c] = std::min(us[c], 250.f * ms);
+      }
+    size_t best = 0;
+    for (size_t c = 1; c < cand.size(); ++c)
+      if (us[c] < us[best]) best = c;
+    val.sh[d] = cand[best];
+    A.sh[d] = cand[best];   // the next sweep's candidates read this one's output
+    char line[96];
+    std::snprintf(line, sizeof(line), " %s=%dx%d%s", nm[d], cand[best].g, cand[best].k, cand[best].staged ? "s" : "");
+    rep += line;
+    for (size_t c = 0; c < cand.size(); ++c) {
+      std::snprintf(line, sizeof(line), " [%s %dx%d%s %.2f us]", nm[d], cand[c].g, cand[c].k,
+                    cand[c].staged ? "s" : "", us[c]);
+      rep += line;
+    }
+    rep += ";";
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaGetLastError());
+  for (int d = 0; d < 3; ++d) F->adi[d] = val.sh[d];
+  F->adi_set = true;
+  val.report = rep;
+  ctx->tune_report = rep;
+  std::lock_guard<std::mutex> lk(g_adi_mu);
+  g_adi_tune[key] = val;
+  return ADSCF_OK;
 }
 
 // 1D chains of every line: FP32 sweeps on lines of up to 32 * kFilmWarpM
@@ -136,6 +260,9 @@ int chains_t(adscf_ctx* ctx, const double* d_w) {
     if (sizeof(T) == 4) {
       const size_t n = (size_t)ctx->ntypes * D.npts;
       k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
+    }
+    if constexpr (sizeof(T) == 4) {
+      if (!F->adi_set) adi_defaults(F, D);
     }
     const AdiLaunch A = adi_launch<T>(F, D, 2);
     for (int st = 1; st <= D.ns; ++st) adi_step<T>(A, D, fr, st, 2, s);
@@ -168,6 +295,12 @@ int step_single_t(adscf_ctx* ctx, double* d_prop, const double* d_w, double ds) 
   double h_dss[2] = {0.0, ds};
   // a one-step schedule in the 2 spare entries past the contour schedule
   CK(cudaMemcpyAsync(F->d_dss + D.ns + 1, h_dss, sizeof(h_dss), cudaMemcpyHostToDevice, s));
+  if (F->d_adicf) {   // and its ADI coefficients
+    float h_cf[12];
+    adi_coef_rows(h_dss, 2, D.dx, D.dy, h_cf);
+    CK(cudaMemcpyAsync(F->d_adicf + 6 * (D.ns + 1), h_cf, sizeof(h_cf), cudaMemcpyHostToDevice, s));
+    D.adicf = F->d_adicf + 6 * (D.ns + 1);
+  }
   D.dss = F->d_dss + D.ns + 1;
   D.ns = 1;
   D.na = 1;
@@ -180,6 +313,9 @@ int step_single_t(adscf_ctx* ctx, double* d_prop, const double* d_w, double ds) 
   if (ctx->geometry == ADSCF_FILM_3D) {
     if (sizeof(T) == 4)   // one field (type 0) of npts values
       k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, s>>>(fr, D.wf, n);
+    if constexpr (sizeof(T) == 4) {
+      if (!F->adi_set) adi_defaults(F, fdev<float>(F));
+    }
     const AdiLaunch A = adi_launch<T>(F, D, 1);
     adi_step<T>(A, D, fr, 1, 1, s);
   } else {
@@ -218,6 +354,7 @@ void fill_dev(adscf_ctx* ctx, FilmState* F, const adscf_params* p) {
   D.span = p->int_span;
   D.alpha = F->d_alpha; D.beta = F->d_beta; D.gamma = F->d_gamma;
   D.dss = F->d_dss; D.wA = F->d_wA; D.wB = F->d_wB;
+  D.adicf = F->d_adicf;
   D.wz = ctx->d_wz;
   D.graft = F->d_graft;
   D.q = static_cast<T*>(F->d_q);
@@ -276,6 +413,12 @@ int film_create(adscf_ctx* ctx, const adscf_params* p) {
   CK(cudaMemcpy(F->d_beta, be.data(), (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(F->d_gamma, ga.data(), (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(F->d_dss, dss.data(), (ctx->ns + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  if (ctx->geometry == ADSCF_FILM_3D) {
+    std::vector<float> cf(6 * ((size_t)ctx->ns + 3), 0.f);
+    adi_coef_rows(dss.data(), ctx->ns + 1, p->sizex / p->gx, p->sizey / p->gy, cf.data());
+    CK(cudaMalloc(&F->d_adicf, cf.size() * sizeof(float)));
+    CK(cudaMemcpy(F->d_adicf, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   CK(cudaMemcpy(F->d_wA, wA.data(), (ctx->ns + 1) * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(F->d_wB, wB.data(), (ctx->ns + 1) * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_wz, wz.data(), (gz + 1) * sizeof(double), cudaMemcpyHostToDevice));
@@ -322,6 +465,40 @@ int film_create(adscf_ctx* ctx, const adscf_params* p) {
   else fill_dev<float>(ctx, F, p);
   ctx->film_launches = ctx->geometry == ADSCF_FILM_3D ? 1 + 3 * ctx->ns : 1;
   ctx->film_contour_launches = 1;
+  if (ctx->geometry == ADSCF_FILM_3D && !F->t64) {   // FP32 ADI sweeps: pick their shapes
+    FilmDev<float>& D = F->f32;
+    if (!ctx->autotune) {
+      adi_defaults(F, D);
+      return ADSCF_OK;
+    }
+    const size_t n = (size_t)ctx->ntypes * D.npts;
+    CK(cudaMemsetAsync(ctx->d_tmp, 0, n * sizeof(double), ctx->stream));
+    const FieldRef fr = make_ref(ctx, ctx->d_tmp);
+    k_film_fill<float><<<std::max(1, (D.npts + 255) / 256), 256, 0, ctx->stream>>>(D.q, D.qd, D.npts);
+    k_film_wconv<<<(int)std::min<size_t>((n + 255) / 256, 152 * 4), 256, 0, ctx->stream>>>(fr, D.wf, n);
+    CK(cudaGetLastError());
+    return adi_tune(ctx, F, D, fr);
+  }
+  return ADSCF_OK;
+}
+
+// Pin the FP32 ADI sweep shapes by lanes per line (0: one thread per line)
+// and staging through shared memory (mask: 2 y, 4 z).
+int film_set_adi_plan(adscf_ctx* ctx, const int lanes[3], int staged) {
+  FilmState* F = ctx->film;
+  if (ctx->geometry != ADSCF_FILM_3D || F->t64) return ADSCF_E_STATE;
+  AdiShape sh[3];
+  for (int d = 0; d < 3; ++d) {
+    sh[d] = {0, 0, 0};
+    const int st = (staged >> d) & 1;
+    if (lanes[d] == 0 && !st) continue;
+    bool found = false;
+    for (const AdiShape& a : adi_shapes(d, F->f32))
+      if (a.g == lanes[d] && a.staged == st) { sh[d] = a; found = true; }
+    if (!found) return ADSCF_E_ARG;
+  }
+  for (int d = 0; d < 3; ++d) F->adi[d] = sh[d];
+  F->adi_set = true;
   return ADSCF_OK;
 }
 
@@ -375,7 +552,7 @@ void film_destroy(adscf_ctx* ctx) {
   if (!F) return;
   cudaFree(F->d_fe_w); cudaFree(F->d_fe_part); cudaFree(F->d_fe_out);
   cudaFree(F->d_alpha); cudaFree(F->d_beta); cudaFree(F->d_gamma);
-  cudaFree(F->d_dss); cudaFree(F->d_wA); cudaFree(F->d_wB); cudaFree(F->d_graft);
+  cudaFree(F->d_dss); cudaFree(F->d_adicf); cudaFree(F->d_wA); cudaFree(F->d_wB); cudaFree(F->d_graft);
   cudaFree(F->d_alf); cudaFree(F->d_wf);
   cudaFree(F->d_q); cudaFree(F->d_qd); cudaFree(F->d_gam); cudaFree(F->d_w1);
   cudaFree(F->d_err); cudaFree(ctx->d_qpart);

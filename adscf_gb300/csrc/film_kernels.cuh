@@ -65,6 +65,9 @@ struct FilmDev {
   const float* bef;
   const float* gaf;
   float* wf;
+  // FP32 ADI sweeps: per contour-schedule entry k (ds = dss[k]) the FP32
+  // coefficients ax, bx, ay, by, ds, ds/2, formed in FP64 on the host
+  const float* adicf;
 };
 
 // ---------------------------------------------------------------------------

@@ -275,25 +275,23 @@ k_film1d_warp_b(const FilmDev<float>* __restrict__ Fs, const ScfDev* __restrict_
 // x and y systems are the reference's periodic ones (cyclicTriDiag, :149-176)
 // solved with the reduced system closed cyclically.  blockIdx.y = chain.
 // ---------------------------------------------------------------------------
-// Per-chain FP32 coefficients of a step, formed once per block in FP64 (as
-// k_adi_x / k_adi_y form them per thread) and shared: every thread forming
-// them would keep GB300's narrow FP64 pipe busy for the whole sweep.
+// Shape of a warp-solver sweep: G lanes per line, K points per lane (g = 0:
+// the one-thread-per-line kernels); staged: the tile goes through shared
+// memory (k_adi_yz_s, y and z sweeps).
+struct AdiShape {
+  int g, k, staged;
+};
+
+// Per-chain FP32 coefficients of a step, read from the context's table
+// (formed in FP64 on the host, rounded as k_adi_x / k_adi_y form them per
+// thread): forming them on the device would keep GB300's narrow FP64 pipe
+// and a block barrier on every sweep's critical path.
 struct AdiCoef {
   float ax, bx, ay, by, dsf, hdsf;
 };
 __device__ __forceinline__ AdiCoef adi_coef(const FilmDev<float>& F, int dir, int s) {
-  __shared__ AdiCoef cs;
-  if (threadIdx.x == 0) {
-    const double ds = film_ds(F.dss, dir, s, F.ns);
-    cs.ax = (float)(-ds / F.dx / F.dx / 2.0);
-    cs.bx = (float)(ds / F.dx / F.dx);
-    cs.ay = (float)(-ds / F.dy / F.dy / 2.0);
-    cs.by = (float)(ds / F.dy / F.dy);
-    cs.dsf = (float)ds;
-    cs.hdsf = (float)(0.5 * ds);
-  }
-  __syncthreads();
-  return cs;
+  const float* c = F.adicf + 6 * (dir == 0 ? s : F.ns + 1 - s);
+  return AdiCoef{__ldg(c), __ldg(c + 1), __ldg(c + 2), __ldg(c + 3), __ldg(c + 4), __ldg(c + 5)};
 }
 
 template <int G, int K>
@@ -446,4 +444,118 @@ k_adi_z_w(FilmDev<float> F, int s) {
       if (j < n) qn[(size_t)j * L + line] = (j > 0 && j < n - 1) ? wq[i] + r[i] : r[i];
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory staged y and z sweeps.  The y lines (stride gx) and z lines
+// (stride gx gy) run across x, so a warp that holds one line reads a
+// different 32-byte sector per lane.  Here a block takes a tile of 32
+// neighbouring lines (32 consecutive x of one plane for y, 32 consecutive
+// (y, x) lines for z), reads every row of the tile with 32 consecutive
+// floats per warp load, keeps the tile in shared memory (rows padded to 33
+// floats), solves its lines there with the warp solver (G lanes, K rows per
+// lane, 128 / G lines per round of the block's four warps) and writes the
+// tile back the same way.  Right-hand sides, matrices and the solver are
+// those of k_adi_y_w / k_adi_z_w; neighbour values come from shared memory
+// instead of shuffles.  Shared memory: (Z ? 3 : 2) n 33 floats.
+// ---------------------------------------------------------------------------
+constexpr int kAdiTile = 32;
+constexpr int kAdiPad = 33;
+
+__host__ __device__ constexpr size_t adi_staged_smem(int n, bool z) {
+  return (size_t)(z ? 3 : 2) * n * kAdiPad * sizeof(float);
+}
+
+template <int G, int K, bool Z>
+__global__ void __launch_bounds__(128)
+k_adi_yz_s(FilmDev<float> F, int s) {
+  static_assert(G >= 4, "four warps cover 32 lines per round at G >= 4");
+  extern __shared__ __align__(16) float smf[];
+  constexpr int LPW = 32 / G;
+  const int gx = F.gx, L = F.nlines;
+  const int n = Z ? F.gz + 1 : F.gy;
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, gl = lane & (G - 1);
+  size_t base, rstride;
+  int cnt;
+  if (Z) {
+    const int l0 = blockIdx.x * kAdiTile;
+    base = (size_t)l0;
+    rstride = (size_t)L;
+    cnt = min(kAdiTile, L - l0);
+  } else {
+    const int tx = (gx + kAdiTile - 1) / kAdiTile;
+    const int z = 1 + blockIdx.x / tx, x0 = (blockIdx.x % tx) * kAdiTile;
+    base = (size_t)z * L + x0;
+    rstride = (size_t)gx;
+    cnt = min(kAdiTile, gx - x0);
+  }
+  const int dir = blockIdx.y;
+  const AdiCoef cf = adi_coef(F, dir, s);
+  const float* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;
+  float* w1 = F.w1 + (size_t)dir * F.npts;
+  const int ty = (F.brush || F.single) ? 0 : film_type(dir, s, F.ns, F.na);
+  const float* wl = F.wf + (size_t)ty * F.npts;
+  float* sf = smf;                       // q - q** (z) or q - q* (y); then the result
+  float* sw = smf + n * kAdiPad;         // q** (z, 0 on the walls) or q*
+  float* sl = smf + 2 * n * kAdiPad;     // z: field of the step's type
+  for (int j = wp; j < n; j += 4) {
+    float f = 0.f, wq = 0.f, wv = 0.f;
+    if (lane < cnt) {
+      const size_t idx = base + (size_t)j * rstride + lane;
+      if (Z) {
+        wq = (j == 0 || j == n - 1) ? 0.f : __ldg(w1 + idx);
+        wv = __ldg(wl + idx);
+      } else {
+        wq = w1[idx];
+      }
+      f = __ldg(p0 + idx) - wq;
+    }
+    sf[j * kAdiPad + lane] = f;
+    sw[j * kAdiPad + lane] = wq;
+    if (Z) sl[j * kAdiPad + lane] = wv;
+  }
+  __syncthreads();
+  const CnStep st{0.0, cf.dsf, cf.hdsf};
+  const float ay = cf.ay, by = cf.by, cy = ay;
+#pragma unroll 1
+  for (int r0 = 0; r0 < kAdiTile; r0 += 4 * LPW) {
+    const int tl = r0 + wp * LPW + lane / G;   // line of the tile
+    const int j0 = gl * K;
+    float a[K], d[K], c[K], r[K], wq[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const int j = j0 + i;
+      a[i] = 0.f; d[i] = 1.f; c[i] = 0.f; r[i] = 0.f; wq[i] = 0.f;
+      if (j < n) {
+        const float f = sf[j * kAdiPad + tl];
+        wq[i] = sw[j * kAdiPad + tl];
+        if (Z) {
+          if (j > 0 && j < n - 1) {
+            const float fm = sf[(j - 1) * kAdiPad + tl], fp = sf[(j + 1) * kAdiPad + tl];
+            float ai, ci, bi, hw;
+            cn_row<float>(F, st, j, 0.0, sl[j * kAdiPad + tl], ai, ci, bi, hw);
+            a[i] = ai; c[i] = ci;
+            d[i] = 1.f + bi + hw;
+            r[i] = ai * (fm - f) + ci * (fp - f) + hw * f;
+          }
+        } else {
+          const float em = sf[(j == 0 ? n - 1 : j - 1) * kAdiPad + tl];
+          const float ep = sf[(j == n - 1 ? 0 : j + 1) * kAdiPad + tl];
+          r[i] = ay * (em - f) + cy * (ep - f);
+          a[i] = ay; c[i] = cy; d[i] = 1.f + by;
+        }
+      }
+    }
+    fw::solve<G, K>(a, d, c, r, !Z, F.err);
+    __syncwarp();   // every lane of the line has read its rows
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const int j = j0 + i;
+      if (j < n) sf[j * kAdiPad + tl] = (!Z || (j > 0 && j < n - 1)) ? wq[i] + r[i] : r[i];
+    }
+  }
+  __syncthreads();
+  float* out = Z ? (dir == 0 ? F.q : F.qd) + (size_t)s * F.npts : w1;
+  if (lane < cnt)
+    for (int j = wp; j < n; j += 4) out[base + (size_t)j * rstride + lane] = sf[j * kAdiPad + lane];
 }

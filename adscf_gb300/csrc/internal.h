@@ -151,6 +151,7 @@ int film_enqueue_propagate(adscf_ctx* ctx, const double* d_w);
 int film_enqueue_chains(adscf_ctx* ctx, const double* d_w);
 int film_enqueue_contour(adscf_ctx* ctx);
 int film_step_single(adscf_ctx* ctx, double* d_prop, const double* d_w, double ds);
+int film_set_adi_plan(adscf_ctx* ctx, const int lanes[3], int staged);   // FP32 ADI lanes per line (x, y, z)
 double* film_fe_field(adscf_ctx* ctx);                           // device buffer for the fields of film_forward
 int film_forward(adscf_ctx* ctx, double* out_F);                // F at fixed fields (films, brush)
 int film_backward(adscf_ctx* ctx, double* dF_dchi, double* dF_dU);

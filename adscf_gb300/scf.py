@@ -240,6 +240,13 @@ class Context:
         """Pin the kernel of the Y, Z and X passes (0 plain, 1 persistent, 2 TMA)."""
         self._ck(self.lib.adscf_set_pass_plan(self.h, int(y), int(z), int(x)))
 
+    def set_adi_plan(self, x_lanes, y_lanes, z_lanes, staged=0):
+        """Pin the lanes per line of the FP32 ADI sweeps of a Film_3D context
+        (0: one thread per line) and their staging through shared memory
+        (mask: 2 for y, 4 for z)."""
+        self._ck(self.lib.adscf_set_adi_plan(self.h, int(x_lanes), int(y_lanes), int(z_lanes),
+                                             int(staged)))
+
     # -- differentiation (FP64 bulk) ----------------------------------------
     def forward(self, field):
         """Free energy per chain at `field` [ntypes][npts], no mixing; keeps

@@ -250,6 +250,21 @@ enum { ADSCF_PASS_PLAIN = 0, ADSCF_PASS_PERSISTENT = 1, ADSCF_PASS_TMA = 2,
 ADSCF_API int adscf_tuning(const adscf_ctx *ctx, char *buf, int len);
 ADSCF_API int adscf_set_pass_plan(adscf_ctx *ctx, int y, int z, int x);
 
+/* ---- ADI sweep autotuner (Film_3D, FP32 sweeps) -------------------------
+ * No reference counterpart.  Each Douglas ADI sweep (x, y, z lines) runs on
+ * a warp solver with G lanes per line and K points per lane -- for the y and
+ * z lines optionally staged through shared memory in tiles of 32 lines, so
+ * that global accesses are coalesced -- or on one thread per line.  At
+ * context creation every shape that fits the lines is timed on the
+ * context's buffers and each sweep keeps its fastest (cached per device and
+ * grid; ADSCF_AUTOTUNE=0 keeps the defaults).  Shapes order the FP32
+ * line-solve arithmetic differently, so results agree to FP32 rounding, not
+ * bit for bit.  adscf_tuning reports the choice and the timings ("GxK", "s"
+ * for staged); adscf_set_adi_plan pins lanes per line for each sweep (0: one
+ * thread per line) and staging (mask: 2 y, 4 z); ADSCF_E_ARG if no shape
+ * matches, ADSCF_E_STATE for other contexts.                               */
+ADSCF_API int adscf_set_adi_plan(adscf_ctx *ctx, int x_lanes, int y_lanes, int z_lanes, int staged);
+
 /* ---- differentiation (bulk, FP64 context, canonical ensemble) ----------
  * No counterpart in the reference, which has no derivatives; it replaces
  * the reference's practice of differencing converged free energies of

@@ -1,6 +1,8 @@
 """Film (Film_1D CN, Film_3D Douglas ADI) and brush propagators on the GPU,
 through the C ABI, against the FP64 oracle (oracle/film.py).  Tolerances:
 FP64 relative 1e-11; split (FP32 sweeps on a mildly graded mesh) 2e-5."""
+import re
+
 import numpy as np
 import pytest
 
@@ -121,6 +123,58 @@ def test_film3d_split_precision(rng):
         dens, res = c.propagate_diblock(field)
     assert abs(np.log(res.Qsum) - np.log(ref["Qsum"])) < 2e-6
     assert np.max(np.abs(dens - ref["density"])) < 2e-6 * np.max(np.abs(ref["density"]))
+
+
+def _adi_shapes(n, periodic, stageable, z):
+    """(lanes, staged) of the warp-solver shapes for a line of n points, as
+    the library enumerates them, plus (0, 0): one thread per line."""
+    out = []
+    for g in (2, 4, 8, 16, 32):
+        if periodic:
+            ok = any(n == g * k for k in (2, 4))
+        else:
+            k = max(2, -(-n // g))
+            ok = k <= 4 or (k <= 8 and g >= 8)
+        if ok:
+            out.append((g, 0))
+    if stageable and (3 if z else 2) * n * 33 * 4 <= 46 * 1024:
+        out += [(g, 1) for g, _ in list(out) if g >= 4]
+    return out + [(0, 0)]
+
+
+def test_film3d_every_adi_shape_vs_oracle(rng):
+    """Every ADI sweep shape the autotuner may pick (warp solver with each
+    lane count, staged through shared memory or not, and one thread per
+    line), one sweep at a time with the other two at the tuner's choice,
+    against the FP64 oracle; the tuner's report names a shape per sweep."""
+    gx, gy, gz, ds = 16, 32, 24, 0.01
+    dz, zr = of.generate_mesh(0, gz, 3.0)
+    size = (3.2, 4.0, 3.0)
+    field = 0.5 * rng.standard_normal((2, gz + 1, gy, gx))
+    dss = np.r_[0.0, np.full(60, ds)]   # blocks of 15 and 45 steps
+    step = lambda p, w, h: of.adi_step_3d(p, w, dz, size[0] / gx, size[1] / gy, h)
+    ref = of.film_propagate_diblock(field, dz, dss, 15, step, dx=size[0] / gx,
+                                    dy=size[1] / gy, int_scheme=1, span="full", sizes=size)
+    with film_ctx(FILM_3D, (gx, gy, gz), dz, size, ds, f=(0.15, 0.45), prec=SPLIT) as c:
+        rep = c.tuning()
+        chosen = re.findall(r"\b([xyz])=(\d+)x(\d+)(s?)", rep[rep.index("adi"):])
+        assert sorted(a for a, _, _, _ in chosen) == ["x", "y", "z"]
+        tuned = {a: (int(g), 1 if st else 0) for a, g, _, st in chosen}
+        shapes = {"x": _adi_shapes(gx, True, False, False), "y": _adi_shapes(gy, True, True, False),
+                  "z": _adi_shapes(gz + 1, False, True, True)}
+        assert len(shapes["x"]) >= 3 and len(shapes["y"]) >= 5 and len(shapes["z"]) >= 6
+        for axis in "xyz":
+            for sh in shapes[axis]:
+                plan = dict(tuned, **{axis: sh})
+                mask = 2 * plan["y"][1] + 4 * plan["z"][1]
+                c.set_adi_plan(plan["x"][0], plan["y"][0], plan["z"][0], mask)
+                dens, res = c.propagate_diblock(field)
+                assert abs(np.log(res.Qsum) - np.log(ref["Qsum"])) < 2e-6, (axis, sh)
+                assert np.max(np.abs(dens - ref["density"])) < 2e-6 * np.max(np.abs(ref["density"])), (axis, sh)
+        with pytest.raises(AdscfError):
+            c.set_adi_plan(3, 0, 0)
+        with pytest.raises(AdscfError):
+            c.set_adi_plan(8, 16, 8, 1)   # the x sweep has no staged form
 
 
 def test_brush_propagate_homopolymer(rng):
