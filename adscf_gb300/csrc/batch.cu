@@ -67,14 +67,21 @@ struct adscf_batch {
   };
   std::vector<PassClass> cls;
   int maxns = 0, cont_blocks = 64, clos_grid = 0, mix_grid = 0;
-  // persistent sweep: items of every pass of every instance in dependency
-  // order, control words [next item, error flag, done count per instance]
+  // persistent sweep: one launch, a CTA range per kernel class, work items
+  // of every pass of every instance of the class in dependency order;
+  // control words [class counters][error flag][items done per instance]
+  struct SweepClass {
+    int n = 0;                          // kernel class (line length; 0: generic)
+    int off = 0, count = 0;             // its items in d_items
+  };
+  std::vector<SweepClass> sw;
   int4* d_items = nullptr;
-  int nitems = 0;
   int* d_ctl = nullptr;
+  void* d_ranges = nullptr;             // SweepRange per class
   int sweep_grid = 0;
   size_t sweep_smem = 0;
-  bool sweep = true;                    // persistent sweep (ADSCF_BATCH_SWEEP=0: one launch per pass)
+  bool sweep = true;                    // persistent sweeps (ADSCF_BATCH_SWEEP=0: one launch per pass)
+  int sweep_tiles = 8;                  // tiles per sweep item (ADSCF_SWEEP_TILES)
   cudaGraphExec_t g_iter = nullptr;
   double* h_pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -181,22 +188,26 @@ int check_params(const adscf_params& q, int prec, std::string& why) {
 
 // ---------------------------------------------------------------------------
 // Persistent sweep of a bulk batch: every line pass of every contour step of
-// every instance in one launch.  The host lists work items in dependency
-// order -- X of node 0, then per step t the Yf, Z, Yi and X passes -- with
-// the instances interleaved within each pass; an item is up to kSweepTiles
-// tiles of one pass of one instance and carries the number of items of that
-// instance listed before it.  Resident CTAs take items in list order from an
-// atomic counter, wait (bounded) until their instance has completed that many
-// items, run the pass's tile function, and count the item done with release
-// semantics.  Every item an item waits for was taken earlier by a resident
-// CTA that waits only on earlier items, so the sweep cannot deadlock; a wait
-// that runs out sets the error flag and ends its CTA, and the CTAs waiting on
-// it run out in turn.  The tile functions are those of the per-pass kernels,
-// so results are bit for bit those of the launch-per-pass schedule.
+// every instance in one launch.  Instances fall into kernel classes (register
+// FFT of one cubic size, or the generic mixed-radix passes); each class gets
+// a range of the CTAs in proportion to its point-steps and runs its own
+// instantiation of the tile functions, so the classes share the GPU without
+// sharing registers.  The host lists each class's work items in dependency
+// order -- X of node 0, then per step t the Yf, Z, Yi and X passes -- with the
+// instances interleaved within each pass; an item is a few tiles of one pass
+// of one instance and carries the number of items of that instance listed
+// before it.  The CTAs of a class take its items in list order from the
+// class's atomic counter, wait (bounded) until their instance has completed
+// that many items, run the pass's tile function, and count the item done
+// with release semantics.  Every item an item waits for was taken earlier by
+// a running CTA that waits only on earlier items, so the sweep cannot
+// deadlock, however many of its CTAs are resident; a wait that runs out sets
+// the error flag and ends its CTA, and the CTAs waiting on it run out in
+// turn.  The tile functions are those of the per-pass kernels, so results are
+// bit for bit those of the launch-per-pass schedule.
 // item: x instance, y first tile | ntiles << 20, z t << 3 | pass, w items before
 // ---------------------------------------------------------------------------
 enum { SW_XINIT = 0, SW_YF = 1, SW_Z = 2, SW_YI = 3, SW_X = 4 };
-constexpr int kSweepTiles = 8;
 constexpr int kSweepPolls = 1 << 22;
 
 __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
@@ -205,72 +216,49 @@ __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
   return v;
 }
 
-// One tile of a pass, each (kernel class, pass) in a function of its own
-// (not inlined), so that every pass gets the kernel's whole register budget.
-template <typename T, int N, int KIND>
-__device__ __noinline__ void sweep_rs(const BulkDev<T>* insts, int2 w, int t, const cplx<T>* tw, const T* fk,
-                                      const double* g64, unsigned char* sm) {
-  rs_tile<T, N, KIND>(insts, w, tw, fk, nullptr, g64, t, sm);
-}
+// one tile of a pass of kernel class N (0: generic mixed-radix passes)
 template <typename T, int N>
-__device__ __noinline__ void sweep_rx(const BulkDev<T>* insts, int2 w, int t, int mode, const cplx<T>* tw,
-                                      unsigned char* sm) {
+__device__ __forceinline__ void sweep_tile(const BulkDev<T>* insts, int2 w, int pass, int t, const cplx<T>* tw,
+                                           const T* fk, const double* g64, unsigned char* sm) {
   const XAux none{nullptr, nullptr, nullptr};
-  rx_tile<T, N>(insts, w, tw, t, mode, none, sm);
-}
-template <typename T, int N>
-__device__ __forceinline__ void sweep_reg(const BulkDev<T>* insts, int2 w, int pass, int t, const cplx<T>* tw,
-                                          const T* fk, const double* g64, unsigned char* sm) {
-  switch (pass) {
-    case SW_XINIT: sweep_rx<T, N>(insts, w, 0, XM_INIT, tw, sm); break;
-    case SW_YF: sweep_rs<T, N, 0>(insts, w, t, tw, fk, g64, sm); break;
-    case SW_Z: sweep_rs<T, N, 2>(insts, w, t, tw, fk, g64, sm); break;
-    case SW_YI: sweep_rs<T, N, 1>(insts, w, t, tw, fk, g64, sm); break;
-    default: sweep_rx<T, N>(insts, w, t, XM_STEP, tw, sm); break;
+  if constexpr (N == 0) {
+    if (pass == SW_XINIT) xpass_tile<T>(insts, w, tw, 0, XM_INIT, none, sm);
+    else if (pass == SW_X) xpass_tile<T>(insts, w, tw, t, XM_STEP, none, sm);
+    else strided_tile<T>(insts, w, tw, fk, nullptr, g64, t, pass == SW_YF ? 0 : pass == SW_Z ? 2 : 1, sm);
+  } else {
+    switch (pass) {
+      case SW_XINIT: rx_tile<T, N>(insts, w, tw, 0, XM_INIT, none, sm); break;
+      case SW_YF: rs_tile<T, N, 0>(insts, w, tw, fk, nullptr, g64, t, sm); break;
+      case SW_Z: rs_tile<T, N, 2>(insts, w, tw, fk, nullptr, g64, t, sm); break;
+      case SW_YI: rs_tile<T, N, 1>(insts, w, tw, fk, nullptr, g64, t, sm); break;
+      default: rx_tile<T, N>(insts, w, tw, t, XM_STEP, none, sm); break;
+    }
   }
 }
 
-template <typename T>
-__device__ __noinline__ void sweep_gx(const BulkDev<T>* insts, int2 w, int t, int mode, const cplx<T>* tw,
-                                      unsigned char* sm) {
-  const XAux none{nullptr, nullptr, nullptr};
-  xpass_tile<T>(insts, w, tw, t, mode, none, sm);
-}
-template <typename T>
-__device__ __noinline__ void sweep_gs(const BulkDev<T>* insts, int2 w, int t, int kind, const cplx<T>* tw,
-                                      const T* fk, const double* g64, unsigned char* sm) {
-  strided_tile<T>(insts, w, tw, fk, nullptr, g64, t, kind, sm);
-}
-template <typename T>
-__device__ __forceinline__ void sweep_generic(const BulkDev<T>* insts, int2 w, int pass, int t, const cplx<T>* tw,
-                                              const T* fk, const double* g64, unsigned char* sm) {
-  if (pass == SW_XINIT) sweep_gx<T>(insts, w, 0, XM_INIT, tw, sm);
-  else if (pass == SW_X) sweep_gx<T>(insts, w, t, XM_STEP, tw, sm);
-  else sweep_gs<T>(insts, w, t, pass == SW_YF ? 0 : pass == SW_Z ? 2 : 1, tw, fk, g64, sm);
-}
-
-template <typename T>
-__global__ void __launch_bounds__(BULK_THREADS, 2)
-k_batch_sweep(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ items, int nitems,
-              int* __restrict__ ctl, const cplx<T>* __restrict__ tw, const T* __restrict__ fk,
-              const double* __restrict__ g64) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_k;
+// One class's share of the sweep: CTAs take that class's items until its
+// list is exhausted.  next: the class's item counter, err: the batch's error
+// flag, done: items completed per instance.
+template <typename T, int N>
+__device__ __forceinline__ void sweep_class(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ items,
+                                            int nitems, int* next, int* err, int* done_all, int& s_k,
+                                            const cplx<T>* __restrict__ tw, const T* __restrict__ fk,
+                                            const double* __restrict__ g64, unsigned char* smraw) {
   for (;;) {
     __syncthreads();                     // the previous item is done with shared memory
-    if (threadIdx.x == 0) s_k = atomicAdd(&ctl[0], 1);
+    if (threadIdx.x == 0) s_k = atomicAdd(next, 1);
     __syncthreads();
     const int k = s_k;
     if (k >= nitems) break;
     const int4 it = items[k];
-    int* done = &ctl[2 + it.x];
+    int* done = done_all + it.x;
     bool ok = true;
     if (threadIdx.x == 0) {
       for (int i = 0; ld_acquire_gpu(done) < it.w; ++i) {
         if (i >= kSweepPolls) { ok = false; break; }
         __nanosleep(64);
       }
-      if (!ok) atomicOr(&ctl[1], 1);
+      if (!ok) atomicOr(err, 1);
     }
     if (!__syncthreads_or(!ok)) {
       ld_acquire_gpu(done);              // every thread's loads follow the producers' stores
@@ -279,28 +267,51 @@ k_batch_sweep(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ ite
     }
     const int pass = it.z & 7, t = it.z >> 3;
     const int tile0 = it.y & 0xfffff, nt = it.y >> 20;
-    const BulkDev<T>& I = insts[it.x];
-    const int n = I.gx;
-    const bool reg = I.gy == n && I.gz == n && batch_reg_size(n);
     for (int j = 0; j < nt; ++j) {
       if (j) __syncthreads();            // the tile function reuses shared memory
-      const int2 w = make_int2(it.x, tile0 + j);
-      switch (reg ? n : 0) {
-        case 24: sweep_reg<T, 24>(insts, w, pass, t, tw, fk, g64, smraw); break;
-        case 32: sweep_reg<T, 32>(insts, w, pass, t, tw, fk, g64, smraw); break;
-        case 40: sweep_reg<T, 40>(insts, w, pass, t, tw, fk, g64, smraw); break;
-        case 48: sweep_reg<T, 48>(insts, w, pass, t, tw, fk, g64, smraw); break;
-        case 64: sweep_reg<T, 64>(insts, w, pass, t, tw, fk, g64, smraw); break;
-        case 128: sweep_reg<T, 128>(insts, w, pass, t, tw, fk, g64, smraw); break;
-        case 256: sweep_reg<T, 256>(insts, w, pass, t, tw, fk, g64, smraw); break;
-        default: sweep_generic<T>(insts, w, pass, t, tw, fk, g64, smraw);
-      }
+      sweep_tile<T, N>(insts, make_int2(it.x, tile0 + j), pass, t, tw, fk, g64, smraw);
     }
     __syncthreads();                     // every thread's stores of the item are issued
     if (threadIdx.x == 0) {
       __threadfence();
       atomicAdd(done, 1);
     }
+  }
+}
+
+// Kernel class of a CTA range of the sweep: line length n (0: generic), its
+// items [off, off + count) and CTAs [cta0, cta0 + ncta).
+struct SweepRange {
+  int n, off, count, cta0, ncta;
+};
+constexpr int kMaxSweepClasses = 8;
+
+// One launch for every class: the CTAs of range c work on class c only, so
+// each class keeps its share of the GPU whatever the others do; each range
+// runs the class's own instantiation of the loop (inlined).  ctl: [class
+// counters][error flag][items done per instance].
+template <typename T>
+__global__ void __launch_bounds__(BULK_THREADS, 2)
+k_batch_sweep(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ items,
+              const SweepRange* __restrict__ ranges, int ncls, int* __restrict__ ctl,
+              const cplx<T>* __restrict__ tw, const T* __restrict__ fk, const double* __restrict__ g64) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ int s_k;
+  int c = 0;
+  while (c + 1 < ncls && (int)blockIdx.x >= ranges[c + 1].cta0) ++c;
+  const SweepRange R = ranges[c];
+  const int4* it = items + R.off;
+  int* err = ctl + ncls;
+  int* done = err + 1;
+  switch (R.n) {
+    case 24: sweep_class<T, 24>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
+    case 32: sweep_class<T, 32>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
+    case 40: sweep_class<T, 40>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
+    case 48: sweep_class<T, 48>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
+    case 64: sweep_class<T, 64>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
+    case 128: sweep_class<T, 128>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
+    case 256: sweep_class<T, 256>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
+    default: sweep_class<T, 0>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw);
   }
 }
 
@@ -474,9 +485,12 @@ int build(adscf_batch* b) {
     BK(cudaMemcpyAsync(C.wy, wy.data(), wy.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
     BK(cudaMemcpyAsync(C.wz, wz.data(), wz.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
   }
-  // items of the persistent sweep (k_batch_sweep): per step and pass, the
-  // instances still on their contour in the same order as the work lists
+  // items of the persistent sweeps (k_batch_sweep), class by class: per step
+  // and pass, the class's instances still on their contour in the same order
+  // as the work lists
   {
+    if (const char* e = std::getenv("ADSCF_SWEEP_TILES")) b->sweep_tiles = std::max(1, std::min(64, std::atoi(e)));
+    if (const char* e = std::getenv("ADSCF_BATCH_SWEEP")) b->sweep = std::atoi(e) != 0;
     std::vector<int> tx(n), ty(n), tz(n), before(n, 0);
     for (int i = 0; i < n; ++i) {
       const BulkDev<T>& d = I[i];
@@ -491,24 +505,31 @@ int build(adscf_batch* b) {
     std::vector<int4> items;
     auto add = [&](int i, int ntiles, int pass, int t) {
       int k = 0;
-      for (int t0 = 0; t0 < ntiles; t0 += kSweepTiles, ++k) {
-        const int nt = std::min(kSweepTiles, ntiles - t0);
+      for (int t0 = 0; t0 < ntiles; t0 += b->sweep_tiles, ++k) {
+        const int nt = std::min(b->sweep_tiles, ntiles - t0);
         items.push_back(make_int4(i, t0 | (nt << 20), (t << 3) | pass, before[i]));
       }
       before[i] += k;
     };
-    for (int i : ord) add(i, tx[i], SW_XINIT, 0);
-    for (int t = 1; t <= b->maxns; ++t) {
-      for (int pass : {SW_YF, SW_Z, SW_YI, SW_X})
-        for (int i : ord)
-          if (b->ns[i] >= t) add(i, pass == SW_X ? tx[i] : pass == SW_Z ? tz[i] : ty[i], pass, t);
+    for (const auto& C : b->cls) {
+      adscf_batch::SweepClass W;
+      W.n = C.n;
+      W.off = (int)items.size();
+      for (int i : ord)
+        if (class_of(i) == C.n) add(i, tx[i], SW_XINIT, 0);
+      for (int t = 1; t <= b->maxns; ++t)
+        for (int pass : {SW_YF, SW_Z, SW_YI, SW_X})
+          for (int i : ord)
+            if (class_of(i) == C.n && b->ns[i] >= t)
+              add(i, pass == SW_X ? tx[i] : pass == SW_Z ? tz[i] : ty[i], pass, t);
+      W.count = (int)items.size() - W.off;
+      b->sw.push_back(W);
     }
-    b->nitems = (int)items.size();
     BK(cudaMalloc(&b->d_items, items.size() * sizeof(int4)));
     BK(cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, b->stream));
-    BK(cudaMalloc(&b->d_ctl, (2 + (size_t)n) * sizeof(int)));
-    BK(cudaMemsetAsync(b->d_ctl, 0, (2 + (size_t)n) * sizeof(int), b->stream));
-    if (const char* e = std::getenv("ADSCF_BATCH_SWEEP")) b->sweep = std::atoi(e) != 0;
+    const size_t nctl = b->sw.size() + 1 + (size_t)n;
+    BK(cudaMalloc(&b->d_ctl, nctl * sizeof(int)));
+    BK(cudaMemsetAsync(b->d_ctl, 0, nctl * sizeof(int), b->stream));
   }
   size_t smmax = 0;
   for (const auto& C : b->cls) smmax = std::max(smmax, std::max(C.smx, std::max(C.smy, C.smz)));
@@ -526,21 +547,39 @@ int build(adscf_batch* b) {
   ADSCF_BATTR(24) ADSCF_BATTR(32) ADSCF_BATTR(40) ADSCF_BATTR(48) ADSCF_BATTR(64) ADSCF_BATTR(128)
   ADSCF_BATTR(256)
 #undef ADSCF_BATTR
-  {  // persistent sweep: resident CTAs with the largest tile layout of the batch
-     // (the kernel's static shared memory counts against the same limit)
+  {  // persistent sweep: each class's share of the resident CTAs in proportion
+     // to its point-steps (at least one CTA); the kernel's static shared
+     // memory counts against the opt-in limit
+    const int ncls = (int)b->sw.size();
+    if (ncls > kMaxSweepClasses) b->sweep = false;
+    int nsm = 0, occ = 0;
+    BK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev));
     cudaFuncAttributes fa{};
     BK(cudaFuncGetAttributes(&fa, k_batch_sweep<T>));
     b->sweep_smem = std::max<size_t>(smmax, 16);
-    int occ = 0, nsm = 0;
-    if (b->sweep_smem + fa.sharedSizeBytes > (size_t)optin) {
-      b->sweep = false;
-    } else {
+    if (b->sweep_smem + fa.sharedSizeBytes <= (size_t)optin) {
       BK(cudaFuncSetAttribute(k_batch_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->sweep_smem));
       BK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_sweep<T>, BULK_THREADS, b->sweep_smem));
     }
-    BK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev));
-    b->sweep_grid = std::max(1, occ) * nsm;
     if (occ < 1) b->sweep = false;
+    const int slots = std::max(1, occ) * nsm;
+    double total = 0.0;
+    std::vector<double> work(ncls, 0.0);
+    for (int c = 0; c < ncls; ++c) {
+      for (int i = 0; i < n; ++i)
+        if (class_of(i) == b->sw[c].n) work[c] += (double)I[i].npts * b->ns[i];
+      total += work[c];
+    }
+    std::vector<SweepRange> rg(std::max(ncls, 1));
+    int cta = 0;
+    for (int c = 0; c < ncls; ++c) {
+      const int share = std::max(1, (int)(slots * (total > 0 ? work[c] / total : 1.0 / ncls)));
+      rg[c] = SweepRange{b->sw[c].n, b->sw[c].off, b->sw[c].count, cta, share};
+      cta += share;
+    }
+    b->sweep_grid = cta;
+    BK(cudaMalloc(&b->d_ranges, rg.size() * sizeof(SweepRange)));
+    BK(cudaMemcpyAsync(b->d_ranges, rg.data(), rg.size() * sizeof(SweepRange), cudaMemcpyHostToDevice, b->stream));
   }
   BK(cudaStreamSynchronize(b->stream));
   return ADSCF_OK;
@@ -848,9 +887,10 @@ int enqueue_propagation(adscf_batch* b) {
     }
   };
   if (b->sweep) {
-    BK(cudaMemsetAsync(b->d_ctl, 0, (2 + (size_t)b->n) * sizeof(int), s));
-    k_batch_sweep<T><<<b->sweep_grid, BULK_THREADS, b->sweep_smem, s>>>(d, b->d_items, b->nitems, b->d_ctl, tw,
-                                                                       fk, g64);
+    const int ncls = (int)b->sw.size();
+    BK(cudaMemsetAsync(b->d_ctl, 0, (ncls + 1 + (size_t)b->n) * sizeof(int), s));
+    k_batch_sweep<T><<<b->sweep_grid, BULK_THREADS, b->sweep_smem, s>>>(
+        d, b->d_items, static_cast<const SweepRange*>(b->d_ranges), ncls, b->d_ctl, tw, fk, g64);
     k_bulk_contour<T><<<dim3(b->cont_blocks, b->n), BULK_THREADS, 0, s>>>(d);
     BK(cudaGetLastError());
     return ADSCF_OK;
@@ -938,12 +978,13 @@ int read_iters(adscf_batch* b, std::vector<int>& it) {
 }
 
 int read_results(adscf_batch* b, adscf_iter_result* out, double* max_acc) {
-  if (b->d_ctl) {   // a bounded wait of the persistent sweep expired
+  if (b->d_ctl) {   // a bounded wait of a persistent sweep expired
     int f = 0;
-    BK(cudaMemcpyAsync(&f, b->d_ctl + 1, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    int* err = b->d_ctl + b->sw.size();
+    BK(cudaMemcpyAsync(&f, err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
     BK(cudaStreamSynchronize(b->stream));
     if (f) {
-      BK(cudaMemsetAsync(b->d_ctl + 1, 0, sizeof(int), b->stream));
+      BK(cudaMemsetAsync(err, 0, sizeof(int), b->stream));
       return berr(b, ADSCF_E_TIMEOUT, "a bounded wait of the persistent sweep expired");
     }
   }
@@ -1266,7 +1307,7 @@ int adscf_batch_destroy(adscf_batch* b) {
   cudaFree(b->d_tw); cudaFree(b->d_fk); cudaFree(b->d_g64);
   for (auto& C : b->cls) { cudaFree(C.wx); cudaFree(C.wy); cudaFree(C.wz); }
   cudaFree(b->d_f32); cudaFree(b->d_f64); cudaFree(b->d_list32); cudaFree(b->d_list64); cudaFree(b->d_items32);
-  cudaFree(b->d_items); cudaFree(b->d_ctl);
+  cudaFree(b->d_items); cudaFree(b->d_ctl); cudaFree(b->d_ranges);
   cudaFree(b->d_tabf);
   if (b->h_pinned) cudaFreeHost(b->h_pinned);
   if (b->own_stream) cudaStreamDestroy(b->own_stream);
