@@ -90,6 +90,7 @@ SIGNATURES = {
     "adscf_fourier2real": (C.c_int, [C.c_void_p, _dp, _dp]),
     "adscf_integrator": (C.c_int, [C.c_void_p, _dp, _dp]),
     "adscf_mean_fields": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "adscf_update_solvent": (C.c_int, [C.c_void_p, _dp, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]),
     "adscf_interaction_energy": (C.c_int, [C.c_void_p, _dp, _dp]),
     "adscf_mix": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int]),
     "adscf_mix_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),

@@ -554,12 +554,15 @@ int build(adscf_batch* b) {
     if (ncls > kMaxSweepClasses) b->sweep = false;
     int nsm = 0, occ = 0;
     BK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev));
+    // two resident CTAs per SM (128 registers): at three, the register-FFT
+    // classes spill and the C5 sweep ran 4% slower
+    const auto kern = k_batch_sweep<T>;
     cudaFuncAttributes fa{};
-    BK(cudaFuncGetAttributes(&fa, k_batch_sweep<T>));
+    BK(cudaFuncGetAttributes(&fa, kern));
     b->sweep_smem = std::max<size_t>(smmax, 16);
     if (b->sweep_smem + fa.sharedSizeBytes <= (size_t)optin) {
-      BK(cudaFuncSetAttribute(k_batch_sweep<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->sweep_smem));
-      BK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_sweep<T>, BULK_THREADS, b->sweep_smem));
+      BK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->sweep_smem));
+      BK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, BULK_THREADS, b->sweep_smem));
     }
     if (occ < 1) b->sweep = false;
     const int slots = std::max(1, occ) * nsm;

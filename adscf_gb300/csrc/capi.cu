@@ -18,6 +18,8 @@ namespace {
 // nint: round half away from zero (Fortran NINT)
 int nint(double x) { return x >= 0 ? (int)std::floor(x + 0.5) : -(int)std::floor(-x + 0.5); }
 
+}  // namespace
+
 int grid_blocks(size_t n, int per, int cap) {
   size_t b = (n + per - 1) / per;
   if (b < 1) b = 1;
@@ -62,6 +64,8 @@ int d2h(adscf_ctx* ctx, double* h, const double* d, size_t n) {
   std::memcpy(h, ctx->h_pinned, n * sizeof(double));
   return ADSCF_OK;
 }
+
+namespace {
 
 size_t nvar(const adscf_ctx* c) { return (size_t)c->ntypes * c->npts; }
 double* hx_slot(adscf_ctx* c, int s) { return c->d_hx + (size_t)s * nvar(c); }

@@ -119,6 +119,13 @@ struct NvtxRange {
 
 // errors
 int set_err(adscf_ctx* c, int code, const std::string& msg);
+// host helpers (capi.cu): blocks for n items, capped; host <-> device copies of
+// n doubles through the context's page-locked staging buffer (synchronous)
+int grid_blocks(size_t n, int per, int cap);
+int ensure_pinned(adscf_ctx* ctx, size_t bytes);
+bool host_pinned(const void* p);
+int h2d(adscf_ctx* ctx, double* d, const double* h, size_t n);
+int d2h(adscf_ctx* ctx, double* h, const double* d, size_t n);
 #define CK(call)                                                              \
   do {                                                                        \
     cudaError_t e_ = (call);                                                  \

@@ -187,6 +187,21 @@ class Context:
         self._ck(self.lib.adscf_mean_fields(self.h, L.dptr(d), L.dptr(out)))
         return out.reshape(np.shape(density))
 
+    def update_solvent(self, field, ensemble, rho=1.0, mu=0.0):
+        """Update_Solvent (mod_solvent.f90:85-110) of a monomeric solvent in
+        `field` ([npts]) on this bulk context's grid: dict of distribution,
+        Qsum, density, mu, rho and energy (rho in and mu out when canonical,
+        mu in and rho out when grand canonical)."""
+        w = _f64(field, self.npts)
+        dens = np.empty_like(w)
+        dist = np.empty_like(w)
+        r, m, q, e = C.c_double(rho), C.c_double(mu), C.c_double(), C.c_double()
+        self._ck(self.lib.adscf_update_solvent(self.h, L.dptr(w), int(ensemble), C.byref(r), C.byref(m),
+                                               C.byref(q), C.byref(e), L.dptr(dens), L.dptr(dist)))
+        shape = np.shape(field)
+        return {"distribution": dist.reshape(shape), "Qsum": q.value, "density": dens.reshape(shape),
+                "mu": m.value, "rho": r.value, "energy": e.value}
+
     def interaction_energy(self, density):
         d = _f64(density, self.ntypes * self.npts)
         out = C.c_double()

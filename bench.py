@@ -473,16 +473,30 @@ def batch_legs(torch, A, stream, args, world=1, rank=0):
     return out
 
 
-def run_profile_workload(name):
+def run_profile_workload(name, adi_plan=None):
     """One SCF iteration of a film or batch workload for a launch list:
     c4 (Film_3D, 64 x 64 x 65, ADI), c2 (4096 films), c5 (256 bulk
-    instances), after two untimed iterations."""
+    instances), after two untimed iterations.  For c4 the ADI plan in use is
+    printed as "adi plan x,y,z,staged"; ``adi_plan`` pins one (with
+    ADSCF_AUTOTUNE=0 the context skips the tuner's candidate launches, whose
+    timings mean nothing under a profiler)."""
     import adscf_gb300 as A
     if name == "c4":
         kw, w = c4_film3d(A)
         with A.Context(A.FILM_3D, **kw) as c:
+            if adi_plan:
+                c.set_adi_plan(*adi_plan)
+            rep = c.tuning()
             c.set_field(w)
             c.scf_run(3)
+        import re
+        chosen = dict((a, (int(g), st)) for a, g, _, st in
+                      re.findall(r"\b([xyz])=(\d+)x(\d+)(s?)", rep[rep.index("adi"):])) if "adi" in rep else {}
+        if adi_plan:
+            print("adi plan " + ",".join(str(v) for v in adi_plan))
+        elif chosen:
+            mask = (2 if chosen["y"][1] else 0) + (4 if chosen["z"][1] else 0)
+            print(f"adi plan {chosen['x'][0]},{chosen['y'][0]},{chosen['z'][0]},{mask}")
     else:
         inst, fields = c2_films(A) if name == "c2" else c5_bulk(A)
         with A.Batch(inst) as b:
@@ -536,10 +550,14 @@ def main():
     ap.add_argument("--pass-plan", default=None,
                     help="with --profile: pin the Y, Z, X pass kernels, e.g. 2,2,3 "
                          "(0 plain, 1 persistent, 2 TMA, 3 fused XY)")
+    ap.add_argument("--adi-plan", default=None,
+                    help="with --profile c4: pin the ADI sweeps' lanes per line x,y,z and the "
+                         "staging mask (2 y, 4 z), e.g. 16,16,16,6")
     args = ap.parse_args()
     if args.profile:
         if args.profile != "bulk":
-            return run_profile_workload(args.profile)
+            adi = tuple(int(v) for v in args.adi_plan.split(",")) if args.adi_plan else None
+            return run_profile_workload(args.profile, adi)
         plan = tuple(int(v) for v in args.pass_plan.split(",")) if args.pass_plan else None
         return run_profile(plan)
     if args.warmup < 3:

@@ -114,6 +114,16 @@ module adscf
        real(c_double), intent(in) :: density(*)
        real(c_double), intent(out) :: field(*)
      end function
+     integer(c_int) function adscf_update_solvent(ctx, field, ensemble, rho, mu, qsum, energy, &
+          density, distribution) bind(C, name="adscf_update_solvent")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), intent(in) :: field(*)
+       integer(c_int), value :: ensemble
+       real(c_double), intent(inout) :: rho, mu
+       real(c_double), intent(out) :: qsum, energy
+       real(c_double), intent(out) :: density(*), distribution(*)
+     end function
      integer(c_int) function adscf_mix(ctx, field, dfield, iter) bind(C, name="adscf_mix")
        import :: c_int, c_ptr, c_double
        type(c_ptr), value :: ctx

@@ -180,6 +180,19 @@ ADSCF_API int adscf_mean_fields(adscf_ctx *ctx, const double *density, double *f
 ADSCF_API int adscf_interaction_energy(adscf_ctx *ctx, const double *density,
                              double *energy);
 
+/* ---- monomeric solvent --------------------------------------------------
+ * Update_Solvent (Bulk_3D_FFT/Polymer_Modules/mod_solvent.f90:85-110) on a
+ * bulk context's grid: distribution = exp(-field), Qsum = dvol sum, then
+ * canonical (ensemble 1): density = rho V distribution / Qsum,
+ *   mu = log(rho V / Qsum), energy = rho V (mu - 1);
+ * grand canonical (2): density = exp(mu) distribution,
+ *   rho = dvol sum(density) / V, energy = -rho V.
+ * field, density and distribution (optional, NULL to skip) are [npts];
+ * rho and mu are read or written as the ensemble requires.                 */
+ADSCF_API int adscf_update_solvent(adscf_ctx *ctx, const double *field, int ensemble, double *rho,
+                                   double *mu, double *Qsum, double *energy, double *density,
+                                   double *distribution);
+
 /* ---- mixing -----------------------------------------------------------
  * Mix_Fields (main_diblock.f90:315-372) with Mixing_Simple / Mixing_Lambda /
  * Mixing_Anderson (mod_iterate.f90:27-150), history kept on the device

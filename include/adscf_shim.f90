@@ -10,6 +10,7 @@
 !   replaced file (Bulk_3D_FFT)                      module here
 !   General_Routines/mod_propagate.f90               Propagate
 !   Polymer_Modules/mod_diblock.f90                  Molecule_Diblock_Copolymer
+!   Polymer_Modules/mod_solvent.f90                  Molecule_Solvent
 !   General_Routines/mod_iterate.f90 (Mixing_*)      Iterate
 !   Film_CK_AD/Film_3D/Geometry_Modules/mod_realspace.f90
 !     Propagate_Step, integrator                     RealSpace_adscf (used
@@ -28,12 +29,13 @@ module adscf_shim_state
   type(c_ptr), save :: bulk_ctx = c_null_ptr    ! propagation (Propagate, Molecule_*)
   type(c_ptr), save :: mix_ctx = c_null_ptr     ! mixing (Iterate)
   type(c_ptr), save :: film_ctx = c_null_ptr    ! film steps and integrator
+  type(c_ptr), save :: grid_ctx = c_null_ptr    ! grid-only routines (Molecule_Solvent)
   ! the chain the bulk context was created for
   real(c_double), save :: cur_len(2) = -1d0, cur_rho = -1d0, cur_mu = 0d0
   integer(c_int), save :: cur_types(2) = -1, cur_ens = -1
   integer, save :: cur_mix = -1
   real(c_double), save :: cur_lam = -1d0
-  public :: shim_bulk_context, shim_mix_context, shim_film_context
+  public :: shim_bulk_context, shim_mix_context, shim_film_context, shim_grid_context
 contains
 
   subroutine base_params(p)
@@ -99,6 +101,19 @@ contains
     cur_ens = ensemble; cur_rho = rho; cur_mu = mu
     ctx = bulk_ctx
   end function shim_bulk_context
+
+  ! bulk context of the Global grid and box, for routines that use only them
+  function shim_grid_context() result(ctx)
+    type(c_ptr) :: ctx
+    type(adscf_params) :: p
+    integer(c_int) :: rc
+    if (.not. c_associated(grid_ctx)) then
+      call base_params(p)
+      rc = adscf_ctx_create(p, grid_ctx)
+      call adscf_check(grid_ctx, rc, 'adscf_ctx_create (grid)')
+    end if
+    ctx = grid_ctx
+  end function shim_grid_context
 
   ! bulk context that holds the mixing history of one mixing scheme
   function shim_mix_context(mixing_type, lambda) result(ctx)
@@ -273,6 +288,63 @@ contains
   end subroutine Propagate_Diblock
 
 end module Molecule_Diblock_Copolymer
+
+! ---------------------------------------------------------------------------
+! Molecule_Solvent (Bulk_3D_FFT/Polymer_Modules/mod_solvent.f90)
+module Molecule_Solvent
+  use iso_c_binding
+  use adscf
+  use adscf_shim_state
+  use Global
+  implicit none
+  private
+
+  ! same members as the reference's type (mod_solvent.f90:19-28)
+  type monomeric_solvent
+    integer :: label
+    integer :: monomer_type
+    integer :: ensemble
+    double precision :: rho
+    double precision :: mu
+    double precision :: energy
+    double precision :: Qsum
+    double precision, dimension(gridx, gridy, gridz) :: distribution
+    double precision, dimension(gridx, gridy, gridz) :: density
+  end type monomeric_solvent
+
+  public :: monomeric_solvent, Initialize_Solvent, Update_Solvent
+contains
+
+  ! set-up with the reference's semantics (mod_solvent.f90:41-76)
+  subroutine Initialize_Solvent(solvent, label, monomer_type, ensemble, rho, mu)
+    integer, intent(in) :: label, ensemble, monomer_type
+    double precision, intent(in) :: rho, mu
+    type(monomeric_solvent), intent(out) :: solvent
+    if (ensemble /= 1 .and. ensemble /= 2) print *, 'Invalid Ensemble'
+    solvent%label = label
+    solvent%monomer_type = monomer_type
+    solvent%ensemble = ensemble
+    solvent%rho = rho
+    solvent%mu = mu
+    solvent%energy = 0d0
+    solvent%Qsum = 0d0
+    solvent%distribution = 0d0
+    solvent%density = solvent%rho * volume / dvol / dble(gridx * gridy * gridz)
+  end subroutine Initialize_Solvent
+
+  ! distribution, Qsum, density and energy on the GPU (mod_solvent.f90:85-110)
+  subroutine Update_Solvent(solvent, field)
+    type(monomeric_solvent), intent(inout) :: solvent
+    double precision, dimension(gridx, gridy, gridz), intent(in) :: field
+    type(c_ptr) :: ctx
+    integer(c_int) :: rc
+    ctx = shim_grid_context()
+    rc = adscf_update_solvent(ctx, field, int(solvent%ensemble, c_int), solvent%rho, solvent%mu, &
+                              solvent%Qsum, solvent%energy, solvent%density, solvent%distribution)
+    call adscf_check(ctx, rc, 'Update_Solvent')
+  end subroutine Update_Solvent
+
+end module Molecule_Solvent
 
 ! ---------------------------------------------------------------------------
 ! Iterate (Bulk_3D_FFT/General_Routines/mod_iterate.f90:13,27-150): the

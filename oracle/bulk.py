@@ -213,3 +213,27 @@ def density_by_type(blk_density, monomer_type=(0, 1)):
     for i in range(2):
         dens[monomer_type[i]] += blk_density[i]
     return dens
+
+
+def update_solvent(field, grid, size, ensemble, rho=1.0, mu=0.0):
+    """Update_Solvent, Bulk_3D_FFT/Polymer_Modules/mod_solvent.f90:85-110.
+
+    distribution = exp(-field), Qsum = dvol * sum; canonical (1):
+    density = rho V dist / Qsum, mu = log(rho V / Qsum), energy = rho V (mu - 1);
+    grand canonical (2): density = exp(mu) dist, rho = sum(density) dvol / V,
+    energy = -rho V."""
+    volume, dvol = volume_parameters(grid, size)
+    dist = np.exp(-np.asarray(field, dtype=np.float64))
+    qsum = dvol * dist.sum()
+    if ensemble == 1:
+        density = rho * volume * dist / qsum
+        mu = np.log(rho * volume / qsum)
+        energy = rho * volume * (mu - 1.0)
+    elif ensemble == 2:
+        density = np.exp(mu) * dist
+        rho = density.sum() * dvol / volume
+        energy = -rho * volume
+    else:
+        raise ValueError("Invalid ensemble; Cannot calculate Density")
+    return {"distribution": dist, "Qsum": qsum, "density": density, "mu": mu, "rho": rho,
+            "energy": energy}

@@ -210,6 +210,23 @@ def test_scf_iteration_host_buffers(rng):
         assert np.array_equal(c.get_field(), x4) and np.array_equal(c.get_density(), d4)
 
 
+@pytest.mark.parametrize("ensemble", [1, 2])
+def test_update_solvent_vs_oracle(ensemble, rng):
+    """Update_Solvent (mod_solvent.f90:85-110) on the GPU against the FP64
+    oracle, both ensembles (relative 1e-13: exp and the sums in FP64)."""
+    grid, size = (24, 20, 16), (4.0, 3.5, 4.5)
+    w = 0.5 * rng.standard_normal((grid[2], grid[1], grid[0]))
+    ref = ob.update_solvent(w, grid, size, ensemble, rho=0.9, mu=0.4)
+    with mkctx(grid, size) as c:
+        out = c.update_solvent(w, ensemble, rho=0.9, mu=0.4)
+        again = c.update_solvent(w, ensemble, rho=0.9, mu=0.4)
+    for k in ("Qsum", "mu", "rho", "energy"):
+        assert abs(out[k] - ref[k]) <= 1e-13 * max(1.0, abs(ref[k])), k
+        assert out[k] == again[k], k
+    for k in ("distribution", "density"):
+        assert np.max(np.abs(out[k] - ref[k])) <= 1e-13 * np.max(np.abs(ref[k])), k
+
+
 def test_bad_arguments_return_status():
     from adscf_gb300 import AdscfError
     with pytest.raises(AdscfError):

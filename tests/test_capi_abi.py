@@ -118,10 +118,11 @@ def test_fortran_binding_names_declared_symbols():
     bound = re.findall(r'bind\(C, name="(\w+)"\)', f90)
     assert bound and set(bound) <= decl
     shim = (ROOT / "include" / "adscf_shim.f90").read_text()
-    for mod in ("Propagate", "Molecule_Diblock_Copolymer", "Iterate", "RealSpace_adscf"):
+    for mod in ("Propagate", "Molecule_Diblock_Copolymer", "Molecule_Solvent", "Iterate", "RealSpace_adscf"):
         assert re.search(r"^module %s$" % mod, shim, re.M), mod
     for proc in ("Calculate_Expfield", "Propagate_Step", "Initialize_Diblock", "Propagate_Diblock",
-                 "Mixing_Simple", "Mixing_Lambda", "Mixing_Anderson", "integrator"):
+                 "Initialize_Solvent", "Update_Solvent", "Mixing_Simple", "Mixing_Lambda",
+                 "Mixing_Anderson", "integrator"):
         assert re.search(r"^\s*subroutine %s\(" % proc, shim, re.M), proc
     called = set(re.findall(r"\b(adscf_\w+)\(", shim)) - {"adscf_check", "adscf_error_text"}
     assert called <= set(bound), called - set(bound)

@@ -118,3 +118,28 @@ def test_multiblock_reversed_sequence_is_the_same_chain(rng):
     b = ob.propagate_multiblock(w, grid, size, ds, blocks[::-1], types[::-1])
     assert np.isclose(a["Qsum"], b["Qsum"], rtol=1e-12)
     assert np.allclose(a["density"], b["density"][::-1], rtol=1e-10, atol=1e-14)
+
+
+def test_update_solvent_known_answers(rng):
+    """Update_Solvent (mod_solvent.f90:85-110): a uniform field w gives
+    Qsum = V exp(-w); canonical density rho everywhere and mu = log(rho) + w;
+    grand canonical density exp(mu - w) and rho equal to it; both ensembles
+    agree when mu is the canonical one."""
+    grid, size = (4, 5, 6), (2.0, 2.5, 3.0)
+    V = 2.0 * 2.5 * 3.0
+    w = np.full((6, 5, 4), 0.7)
+    c = ob.update_solvent(w, grid, size, 1, rho=0.8)
+    assert np.isclose(c["Qsum"], V * np.exp(-0.7))
+    assert np.allclose(c["density"], 0.8)
+    assert np.isclose(c["mu"], np.log(0.8) + 0.7)
+    assert np.isclose(c["energy"], 0.8 * V * (c["mu"] - 1.0))
+    g = ob.update_solvent(w, grid, size, 2, mu=0.3)
+    assert np.allclose(g["density"], np.exp(0.3 - 0.7))
+    assert np.isclose(g["rho"], np.exp(0.3 - 0.7))
+    assert np.isclose(g["energy"], -g["rho"] * V)
+    w = rng.standard_normal((6, 5, 4))
+    c = ob.update_solvent(w, grid, size, 1, rho=1.3)
+    g = ob.update_solvent(w, grid, size, 2, mu=c["mu"])
+    assert np.allclose(g["density"], c["density"]) and np.isclose(g["rho"], 1.3)
+    with pytest.raises(ValueError):
+        ob.update_solvent(w, grid, size, 3)
