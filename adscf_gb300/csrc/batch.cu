@@ -238,20 +238,29 @@ __device__ __forceinline__ void sweep_tile(const BulkDev<T>* insts, int2 w, int 
 
 // One class's share of the sweep: CTAs take that class's items until its
 // list is exhausted.  next: the class's item counter, err: the batch's error
-// flag, done: items completed per instance.
+// flag, done: items completed per instance; s_q: two shared slots for the
+// current and the reserved next item.  Per item, thread 0 waits for the
+// item's dependencies and reserves the next item (so the atomic's latency
+// overlaps the tiles); thread 32 releases the previous item after the loop's
+// barrier, while thread 0 waits.  An item reserved early waits only on items
+// taken before it, and a release never waits, so neither can deadlock.
 template <typename T, int N>
 __device__ __forceinline__ void sweep_class(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ items,
-                                            int nitems, int* next, int* err, int* done_all, int& s_k,
+                                            int nitems, int* next, int* err, int* done_all, int* s_q,
                                             const cplx<T>* __restrict__ tw, const T* __restrict__ fk,
                                             const double* __restrict__ g64, unsigned char* smraw) {
-  for (;;) {
-    __syncthreads();                     // the previous item is done with shared memory
-    if (threadIdx.x == 0) s_k = atomicAdd(next, 1);
-    __syncthreads();
-    const int k = s_k;
+  int pend = -1;                         // instance of the finished, unreleased item
+  if (threadIdx.x == 0) s_q[0] = atomicAdd(next, 1);
+  for (int par = 0;; par ^= 1) {
+    __syncthreads();                     // the previous item's stores are issued; s_q[par] is set
+    if (threadIdx.x == 32 && pend >= 0) {
+      __threadfence();
+      atomicAdd(done_all + pend, 1);
+    }
+    const int k = s_q[par];
     if (k >= nitems) break;
     const int4 it = items[k];
-    int* done = done_all + it.x;
+    const int* done = done_all + it.x;
     bool ok = true;
     if (threadIdx.x == 0) {
       for (int i = 0; ld_acquire_gpu(done) < it.w; ++i) {
@@ -259,23 +268,17 @@ __device__ __forceinline__ void sweep_class(const BulkDev<T>* __restrict__ insts
         __nanosleep(64);
       }
       if (!ok) atomicOr(err, 1);
+      __threadfence();                   // the CTA's loads of the item follow the producers' stores
+      s_q[par ^ 1] = ok ? atomicAdd(next, 1) : nitems;
     }
-    if (!__syncthreads_or(!ok)) {
-      ld_acquire_gpu(done);              // every thread's loads follow the producers' stores
-    } else {
-      break;
-    }
+    if (__syncthreads_or(!ok)) break;
     const int pass = it.z & 7, t = it.z >> 3;
     const int tile0 = it.y & 0xfffff, nt = it.y >> 20;
     for (int j = 0; j < nt; ++j) {
       if (j) __syncthreads();            // the tile function reuses shared memory
       sweep_tile<T, N>(insts, make_int2(it.x, tile0 + j), pass, t, tw, fk, g64, smraw);
     }
-    __syncthreads();                     // every thread's stores of the item are issued
-    if (threadIdx.x == 0) {
-      __threadfence();
-      atomicAdd(done, 1);
-    }
+    pend = it.x;
   }
 }
 
@@ -296,7 +299,7 @@ k_batch_sweep(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ ite
               const SweepRange* __restrict__ ranges, int ncls, int* __restrict__ ctl,
               const cplx<T>* __restrict__ tw, const T* __restrict__ fk, const double* __restrict__ g64) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ int s_k;
+  __shared__ int s_q[2];
   int c = 0;
   while (c + 1 < ncls && (int)blockIdx.x >= ranges[c + 1].cta0) ++c;
   const SweepRange R = ranges[c];
@@ -304,14 +307,14 @@ k_batch_sweep(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ ite
   int* err = ctl + ncls;
   int* done = err + 1;
   switch (R.n) {
-    case 24: sweep_class<T, 24>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
-    case 32: sweep_class<T, 32>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
-    case 40: sweep_class<T, 40>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
-    case 48: sweep_class<T, 48>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
-    case 64: sweep_class<T, 64>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
-    case 128: sweep_class<T, 128>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
-    case 256: sweep_class<T, 256>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw); break;
-    default: sweep_class<T, 0>(insts, it, R.count, ctl + c, err, done, s_k, tw, fk, g64, smraw);
+    case 24: sweep_class<T, 24>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
+    case 32: sweep_class<T, 32>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
+    case 40: sweep_class<T, 40>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
+    case 48: sweep_class<T, 48>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
+    case 64: sweep_class<T, 64>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
+    case 128: sweep_class<T, 128>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
+    case 256: sweep_class<T, 256>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
+    default: sweep_class<T, 0>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
   }
 }
 
