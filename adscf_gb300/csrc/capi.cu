@@ -119,6 +119,7 @@ int enqueue_iteration(adscf_ctx* ctx) {
   // and the film sweep both locate it through the device counter
   if ((rc = enqueue_propagate(ctx, nullptr))) return rc;
   launch_closure(ctx->S, CL_MEANFIELD | CL_MIXDOTS, ctx->closure_blocks, ctx->stream);
+  CK(cudaEventRecordWithFlags(ctx->ev_dens, ctx->stream, cudaEventRecordExternal));   // densities written
   k_solve<<<1, SOLVE_THREADS, 0, ctx->stream>>>(ctx->S, 1, 1);
   CK(cudaGetLastError());
   if (ctx->geometry == ADSCF_BULK) return bulk_mix_e(ctx);
@@ -282,6 +283,12 @@ int adscf_ctx_create(const adscf_params* p, adscf_ctx** out) {
     return ADSCF_E_CUDA;
   }
   ctx->stream = ctx->own_stream;
+  if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_dens, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ADSCF_E_CUDA);
+  }
   const size_t nv = nvar(ctx);
   ctx->hist_slots = p->mixing_type == 3 ? p->mixing_dim + 1 : 2;
   if (cudaMalloc(&ctx->d_dist, nv * sizeof(double)) ||
@@ -374,6 +381,9 @@ int adscf_ctx_destroy(adscf_ctx* ctx) {
   cudaFree(ctx->d_part); cudaFree(ctx->d_wz); cudaFree(ctx->d_ext);
   cudaFree(ctx->d_mob); cudaFree(ctx->d_ddft);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->ev_dens) cudaEventDestroy(ctx->ev_dens);
+  if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return ADSCF_OK;
@@ -653,9 +663,14 @@ int adscf_scf_iteration(adscf_ctx* ctx, double* field, double* density, adscf_it
   CK(cudaMemcpyAsync(xk, hf, nv * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->geometry == ADSCF_BULK && (rc = bulk_enqueue_expfield(ctx, xk))) return rc;
   CK(cudaGraphLaunch(ctx->g_iter, ctx->stream));
+  // densities to the host as soon as the closure has written them (the
+  // graph's event), beside the solve and the mix; the field after the mix
+  CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_dens, 0));
+  CK(cudaMemcpyAsync(hd, ctx->d_dens, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->copy_stream));
+  CK(cudaEventRecord(ctx->ev_copy, ctx->copy_stream));
   double* xn = hx_slot(ctx, (k + 1) % ctx->hist_slots);
   CK(cudaMemcpyAsync(hf, xn, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(hd, ctx->d_dens, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0));
   adscf_iter_result r{};
   rc = read_result(ctx, &r, nullptr);  // synchronises the stream
   if (!pin) {

@@ -36,6 +36,11 @@ struct adscf_ctx {
   double volume = 0, dvol = 0;
   cudaStream_t stream = nullptr;      // stream all work goes to
   cudaStream_t own_stream = nullptr;  // the context's own stream
+  // adscf_scf_iteration: the iteration graph records ev_dens once the
+  // closure has written the densities, so their copy to the host runs on
+  // copy_stream while the solve and the mix finish
+  cudaEvent_t ev_dens = nullptr, ev_copy = nullptr;
+  cudaStream_t copy_stream = nullptr;
   int dev = 0;
   int film_launches = 0, film_contour_launches = 0;
 
