@@ -1,170 +1,20 @@
-! adscf_shim.f90 -- drop-in replacements for ADSCF's compute modules.
+! adscf_shim.f90 -- drop-in replacements for the compute modules of ADSCF's
+! bulk drivers (Bulk_3D_FFT).
 !
 ! Each module below has the name, public types and procedure signatures of
 ! the reference module it replaces, so the reference's Main_* programs
 ! compile unchanged against it; the bodies call the GB300 library through
-! the `adscf` binding module (adscf.f90).  Build: list this file (after
-! mod_global.f90 and adscf.f90) in place of the replaced source files and
-! link -ladscf_gb300.
+! the `adscf` binding module (adscf.f90) and the shared contexts of
+! adscf_shim_state.f90.  Build: list adscf.f90, adscf_shim_state.f90 and this
+! file (after mod_global.f90) in place of the replaced source files and link
+! -ladscf_gb300.  Film drivers use adscf_shim_film.f90, the brush driver
+! adscf_shim_brush.f90.
 !
 !   replaced file (Bulk_3D_FFT)                      module here
 !   General_Routines/mod_propagate.f90               Propagate
 !   Polymer_Modules/mod_diblock.f90                  Molecule_Diblock_Copolymer
 !   Polymer_Modules/mod_solvent.f90                  Molecule_Solvent
 !   General_Routines/mod_iterate.f90 (Mixing_*)      Iterate
-!   Film_CK_AD/Film_3D/Geometry_Modules/mod_realspace.f90
-!     Propagate_Step, integrator                     RealSpace_adscf (used
-!     beside RealSpace, whose generate_mesh and calculate_Volume stay)
-!
-! Every module shares one library context per geometry (adscf_shim_state),
-! created on first use from the Global module's grid, box and ds.  A
-! non-zero library status prints the library's message and stops, as the
-! reference's routines do on their own errors.
-module adscf_shim_state
-  use iso_c_binding
-  use adscf
-  use Global
-  implicit none
-  private
-  type(c_ptr), save :: bulk_ctx = c_null_ptr    ! propagation (Propagate, Molecule_*)
-  type(c_ptr), save :: mix_ctx = c_null_ptr     ! mixing (Iterate)
-  type(c_ptr), save :: film_ctx = c_null_ptr    ! film steps and integrator
-  type(c_ptr), save :: grid_ctx = c_null_ptr    ! grid-only routines (Molecule_Solvent)
-  ! the chain the bulk context was created for
-  real(c_double), save :: cur_len(2) = -1d0, cur_rho = -1d0, cur_mu = 0d0
-  integer(c_int), save :: cur_types(2) = -1, cur_ens = -1
-  integer, save :: cur_mix = -1
-  real(c_double), save :: cur_lam = -1d0
-  public :: shim_bulk_context, shim_mix_context, shim_film_context, shim_grid_context
-contains
-
-  subroutine base_params(p)
-    type(adscf_params), intent(out) :: p
-    p%geometry = ADSCF_BULK
-    p%gx = gridx; p%gy = gridy; p%gz = gridz
-    p%sizex = sizex; p%sizey = sizey; p%sizez = sizez
-    p%ds = ds
-    p%dss = c_null_ptr; p%ns = 0; p%n_a = 0
-    p%block_length = [0.5d0, 0.5d0]
-    p%ensemble = 1
-    p%rho = 1d0; p%mu = 0d0
-    p%kappa = 0d0; p%chi = 0d0
-    p%monomer_volume = [1d0, 1d0]
-    p%precision = ADSCF_FP64
-    p%mixing_type = ADSCF_MIX_LAMBDA
-    p%mixing_dim = 2
-    p%lambda = 0.1d0
-    p%lam_warm = 1d-3
-    p%warm_iters = 2
-    p%dz = c_null_ptr
-    p%int_scheme = 1; p%int_span = 0
-    p%ext_potential = c_null_ptr
-    p%ww = 0d0
-    p%graft = c_null_ptr
-    p%nblocks = 0
-    p%blocks = c_null_ptr
-    p%block_types = c_null_ptr
-  end subroutine base_params
-
-  ! bulk context for a two-block chain of the given block lengths, monomer
-  ! types (1-based, as the reference's monomer_type) and ensemble; made
-  ! again when the chain changes
-  function shim_bulk_context(block_length, monomer_type, ensemble, rho, mu) result(ctx)
-    real(c_double), intent(in) :: block_length(2), rho, mu
-    integer, intent(in) :: monomer_type(2), ensemble
-    type(c_ptr) :: ctx
-    type(adscf_params) :: p
-    real(c_double), target, save :: blocks(2)
-    integer(c_int), target, save :: types(2)
-    integer(c_int) :: rc
-    if (c_associated(bulk_ctx)) then
-      if (all(cur_len == block_length) .and. all(cur_types == monomer_type) .and. &
-          cur_ens == ensemble .and. cur_rho == rho .and. cur_mu == mu) then
-        ctx = bulk_ctx
-        return
-      end if
-      rc = adscf_ctx_destroy(bulk_ctx)
-      bulk_ctx = c_null_ptr
-    end if
-    call base_params(p)
-    blocks = block_length
-    types = monomer_type - 1
-    p%nblocks = 2
-    p%blocks = c_loc(blocks)
-    p%block_types = c_loc(types)
-    p%block_length = block_length
-    p%ensemble = ensemble
-    p%rho = rho; p%mu = mu
-    rc = adscf_ctx_create(p, bulk_ctx)
-    call adscf_check(bulk_ctx, rc, 'adscf_ctx_create (bulk)')
-    cur_len = block_length; cur_types = monomer_type
-    cur_ens = ensemble; cur_rho = rho; cur_mu = mu
-    ctx = bulk_ctx
-  end function shim_bulk_context
-
-  ! bulk context of the Global grid and box, for routines that use only them
-  function shim_grid_context() result(ctx)
-    type(c_ptr) :: ctx
-    type(adscf_params) :: p
-    integer(c_int) :: rc
-    if (.not. c_associated(grid_ctx)) then
-      call base_params(p)
-      rc = adscf_ctx_create(p, grid_ctx)
-      call adscf_check(grid_ctx, rc, 'adscf_ctx_create (grid)')
-    end if
-    ctx = grid_ctx
-  end function shim_grid_context
-
-  ! bulk context that holds the mixing history of one mixing scheme
-  function shim_mix_context(mixing_type, lambda) result(ctx)
-    integer, intent(in) :: mixing_type
-    real(c_double), intent(in) :: lambda
-    type(c_ptr) :: ctx
-    type(adscf_params) :: p
-    integer(c_int) :: rc
-    if (c_associated(mix_ctx)) then
-      if (cur_mix == mixing_type .and. cur_lam == lambda) then
-        ctx = mix_ctx
-        return
-      end if
-      rc = adscf_ctx_destroy(mix_ctx)
-      mix_ctx = c_null_ptr
-    end if
-    call base_params(p)
-    p%ds = 0.5d0            ! two contour steps: the context only mixes
-    p%mixing_type = mixing_type
-    p%lambda = lambda
-    rc = adscf_ctx_create(p, mix_ctx)
-    call adscf_check(mix_ctx, rc, 'adscf_ctx_create (mixing)')
-    cur_mix = mixing_type; cur_lam = lambda
-    ctx = mix_ctx
-  end function shim_mix_context
-
-  ! Film_3D context on the Global mesh dz(0:gridz)
-  function shim_film_context(zmesh, scheme) result(ctx)
-    real(c_double), intent(in) :: zmesh(0:)
-    integer, intent(in) :: scheme
-    type(c_ptr) :: ctx
-    type(adscf_params) :: p
-    real(c_double), allocatable, target, save :: dzc(:)
-    integer(c_int) :: rc
-    if (c_associated(film_ctx)) then
-      ctx = film_ctx
-      return
-    end if
-    call base_params(p)
-    allocate(dzc(0:size(zmesh) - 1))
-    dzc = zmesh
-    p%geometry = ADSCF_FILM_3D
-    p%dz = c_loc(dzc)
-    p%int_scheme = scheme
-    p%int_span = 0
-    rc = adscf_ctx_create(p, film_ctx)
-    call adscf_check(film_ctx, rc, 'adscf_ctx_create (film)')
-    ctx = film_ctx
-  end function shim_film_context
-
-end module adscf_shim_state
 
 ! ---------------------------------------------------------------------------
 ! Propagate (Bulk_3D_FFT/General_Routines/mod_propagate.f90:22-68)
@@ -400,36 +250,4 @@ contains
 
 end module Iterate
 
-! ---------------------------------------------------------------------------
-! RealSpace_adscf: the Film_3D step and integrator of
-! Film_CK_AD/Film_3D/Geometry_Modules/mod_realspace.f90:22-140,267-281 on
-! the GPU, for a driver compiled against the Film_3D Global module.
-module RealSpace_adscf
-  use iso_c_binding
-  use adscf
-  use adscf_shim_state
-  use Global
-  implicit none
-contains
 
-  subroutine Propagate_Step(prop, field)
-    double precision, dimension(gridx, gridy, 0:gridz), intent(inout) :: prop
-    double precision, dimension(gridx, gridy, 0:gridz), intent(in) :: field
-    type(c_ptr) :: ctx
-    integer(c_int) :: rc
-    ctx = shim_film_context(dz, int_scheme)
-    rc = adscf_propagate_step(ctx, prop, field, ds)
-    call adscf_check(ctx, rc, 'Propagate_Step (film)')
-  end subroutine Propagate_Step
-
-  subroutine integrator(integrand, integral)
-    double precision, dimension(gridx, gridy, 0:gridz), intent(in) :: integrand
-    double precision, intent(out) :: integral
-    type(c_ptr) :: ctx
-    integer(c_int) :: rc
-    ctx = shim_film_context(dz, int_scheme)
-    rc = adscf_integrator(ctx, integrand, integral)
-    call adscf_check(ctx, rc, 'integrator')
-  end subroutine integrator
-
-end module RealSpace_adscf

@@ -110,22 +110,65 @@ def test_struct_field_offsets_match_c(tmp_path, cname, pyname):
     assert _fortran_members(cname) == members
 
 
+SHIMS = ("adscf_shim_state.f90", "adscf_shim.f90", "adscf_shim_film.f90", "adscf_shim_brush.f90")
+
+# Global members each driver family declares (Bulk_3D_FFT/Main_Diblock_Melt,
+# Film_CK_AD/Film_*/Main_Diblock_Melt and Brush_CK_AD/Main_brush
+# mod_global.f90) that the shims read; the shared state module may use only
+# the members all of them declare
+GLOBAL_ONLY = {
+    "adscf_shim_state.f90": {"dz", "int_scheme", "dvol", "volume"},
+    "adscf_shim.f90": {"dz", "int_scheme"},
+    "adscf_shim_film.f90": {"dvol"},
+    "adscf_shim_brush.f90": {"dvol"},
+}
+
+
+def _code(text):
+    return "\n".join(line.split("!")[0] for line in text.splitlines())
+
+
 def test_fortran_binding_names_declared_symbols():
     """Every bind(C) name of the Fortran binding is an entry point of the
-    header, and the shim keeps the reference's module procedure names."""
+    header, the shims keep the reference's module procedure names, and they
+    call only bound entry points."""
     decl = set(declared_symbols())
     f90 = (ROOT / "include" / "adscf.f90").read_text()
     bound = re.findall(r'bind\(C, name="(\w+)"\)', f90)
     assert bound and set(bound) <= decl
-    shim = (ROOT / "include" / "adscf_shim.f90").read_text()
-    for mod in ("Propagate", "Molecule_Diblock_Copolymer", "Molecule_Solvent", "Iterate", "RealSpace_adscf"):
-        assert re.search(r"^module %s$" % mod, shim, re.M), mod
-    for proc in ("Calculate_Expfield", "Propagate_Step", "Initialize_Diblock", "Propagate_Diblock",
-                 "Initialize_Solvent", "Update_Solvent", "Mixing_Simple", "Mixing_Lambda",
-                 "Mixing_Anderson", "integrator"):
-        assert re.search(r"^\s*subroutine %s\(" % proc, shim, re.M), proc
-    called = set(re.findall(r"\b(adscf_\w+)\(", shim)) - {"adscf_check", "adscf_error_text"}
-    assert called <= set(bound), called - set(bound)
+    text = {f: (ROOT / "include" / f).read_text() for f in SHIMS}
+    want_mods = {
+        "adscf_shim_state.f90": ("adscf_shim_state",),
+        "adscf_shim.f90": ("Propagate", "Molecule_Diblock_Copolymer", "Molecule_Solvent", "Iterate"),
+        "adscf_shim_film.f90": ("RealSpace_adscf", "Molecule_Diblock_Copolymer"),
+        "adscf_shim_brush.f90": ("RealSpace_adscf",),
+    }
+    want_procs = {
+        "adscf_shim.f90": ("Calculate_Expfield", "Propagate_Step", "Initialize_Diblock", "Propagate_Diblock",
+                           "Initialize_Solvent", "Update_Solvent", "Mixing_Simple", "Mixing_Lambda",
+                           "Mixing_Anderson"),
+        "adscf_shim_film.f90": ("Propagate_Step", "integrator", "Initialize_Diblock", "Propagate_Diblock"),
+        "adscf_shim_brush.f90": ("Propagate_Step", "integrator"),
+    }
+    for f, mods in want_mods.items():
+        for mod in mods:
+            assert re.search(r"^module %s$" % mod, text[f], re.M), (f, mod)
+    for f, procs in want_procs.items():
+        for proc in procs:
+            assert re.search(r"^\s*subroutine %s\(" % proc, text[f], re.M), (f, proc)
+    for f, t in text.items():
+        called = set(re.findall(r"\b(adscf_\w+)\(", _code(t))) - {"adscf_check", "adscf_error_text"}
+        assert called <= set(bound), (f, called - set(bound))
+
+
+def test_fortran_shims_use_only_their_drivers_globals():
+    """The bulk shim compiles against the bulk Global (no dz, int_scheme),
+    the film and brush shims against theirs (no dvol), and the shared state
+    module against any of them."""
+    for f, banned in GLOBAL_ONLY.items():
+        # identifiers, not derived-type components (p%dz is a member of adscf_params)
+        words = set(re.findall(r"(?<![%\w])[a-z_]\w*", _code((ROOT / "include" / f).read_text()).lower()))
+        assert not (words & banned), (f, words & banned)
 
 
 def test_status_strings_without_gpu(lib):
