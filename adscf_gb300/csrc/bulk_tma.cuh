@@ -21,6 +21,12 @@
 
 namespace tmak {
 
+// prefetch the 128-byte line holding p into L1 (a hint: no register, no wait)
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -486,8 +492,12 @@ k_xy_tma(const BulkDev<float>* __restrict__ insts, const __grid_constant__ CUten
       if (!init) {
         // the Boltzmann factors of the first half of the row's points are
         // loaded before its inverse x transform, so their latency overlaps
-        // it (all sixteen would leave too few registers for the transform)
+        // it (all sixteen would leave too few registers for the transform);
+        // the second half is prefetched into L1, which takes no registers
         constexpr int HP = R1 / 2;
+#pragma unroll
+        for (int m = HP; m < R1; ++m)
+          tmak::prefetch_l1(reinterpret_cast<const float4*>(I.E) + rbase + F::in_index(lt, m));
         EPt<float> epre[HP];
 #pragma unroll
         for (int m = 0; m < HP; ++m) epre[m] = load_ept(I.E, rbase + F::in_index(lt, m));
