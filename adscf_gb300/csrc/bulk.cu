@@ -527,9 +527,9 @@ int tune_t(adscf_ctx* ctx) {
   const XAux none{nullptr, nullptr, nullptr};
   launch_x<T>(ctx, 0, XM_INIT, none);
   const int steps = std::min(ctx->ns, 6);
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  EventPair ev;
+  CK(ev.create());
+  cudaEvent_t e0 = ev.a, e1 = ev.b;
   struct Cand { int y, z, x; float us; };
   std::vector<Cand> cands;
   for (int x : xs)
@@ -552,8 +552,6 @@ int tune_t(adscf_ctx* ctx) {
       c.us = std::min(c.us, 1000.f * ms / steps);
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   CK(cudaGetLastError());
   const Cand* best = &cands[0];
   for (const Cand& c : cands)

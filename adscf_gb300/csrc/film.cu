@@ -183,9 +183,9 @@ int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldR
   }
   cudaStream_t s = ctx->stream;
   AdiLaunch A = adi_launch<float>(F, D, 2);
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  EventPair ev;
+  CK(ev.create());
+  cudaEvent_t e0 = ev.a, e1 = ev.b;
   std::string rep = "adi";
   static const char* nm[3] = {"x", "y", "z"};
   AdiTuneVal val;
@@ -220,8 +220,6 @@ int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldR
     }
     rep += ";";
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   CK(cudaGetLastError());
   for (int d = 0; d < 3; ++d) F->adi[d] = val.sh[d];
   F->adi_set = true;

@@ -124,6 +124,19 @@ struct NvtxRange {
 
 // errors
 int set_err(adscf_ctx* c, int code, const std::string& msg);
+// two timing events destroyed with their scope (the tuners return early on
+// a CUDA error)
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t create() {
+    cudaError_t e = cudaEventCreate(&a);
+    return e != cudaSuccess ? e : cudaEventCreate(&b);
+  }
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
 // host helpers (capi.cu): blocks for n items, capped; host <-> device copies of
 // n doubles through the context's page-locked staging buffer (synchronous)
 int grid_blocks(size_t n, int per, int cap);

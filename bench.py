@@ -319,6 +319,31 @@ def c5_bulk(A, n=256, seed=5, prec=None):
     return inst, fields
 
 
+def oracle_fixture_parity(res, A):
+    """The first iteration of both GPU paths at the C3 start field against the
+    FP64 oracle's values at that field, read from the committed fixture
+    tests/golden/c3_start.json (made by tests/golden/make_c3_start.py); None
+    when the fixture is absent or for another configuration."""
+    path = Path(__file__).resolve().parent / "tests" / "golden" / "c3_start.json"
+    if not path.exists():
+        return None
+    fx = json.loads(path.read_text())
+    if (fx["grid"], fx["L"], fx["ds"], fx["f_A"], fx["chi"], fx["kappa"], fx["seed"]) != \
+            (GRID, L, DS, F_A, CHI, KAPPA, SEED):
+        return None
+    idx = [tuple(i) for i in fx["sample_index"]]
+    ref = np.array(fx["sample_density"])
+    out = {"vs": "FP64 oracle at the same field (tests/golden/c3_start.json): F per chain and log Q, "
+                 "densities at 256 seeded points"}
+    for prec, name in ((A.SPLIT, "split"), (A.FP64, "fp64")):
+        r, d = res[prec]
+        dens = np.asarray(d).reshape(2, GRID, GRID, GRID)
+        out[f"dF_per_chain_{name}"] = abs(r.free_energy - fx["F"])
+        out[f"dlogQ_{name}"] = abs(r.logQ - fx["logQ"])
+        out[f"max_dphi_{name}"] = float(np.max(np.abs(np.array([dens[i] for i in idx]) - ref)))
+    return out
+
+
 def c1_parity(A):
     """C1 (the reference's CPU-runnable case: 32^3, L = 4.0, f_A = 0.30, chiN =
     kappa = 25, ds = 0.01, Anderson m = 10 after 20 lambda = 0.1 steps; start
@@ -592,6 +617,7 @@ def main():
     dF = abs(res[A.SPLIT][0].free_energy - res[A.FP64][0].free_energy)
     dphi = float(np.max(np.abs(res[A.SPLIT][1] - res[A.FP64][1])))
     dlogQ = abs(res[A.SPLIT][0].logQ - res[A.FP64][0].logQ)
+    par_oracle = oracle_fixture_parity(res, A)
 
     # ---- FP64 GPU path timing ---------------------------------------------
     with make_ctx(A, A.FP64, stream) as c64:
@@ -686,6 +712,7 @@ def main():
         "contour_steps_per_s": world * 2 * ns * 1000.0 / ms_step,
         "parity": {"dF_per_chain": dF, "max_dphi": dphi, "dlogQ": dlogQ,
                    "vs": "FP64 GPU path, same field (the bench's start iterate), one iteration"},
+        "parity_oracle": par_oracle,
         "parity_saddle": saddle,
         "stages_ms": {"propagate": t_prop, "contour": t_cont, "update": t_upd,
                       "double_step": t_dstep},
