@@ -339,9 +339,11 @@ int create_t(adscf_ctx* ctx) {
   CK(cudaMalloc(&ctx->d_inst, sizeof(BulkDev<T>)));
   CK(cudaMemcpy(ctx->d_inst, &I, sizeof(I), cudaMemcpyHostToDevice));
   hb<T>(ctx) = I;
-  // default plan: the most specialised kernel available for each pass
+  // default plan: the most specialised kernel available for each pass (the
+  // fused plane pass where the TMA passes run: the tuner's choice at 64^3 and
+  // 128^3 on GB300)
   ctx->plan_y = ctx->plan_z = ctx->tma ? PK_TMA : ctx->pgrid_y ? PK_PERSISTENT : PK_PLAIN;
-  ctx->plan_x = ctx->pgrid_x ? PK_PERSISTENT : PK_PLAIN;
+  ctx->plan_x = ctx->tma && ctx->xy_grid ? PK_FUSED : ctx->pgrid_x ? PK_PERSISTENT : PK_PLAIN;
   if (ctx->autotune) return tune_t<T>(ctx);
   return ADSCF_OK;
 }

@@ -254,7 +254,9 @@ ADSCF_API int adscf_set_wait_limit(adscf_ctx *ctx, int polls);
  * TMA-fed; X: plain, persistent, or the fused plane pass that also does Yi
  * and Yf (then the Y choice is moot) -- is timed on the context's own buffers
  * and the fastest plan kept (cached per device, grid and precision; the
- * environment variable ADSCF_AUTOTUNE=0 keeps the default plan instead).
+ * environment variable ADSCF_AUTOTUNE=0 keeps the default plan instead:
+ * the TMA-fed Y and Z passes with the fused plane pass where they exist,
+ * else the persistent, else the plain kernels).
  * All plans compute the same arithmetic: results do not depend on the choice.
  * adscf_tuning writes the plan and the per-candidate timings as text;
  * adscf_set_pass_plan pins a plan (ADSCF_E_ARG if unavailable).           */
