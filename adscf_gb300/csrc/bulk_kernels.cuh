@@ -85,13 +85,17 @@ __device__ __forceinline__ EPt<double> load_ept(const double* E, size_t g) {
   const double2 v = __ldg(reinterpret_cast<const double2*>(E) + g);
   return {v.x, v.y, 0.0, 0.0};
 }
-// e = exp(-ds w/2) of species c at point p
-__device__ __forceinline__ void store_ept(float* E, size_t p, int c, double e) {
-  const float h = (float)e;
+// the Boltzmann factor e^a of species c at point p: float-float on the split
+// path (exp_ff), the FP64 series on the FP64 path
+__device__ __forceinline__ void store_boltzmann(float* E, size_t p, int c, double a) {
+  float h, l;
+  exp_ff(a, h, l);
   E[4 * p + c] = h;
-  E[4 * p + 2 + c] = (float)(e - (double)h);
+  E[4 * p + 2 + c] = l;
 }
-__device__ __forceinline__ void store_ept(double* E, size_t p, int c, double e) { E[2 * p + c] = e; }
+__device__ __forceinline__ void store_boltzmann(double* E, size_t p, int c, double a) {
+  E[2 * p + c] = exp_boltzmann(a);
+}
 
 template <typename T>
 __device__ __forceinline__ int seq_type(const BulkDev<T>& I, int t) {
@@ -594,8 +598,8 @@ k_bulk_contour(const BulkDev<T>* __restrict__ insts) {
 template <typename T>
 __global__ void k_expfield(const double* __restrict__ w, T* __restrict__ E, size_t npts, double ds) {
   for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npts; p += (size_t)gridDim.x * blockDim.x) {
-    store_ept(E, p, 0, exp_boltzmann(-0.5 * ds * w[p]));
-    store_ept(E, p, 1, exp_boltzmann(-0.5 * ds * w[npts + p]));
+    store_boltzmann(E, p, 0, -0.5 * ds * w[p]);
+    store_boltzmann(E, p, 1, -0.5 * ds * w[npts + p]);
   }
 }
 

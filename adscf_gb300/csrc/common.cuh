@@ -74,3 +74,41 @@ __device__ __forceinline__ double exp_boltzmann(double a) {
   p = fma(p, a, 1.0);
   return fma(p, a, 1.0);
 }
+
+// e^a as an unevaluated pair of floats hi + lo (|lo| <= ulp(hi)/2), for the
+// split path's Boltzmann factors, which are stored as exactly such a pair.
+// a = ah + al in floats; e^ah by the Taylor series to k = 9 (truncation below
+// 3e-16 for |a| <= 1/8) in float-float Horner form (products split by FMA,
+// sums by Knuth's TwoSum, every operation explicitly rounded so the compiler
+// cannot contract them), times (1 + al).  Relative error about 2^-47 (an FP32
+// emulation over |a| <= 1/8 gives 6e-15), on the FP32 pipe: the FP64 series
+// keeps GB300's narrow FP64 pipe busy.  Larger |a| falls back to FP64 exp().
+__device__ __forceinline__ void exp_ff(double a, float& hi, float& lo) {
+  if (fabs(a) > 0.125) {
+    const double e = exp(a);
+    hi = (float)e;
+    lo = (float)(e - (double)hi);
+    return;
+  }
+  constexpr double c[10] = {1.0, 1.0, 1.0 / 2, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720, 1.0 / 5040,
+                            1.0 / 40320, 1.0 / 362880};
+  const float ah = (float)a;
+  const float al = (float)(a - (double)ah);
+  float ph = (float)c[9], pl = (float)(c[9] - (double)(float)c[9]);
+#pragma unroll
+  for (int k = 8; k >= 0; --k) {
+    const float t = __fmul_rn(ph, ah);
+    float e = __fmaf_rn(ph, ah, -t);
+    e = __fmaf_rn(pl, ah, e);
+    const float ch = (float)c[k], cl = (float)(c[k] - (double)(float)c[k]);
+    const float s = __fadd_rn(t, ch);
+    const float bb = __fsub_rn(s, t);
+    float err = __fadd_rn(__fsub_rn(t, __fsub_rn(s, bb)), __fsub_rn(ch, bb));
+    err = __fadd_rn(err, __fadd_rn(e, cl));
+    ph = __fadd_rn(s, err);
+    pl = __fsub_rn(err, __fsub_rn(ph, s));
+  }
+  const float e = __fmaf_rn(ph, al, pl);
+  hi = __fadd_rn(ph, e);
+  lo = __fsub_rn(e, __fsub_rn(hi, ph));
+}

@@ -548,7 +548,7 @@ __device__ __forceinline__ void mix_body(const ScfDev& S, T* E, double ds, int b
     S.hx[(size_t)nxt * nv + i] = x;
     if (E) {  // interleaved Boltzmann factors of the next propagation (two species)
       const int c = i >= (size_t)S.npts;
-      store_ept(E, i - (size_t)c * S.npts, c, exp_boltzmann(-0.5 * ds * x));
+      store_boltzmann(E, i - (size_t)c * S.npts, c, -0.5 * ds * x);
     }
   }
 }
