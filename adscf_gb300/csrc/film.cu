@@ -144,9 +144,10 @@ void adi_step(const AdiLaunch& A, const FilmDev<T>& D, const FieldRef& fr, int s
 // Autotuner of the FP32 ADI sweeps, run once at context creation (outside
 // any stream capture): every warp-solver shape of each sweep and the
 // one-thread-per-line kernel are timed on this context's buffers (node 0
-// filled, a zero field) at step 1 with both chains, twice, four launches
-// each after one warm-up launch, with CUDA events on the context stream;
-// each sweep keeps its fastest.  The x sweep runs first and
+// filled, a zero field) at step 1 with both chains: a CUDA graph of eight
+// back-to-back sweeps, launched once to warm up and then timed three times
+// with CUDA events on the context stream (the minimum counts); each sweep
+// keeps its fastest.  The x sweep runs first and
 // the z sweep last, so every candidate reads finite values written by the
 // sweep before it.  Shapes are cached per (device, grid).  Shapes differ in
 // the order of the FP32 line-solve arithmetic (results agree to rounding);
@@ -193,18 +194,36 @@ int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldR
     std::vector<AdiShape> cand = adi_shapes(d, D);
     cand.push_back({0, 0, 0});
     std::vector<float> us(cand.size(), 1e30f);
-    for (int round = 0; round < 2; ++round)
-      for (size_t c = 0; c < cand.size(); ++c) {
-        A.sh[d] = cand[c];
-        adi_sweep<float>(d, A, D, fr, 1, 2, s);
+    // each candidate as a graph of eight back-to-back sweeps, as the
+    // iteration graph runs them (stream launches of ~5 us kernels would time
+    // the host's launch rate)
+    constexpr int kReps = 8;
+    for (size_t c = 0; c < cand.size(); ++c) {
+      A.sh[d] = cand[c];
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      for (int r = 0; r < kReps; ++r) adi_sweep<float>(d, A, D, fr, 1, 2, s);
+      CK(cudaStreamEndCapture(s, &g));
+      const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      CK(ie);
+      for (int round = 0; round < 3; ++round) {
+        cudaGraphLaunch(ge, s);
         cudaEventRecord(e0, s);
-        for (int r = 0; r < 4; ++r) adi_sweep<float>(d, A, D, fr, 1, 2, s);
+        cudaGraphLaunch(ge, s);
         cudaEventRecord(e1, s);
-        CK(cudaEventSynchronize(e1));
+        const cudaError_t se = cudaEventSynchronize(e1);
+        if (se != cudaSuccess) {
+          cudaGraphExecDestroy(ge);
+          CK(se);
+        }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        us[c] = std::min(us[c], 250.f * ms);
+        us[c] = std::min(us[c], 1000.f * ms / kReps);
       }
+      cudaGraphExecDestroy(ge);
+    }
     size_t best = 0;
     for (size_t c = 1; c < cand.size(); ++c)
       if (us[c] < us[best]) best = c;
