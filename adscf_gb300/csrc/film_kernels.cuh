@@ -526,6 +526,7 @@ __device__ __forceinline__ void film_contour_body(const FilmDev<T>& F, int bid, 
         }
         __syncthreads();
         if (ok) {
+#pragma unroll 8
           for (int k = 0; k < cn; ++k) {
             const int s = s0 + k;
             const float x = F.q[(size_t)s * np + p], y = F.qd[(size_t)(N - s) * np + p];
