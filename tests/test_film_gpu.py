@@ -177,6 +177,27 @@ def test_film3d_every_adi_shape_vs_oracle(rng):
             c.set_adi_plan(8, 16, 8, 1)   # the x sweep has no staged form
 
 
+@pytest.mark.parametrize("geom,grid", [(FILM_3D, (8, 6, 16)), (FILM_1D, (1, 1, 24))])
+def test_film_scf_iteration_host_buffers(geom, grid, rng):
+    """adscf_scf_iteration on films (the densities copied to the host beside
+    the solve and the mix) gives the field and densities of scf_run(1)."""
+    gx, gy, gz = grid
+    dz, zr = of.generate_mesh(0, gz, 3.0)
+    size = (1.6, 1.2, 3.0) if geom == FILM_3D else (1.0, 1.0, 3.0)
+    field = 0.3 * rng.standard_normal((2, gz + 1, gy, gx))
+    kw = dict(ds=0.02, f=(0.3, 0.7), prec=SPLIT, kappa=10.0, chi=12.0, mixing_type=MIX_LAMBDA,
+              lam=0.1, ensemble=2, mu=1.0)
+    with film_ctx(geom, grid, dz, size, **kw) as c:
+        c.set_field(field)
+        c.scf_run(1)
+        x1, d1 = c.get_field(), c.get_density()
+    with film_ctx(geom, grid, dz, size, **kw) as c:
+        c.set_field(field)
+        x2, d2, res = c.scf_iteration(field.reshape(-1))
+    assert res.iter == 1
+    assert np.array_equal(x1.reshape(-1), x2) and np.array_equal(d1.reshape(-1), d2.reshape(-1))
+
+
 def test_brush_propagate_homopolymer(rng):
     gz, D = 80, 5.0
     dz, zr = of.generate_mesh(0, gz, D)
