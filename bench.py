@@ -46,8 +46,9 @@ SEED = 3
 DSTEP_TRAFFIC = 17_531_648
 # L2 traffic of one 128^3 double step from the SM side, measured with ncu
 # (lts__t_sectors_srcunit_tex.sum x 32 B of one launch each of the fused XY
-# plane pass, 2,803,707 sectors, and of the TMA Z pass, 1,247,065 sectors)
-DSTEP_L2_BYTES = (2_803_707 + 1_247_065) * 32
+# plane pass, 2,754,213 sectors, and of the TMA Z pass, 1,190,085 sectors;
+# profiles/k_xy_tma_k_rs_tma_128cube_full.txt)
+DSTEP_L2_BYTES = (2_754_213 + 1_190_085) * 32
 
 
 def c3_fields(n=GRID, length=L, seed=SEED):
