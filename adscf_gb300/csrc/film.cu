@@ -144,8 +144,8 @@ void adi_step(const AdiLaunch& A, const FilmDev<T>& D, const FieldRef& fr, int s
 // Autotuner of the FP32 ADI sweeps, run once at context creation (outside
 // any stream capture): every warp-solver shape of each sweep and the
 // one-thread-per-line kernel are timed on this context's buffers (node 0
-// filled, a zero field) at step 1 with both chains: a CUDA graph of eight
-// back-to-back sweeps, launched once to warm up and then timed three times
+// filled, a zero field) at step 1 with both chains: a CUDA graph of sixteen
+// back-to-back sweeps, launched once to warm up and then timed five times
 // with CUDA events on the context stream (the minimum counts); each sweep
 // keeps its fastest.  The x sweep runs first and
 // the z sweep last, so every candidate reads finite values written by the
@@ -194,10 +194,10 @@ int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldR
     std::vector<AdiShape> cand = adi_shapes(d, D);
     cand.push_back({0, 0, 0});
     std::vector<float> us(cand.size(), 1e30f);
-    // each candidate as a graph of eight back-to-back sweeps, as the
+    // each candidate as a graph of sixteen back-to-back sweeps, as the
     // iteration graph runs them (stream launches of ~5 us kernels would time
     // the host's launch rate)
-    constexpr int kReps = 8;
+    constexpr int kReps = 16;
     for (size_t c = 0; c < cand.size(); ++c) {
       A.sh[d] = cand[c];
       cudaGraph_t g = nullptr;
@@ -208,7 +208,7 @@ int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldR
       const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
       cudaGraphDestroy(g);
       CK(ie);
-      for (int round = 0; round < 3; ++round) {
+      for (int round = 0; round < 5; ++round) {
         cudaGraphLaunch(ge, s);
         cudaEventRecord(e0, s);
         cudaGraphLaunch(ge, s);

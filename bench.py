@@ -422,6 +422,7 @@ def film3d_leg(torch, A, stream, steps):
         ms = e0.elapsed_time(e1) / steps
         res = c.scf_run(0)
         launches = c.lib.adscf_stage_launches(c.h, 0)
+        tuning = c.tuning()
     ns = len(kw["dss"]) - 1
     lines = 2 * ns * (64 * 63 + 64 * 63 + 64 * 64)   # x, y and z line solves, both chains
     return {"workload": "C4: Film_3D diblock, 64x64 lateral L=6, 64-interval tanh z mesh, D=3, "
@@ -429,7 +430,8 @@ def film3d_leg(torch, A, stream, steps):
                         "ADI, split",
             "ms_per_iter": ms, "iter_s": 1000.0 / ms, "line_solves_s": lines * 1000.0 / ms,
             "contour_steps_s": 2 * ns * 1000.0 / ms, "launches_per_iter": launches,
-            "accuracy": res.accuracy, "status": res.status}
+            "accuracy": res.accuracy, "status": res.status,
+            "adi_plan": tuning[tuning.index("adi"):] if "adi" in tuning else tuning}
 
 
 def time_batch(torch, A, inst, fields, stream, steps, warmup):
