@@ -249,10 +249,12 @@ template <int NS>
 __global__ void __launch_bounds__(SCF_THREADS, NS <= 11 ? 4 : 3)
 k_closure(ScfDev S, int flags) { closure_body<NS>(S, flags, blockIdx.x, gridDim.x); }
 
+// held to the register budget of k_closure (the instance's ScfDev is read in
+// place from global memory rather than copied into registers)
 template <int NS>
-__global__ void __launch_bounds__(SCF_THREADS)
+__global__ void __launch_bounds__(SCF_THREADS, NS <= 11 ? 4 : 3)
 k_closure_b(const ScfDev* __restrict__ Ss, int flags) {
-  const ScfDev S = Ss[blockIdx.y];
+  const ScfDev& S = Ss[blockIdx.y];
   if ((int)blockIdx.x >= S.npart_blocks) return;
   closure_body<NS>(S, flags, blockIdx.x, S.npart_blocks);
 }
