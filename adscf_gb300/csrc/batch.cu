@@ -79,6 +79,7 @@ struct adscf_batch {
   int* d_ctl = nullptr;
   void* d_ranges = nullptr;             // SweepRange per class
   int sweep_grid = 0;
+  int sweep_help = 0;                   // class with the most point-steps (finished CTAs help it)
   size_t sweep_smem = 0;
   bool sweep = true;                    // persistent sweeps (ADSCF_BATCH_SWEEP=0: one launch per pass)
   int sweep_tiles = 8;                  // tiles per sweep item (ADSCF_SWEEP_TILES)
@@ -192,7 +193,8 @@ int check_params(const adscf_params& q, int prec, std::string& why) {
 // FFT of one cubic size, or the generic mixed-radix passes); each class gets
 // a range of the CTAs in proportion to its point-steps and runs its own
 // instantiation of the tile functions, so the classes share the GPU without
-// sharing registers.  The host lists each class's work items in dependency
+// sharing registers; a CTA whose class has run out of items then takes items
+// of the class with the most work, which finishes last.  The host lists each class's work items in dependency
 // order -- X of node 0, then per step t the Yf, Z, Yi and X passes -- with the
 // instances interleaved within each pass; an item is a few tiles of one pass
 // of one instance and carries the number of items of that instance listed
@@ -245,11 +247,12 @@ __device__ __forceinline__ void sweep_tile(const BulkDev<T>* insts, int2 w, int 
 // barrier, while thread 0 waits.  An item reserved early waits only on items
 // taken before it, and a release never waits, so neither can deadlock.
 template <typename T, int N>
-__device__ __forceinline__ void sweep_class(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ items,
+__device__ __forceinline__ bool sweep_class(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ items,
                                             int nitems, int* next, int* err, int* done_all, int* s_q,
                                             const cplx<T>* __restrict__ tw, const T* __restrict__ fk,
                                             const double* __restrict__ g64, unsigned char* smraw) {
   int pend = -1;                         // instance of the finished, unreleased item
+  __syncthreads();                       // every thread has read s_q of the class before
   if (threadIdx.x == 0) s_q[0] = atomicAdd(next, 1);
   for (int par = 0;; par ^= 1) {
     __syncthreads();                     // the previous item's stores are issued; s_q[par] is set
@@ -271,7 +274,7 @@ __device__ __forceinline__ void sweep_class(const BulkDev<T>* __restrict__ insts
       __threadfence();                   // the CTA's loads of the item follow the producers' stores
       s_q[par ^ 1] = ok ? atomicAdd(next, 1) : nitems;
     }
-    if (__syncthreads_or(!ok)) break;
+    if (__syncthreads_or(!ok)) return false;
     const int pass = it.z & 7, t = it.z >> 3;
     const int tile0 = it.y & 0xfffff, nt = it.y >> 20;
     for (int j = 0; j < nt; ++j) {
@@ -280,6 +283,7 @@ __device__ __forceinline__ void sweep_class(const BulkDev<T>* __restrict__ insts
     }
     pend = it.x;
   }
+  return true;
 }
 
 // Kernel class of a CTA range of the sweep: line length n (0: generic), its
@@ -289,6 +293,26 @@ struct SweepRange {
 };
 constexpr int kMaxSweepClasses = 8;
 
+// run class c of the sweep until its items run out (false: a bounded wait
+// ran out)
+template <typename T>
+__device__ __forceinline__ bool sweep_dispatch(const SweepRange R, int c, const BulkDev<T>* __restrict__ insts,
+                                               const int4* __restrict__ items, int* ctl, int* err, int* done,
+                                               int* s_q, const cplx<T>* __restrict__ tw, const T* __restrict__ fk,
+                                               const double* __restrict__ g64, unsigned char* smraw) {
+  const int4* it = items + R.off;
+  switch (R.n) {
+    case 24: return sweep_class<T, 24>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
+    case 32: return sweep_class<T, 32>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
+    case 40: return sweep_class<T, 40>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
+    case 48: return sweep_class<T, 48>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
+    case 64: return sweep_class<T, 64>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
+    case 128: return sweep_class<T, 128>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
+    case 256: return sweep_class<T, 256>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
+    default: return sweep_class<T, 0>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
+  }
+}
+
 // One launch for every class: the CTAs of range c work on class c only, so
 // each class keeps its share of the GPU whatever the others do; each range
 // runs the class's own instantiation of the loop (inlined).  ctl: [class
@@ -296,26 +320,18 @@ constexpr int kMaxSweepClasses = 8;
 template <typename T>
 __global__ void __launch_bounds__(BULK_THREADS, 2)
 k_batch_sweep(const BulkDev<T>* __restrict__ insts, const int4* __restrict__ items,
-              const SweepRange* __restrict__ ranges, int ncls, int* __restrict__ ctl,
+              const SweepRange* __restrict__ ranges, int ncls, int help, int* __restrict__ ctl,
               const cplx<T>* __restrict__ tw, const T* __restrict__ fk, const double* __restrict__ g64) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ int s_q[2];
   int c = 0;
   while (c + 1 < ncls && (int)blockIdx.x >= ranges[c + 1].cta0) ++c;
-  const SweepRange R = ranges[c];
-  const int4* it = items + R.off;
   int* err = ctl + ncls;
   int* done = err + 1;
-  switch (R.n) {
-    case 24: sweep_class<T, 24>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
-    case 32: sweep_class<T, 32>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
-    case 40: sweep_class<T, 40>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
-    case 48: sweep_class<T, 48>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
-    case 64: sweep_class<T, 64>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
-    case 128: sweep_class<T, 128>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
-    case 256: sweep_class<T, 256>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw); break;
-    default: sweep_class<T, 0>(insts, it, R.count, ctl + c, err, done, s_q, tw, fk, g64, smraw);
-  }
+  // the CTA's own class, then (once its class has run out of items) the class
+  // with the most work, which finishes last
+  if (!sweep_dispatch<T>(ranges[c], c, insts, items, ctl, err, done, s_q, tw, fk, g64, smraw)) return;
+  if (c != help) sweep_dispatch<T>(ranges[help], help, insts, items, ctl, err, done, s_q, tw, fk, g64, smraw);
 }
 
 template <typename T>
@@ -584,6 +600,8 @@ int build(adscf_batch* b) {
       cta += share;
     }
     b->sweep_grid = cta;
+    for (int c = 1; c < ncls; ++c)
+      if (work[c] > work[b->sweep_help]) b->sweep_help = c;
     BK(cudaMalloc(&b->d_ranges, rg.size() * sizeof(SweepRange)));
     BK(cudaMemcpyAsync(b->d_ranges, rg.data(), rg.size() * sizeof(SweepRange), cudaMemcpyHostToDevice, b->stream));
   }
@@ -896,7 +914,7 @@ int enqueue_propagation(adscf_batch* b) {
     const int ncls = (int)b->sw.size();
     BK(cudaMemsetAsync(b->d_ctl, 0, (ncls + 1 + (size_t)b->n) * sizeof(int), s));
     k_batch_sweep<T><<<b->sweep_grid, BULK_THREADS, b->sweep_smem, s>>>(
-        d, b->d_items, static_cast<const SweepRange*>(b->d_ranges), ncls, b->d_ctl, tw, fk, g64);
+        d, b->d_items, static_cast<const SweepRange*>(b->d_ranges), ncls, b->sweep_help, b->d_ctl, tw, fk, g64);
     k_bulk_contour<T><<<dim3(b->cont_blocks, b->n), BULK_THREADS, 0, s>>>(d);
     BK(cudaGetLastError());
     return ADSCF_OK;
