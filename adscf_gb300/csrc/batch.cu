@@ -100,6 +100,7 @@ struct adscf_batch {
   int zcap32 = 0, zcap64 = 0, lanes32 = 0, lanes64 = 0;
   int film_per_warp = 2, film_warps = 2;
   int max_slots = 2;                    // longest mixing history of the instances
+  int film_cl_threads = SCF_THREADS;    // closure and solve block of a film batch
   float* d_tabf = nullptr;              // FP32 mesh factors of the FP32 sweeps
   int* d_err = nullptr;                 // zero-pivot flag of the sweeps
   // FP64 bulk batches: host copies of the instances and the adjoint state
@@ -797,6 +798,9 @@ int build_film(adscf_batch* b) {
   };
   std::stable_sort(l32.begin(), l32.end(), by_work);
   std::stable_sort(l64.begin(), l64.end(), by_work);
+  long long max_npts = 0;
+  for (int i = 0; i < n; ++i) max_npts = std::max<long long>(max_npts, b->npts[i]);
+  b->film_cl_threads = closure_threads(max_npts);
   b->n32 = (int)l32.size();
   b->n64 = (int)l64.size();
   // layout of the shared-memory sweeps: one thread per (film, chain) runs a
@@ -880,8 +884,9 @@ int enqueue_film(adscf_batch* b) {
   }
   if (b->n32) k_film_contour_b<float><<<b->n32, 256, 0, s>>>(f32, b->d_list32);
   if (b->n64) k_film_contour_b<double><<<b->n64, 256, 0, s>>>(f64, b->d_list64);
-  launch_closure_b(b->d_S, b->max_slots, CL_MEANFIELD | CL_MIXDOTS, dim3(1, b->n), s);
-  k_solve_b<<<b->n, SOLVE_THREADS, 0, s>>>(b->d_S, 1, 1);
+  launch_closure_b(b->d_S, b->max_slots, CL_MEANFIELD | CL_MIXDOTS, dim3(1, b->n), s, b->film_cl_threads);
+  // each partial is summed by one warp whatever the block size
+  k_solve_b<<<b->n, b->film_cl_threads, 0, s>>>(b->d_S, 1, 1);
   k_mix_b<float><<<dim3(1, b->n), SCF_THREADS, 0, s>>>(b->d_S, 1);
   BK(cudaGetLastError());
   return ADSCF_OK;

@@ -116,8 +116,14 @@ enum { CL_MEANFIELD = 1, CL_MIXDOTS = 2, CL_KEEP_OLD = 4, CL_CONJ = 8 };
 // batch of independent instances: instance blockIdx.y (closure, mix) or
 // blockIdx.x (solve) of the ScfDev array, with per-instance partials.
 // closure launches (the kernels are specialised by history length)
+// Threads of a closure block: an instance of at most 256 points (a one-line
+// film or brush, one closure block) takes 64, so a batch of such films runs
+// four times as many closure blocks per SM; alone and in a batch a film sums
+// its points in the same order.
+inline int closure_threads(long long npts) { return npts <= 256 ? 64 : SCF_THREADS; }
 void launch_closure(const ScfDev& S, int flags, int grid, cudaStream_t st);
-void launch_closure_b(const ScfDev* Ss, int max_slots, int flags, dim3 grid, cudaStream_t st);
+void launch_closure_b(const ScfDev* Ss, int max_slots, int flags, dim3 grid, cudaStream_t st,
+                      int threads = SCF_THREADS);
 __global__ void k_mixdots(ScfDev S);
 __global__ void k_solve(ScfDev S, int have_closure, int do_mix);
 __global__ void k_solve_b(const ScfDev* __restrict__ Ss, int have_closure, int do_mix);
@@ -260,14 +266,15 @@ k_closure_b(const ScfDev* __restrict__ Ss, int flags) {
 }
 
 void launch_closure(const ScfDev& S, int flags, int grid, cudaStream_t st) {
-  if (S.slots <= 3) k_closure<3><<<grid, SCF_THREADS, 0, st>>>(S, flags);
-  else if (S.slots <= 11) k_closure<11><<<grid, SCF_THREADS, 0, st>>>(S, flags);
-  else k_closure<SCF_MAX_SLOTS><<<grid, SCF_THREADS, 0, st>>>(S, flags);
+  const int nt = closure_threads(S.npts);
+  if (S.slots <= 3) k_closure<3><<<grid, nt, 0, st>>>(S, flags);
+  else if (S.slots <= 11) k_closure<11><<<grid, nt, 0, st>>>(S, flags);
+  else k_closure<SCF_MAX_SLOTS><<<grid, nt, 0, st>>>(S, flags);
 }
-void launch_closure_b(const ScfDev* Ss, int max_slots, int flags, dim3 grid, cudaStream_t st) {
-  if (max_slots <= 3) k_closure_b<3><<<grid, SCF_THREADS, 0, st>>>(Ss, flags);
-  else if (max_slots <= 11) k_closure_b<11><<<grid, SCF_THREADS, 0, st>>>(Ss, flags);
-  else k_closure_b<SCF_MAX_SLOTS><<<grid, SCF_THREADS, 0, st>>>(Ss, flags);
+void launch_closure_b(const ScfDev* Ss, int max_slots, int flags, dim3 grid, cudaStream_t st, int threads) {
+  if (max_slots <= 3) k_closure_b<3><<<grid, threads, 0, st>>>(Ss, flags);
+  else if (max_slots <= 11) k_closure_b<11><<<grid, threads, 0, st>>>(Ss, flags);
+  else k_closure_b<SCF_MAX_SLOTS><<<grid, threads, 0, st>>>(Ss, flags);
 }
 
 // Mixing dots only (for adscf_mix): x_k, r_k already in the history slot.
