@@ -43,6 +43,7 @@ struct FilmState {
   // FP32 ADI sweeps x, y, z: warp-solver shape of each (g = 0: one thread
   // per line), from the autotuner or the defaults
   AdiShape adi[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  bool adi_fuse = false;        // x and y sweeps as one plane kernel (shape adi[0])
   bool adi_set = false;
 };
 
@@ -50,6 +51,8 @@ struct FilmState {
 std::vector<AdiShape> adi_shapes(int dim, const FilmDev<float>& D);
 AdiShape adi_default_shape(int dim, const FilmDev<float>& D);
 void adi_warp_sweep(int dim, AdiShape sh, const FilmDev<float>& D, int step, int chains, cudaStream_t s);
+bool adi_fused_ok(AdiShape x, AdiShape y, const FilmDev<float>& D);
+void adi_fused_sweep(AdiShape sh, const FilmDev<float>& D, int step, int chains, cudaStream_t s);
 
 namespace {
 
@@ -96,6 +99,7 @@ struct AdiLaunch {
   int wx, wy, wz;
   size_t sx, sy, sz;
   AdiShape sh[3];   // FP32 warp-solver shapes (g = 0: the kernels above)
+  bool fuse = false;  // FP32: x and y sweeps in one plane kernel of shape sh[0]
 };
 template <typename T>
 AdiLaunch adi_launch(const FilmState* F, const FilmDev<T>& D, int chains) {
@@ -116,6 +120,7 @@ AdiLaunch adi_launch(const FilmState* F, const FilmDev<T>& D, int chains) {
   A.gy = dim3((D.gx * (D.gz - 1) + A.wy - 1) / A.wy, chains);
   A.gz = dim3((D.nlines + A.wz - 1) / A.wz, chains);
   for (int d = 0; d < 3; ++d) A.sh[d] = sizeof(T) == 4 ? F->adi[d] : AdiShape{0, 0, 0};
+  A.fuse = sizeof(T) == 4 && F->adi_fuse;
   return A;
 }
 
@@ -138,6 +143,13 @@ void adi_sweep(int dim, const AdiLaunch& A, const FilmDev<T>& D, const FieldRef&
 // One Douglas ADI step (three sweeps) of `chains` chains.
 template <typename T>
 void adi_step(const AdiLaunch& A, const FilmDev<T>& D, const FieldRef& fr, int st, int chains, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (A.fuse) {
+      adi_fused_sweep(A.sh[0], D, st, chains, s);
+      adi_sweep<T>(2, A, D, fr, st, chains, s);
+      return;
+    }
+  }
   for (int d = 0; d < 3; ++d) adi_sweep<T>(d, A, D, fr, st, chains, s);
 }
 
@@ -160,6 +172,7 @@ struct AdiTuneKey {
 };
 struct AdiTuneVal {
   AdiShape sh[3];
+  bool fuse = false;
   std::string report;
 };
 std::mutex g_adi_mu;
@@ -167,6 +180,7 @@ std::map<AdiTuneKey, AdiTuneVal> g_adi_tune;
 
 void adi_defaults(FilmState* F, const FilmDev<float>& D) {
   for (int d = 0; d < 3; ++d) F->adi[d] = adi_default_shape(d, D);
+  F->adi_fuse = false;
   F->adi_set = true;
 }
 
@@ -177,7 +191,9 @@ int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldR
     auto it = g_adi_tune.find(key);
     if (it != g_adi_tune.end()) {
       for (int d = 0; d < 3; ++d) F->adi[d] = it->second.sh[d];
+      F->adi_fuse = it->second.fuse;
       F->adi_set = true;
+      ctx->film_launches = 1 + (F->adi_fuse ? 2 : 3) * ctx->ns;
       ctx->tune_report = it->second.report + " (cached)";
       return ADSCF_OK;
     }
@@ -190,44 +206,51 @@ int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldR
   std::string rep = "adi";
   static const char* nm[3] = {"x", "y", "z"};
   AdiTuneVal val;
+  // each candidate as a graph of sixteen back-to-back sweeps, as the
+  // iteration graph runs them (stream launches of ~5 us kernels would time
+  // the host's launch rate); the best of five timed launches, in us per sweep
+  constexpr int kReps = 16;
+  auto time_graph = [&](auto&& sweep, float* us) -> int {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int r = 0; r < kReps; ++r) sweep();
+    CK(cudaStreamEndCapture(s, &g));
+    const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    CK(ie);
+    for (int round = 0; round < 5; ++round) {
+      cudaGraphLaunch(ge, s);
+      cudaEventRecord(e0, s);
+      cudaGraphLaunch(ge, s);
+      cudaEventRecord(e1, s);
+      const cudaError_t se = cudaEventSynchronize(e1);
+      if (se != cudaSuccess) {
+        cudaGraphExecDestroy(ge);
+        CK(se);
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      *us = std::min(*us, 1000.f * ms / kReps);
+    }
+    cudaGraphExecDestroy(ge);
+    return ADSCF_OK;
+  };
+  float best_us[3] = {0.f, 0.f, 0.f};
   for (int d = 0; d < 3; ++d) {
     std::vector<AdiShape> cand = adi_shapes(d, D);
     cand.push_back({0, 0, 0});
     std::vector<float> us(cand.size(), 1e30f);
-    // each candidate as a graph of sixteen back-to-back sweeps, as the
-    // iteration graph runs them (stream launches of ~5 us kernels would time
-    // the host's launch rate)
-    constexpr int kReps = 16;
     for (size_t c = 0; c < cand.size(); ++c) {
       A.sh[d] = cand[c];
-      cudaGraph_t g = nullptr;
-      cudaGraphExec_t ge = nullptr;
-      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      for (int r = 0; r < kReps; ++r) adi_sweep<float>(d, A, D, fr, 1, 2, s);
-      CK(cudaStreamEndCapture(s, &g));
-      const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
-      cudaGraphDestroy(g);
-      CK(ie);
-      for (int round = 0; round < 5; ++round) {
-        cudaGraphLaunch(ge, s);
-        cudaEventRecord(e0, s);
-        cudaGraphLaunch(ge, s);
-        cudaEventRecord(e1, s);
-        const cudaError_t se = cudaEventSynchronize(e1);
-        if (se != cudaSuccess) {
-          cudaGraphExecDestroy(ge);
-          CK(se);
-        }
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        us[c] = std::min(us[c], 1000.f * ms / kReps);
-      }
-      cudaGraphExecDestroy(ge);
+      const int rc = time_graph([&] { adi_sweep<float>(d, A, D, fr, 1, 2, s); }, &us[c]);
+      if (rc) return rc;
     }
     size_t best = 0;
     for (size_t c = 1; c < cand.size(); ++c)
       if (us[c] < us[best]) best = c;
     val.sh[d] = cand[best];
+    best_us[d] = us[best];
     A.sh[d] = cand[best];   // the next sweep's candidates read this one's output
     char line[96];
     std::snprintf(line, sizeof(line), " %s=%dx%d%s", nm[d], cand[best].g, cand[best].k, cand[best].staged ? "s" : "");
@@ -238,10 +261,23 @@ int adi_tune(adscf_ctx* ctx, FilmState* F, const FilmDev<float>& D, const FieldR
       rep += line;
     }
     rep += ";";
+    // after the y sweep: the x + y plane kernel with the x sweep's shape,
+    // where both sweeps chose it, against the two sweeps' times
+    if (d == 1 && adi_fused_ok(val.sh[0], val.sh[1], D)) {
+      float fus = 1e30f;
+      const int rc = time_graph([&] { adi_fused_sweep(val.sh[0], D, 1, 2, s); }, &fus);
+      if (rc) return rc;
+      val.fuse = fus < best_us[0] + best_us[1];
+      std::snprintf(line, sizeof(line), " xy=%s [xy %dx%d %.2f us against %.2f us];", val.fuse ? "fused" : "apart",
+                    val.sh[0].g, val.sh[0].k, fus, best_us[0] + best_us[1]);
+      rep += line;
+    }
   }
   CK(cudaGetLastError());
   for (int d = 0; d < 3; ++d) F->adi[d] = val.sh[d];
+  F->adi_fuse = val.fuse;
   F->adi_set = true;
+  ctx->film_launches = 1 + (F->adi_fuse ? 2 : 3) * ctx->ns;
   val.report = rep;
   ctx->tune_report = rep;
   std::lock_guard<std::mutex> lk(g_adi_mu);
@@ -499,11 +535,14 @@ int film_create(adscf_ctx* ctx, const adscf_params* p) {
   return ADSCF_OK;
 }
 
-// Pin the FP32 ADI sweep shapes by lanes per line (0: one thread per line)
-// and staging through shared memory (mask: 2 y, 4 z).
+// Pin the FP32 ADI sweep shapes by lanes per line (0: one thread per line),
+// staging through shared memory (mask: 2 y, 4 z) and the fused x + y plane
+// kernel (mask 8; the x and y shapes must allow it).
 int film_set_adi_plan(adscf_ctx* ctx, const int lanes[3], int staged) {
   FilmState* F = ctx->film;
   if (ctx->geometry != ADSCF_FILM_3D || F->t64) return ADSCF_E_STATE;
+  const bool fuse = (staged & 8) != 0;
+  staged &= 7;
   AdiShape sh[3];
   for (int d = 0; d < 3; ++d) {
     sh[d] = {0, 0, 0};
@@ -514,8 +553,11 @@ int film_set_adi_plan(adscf_ctx* ctx, const int lanes[3], int staged) {
       if (a.g == lanes[d] && a.staged == st) { sh[d] = a; found = true; }
     if (!found) return ADSCF_E_ARG;
   }
+  if (fuse && !adi_fused_ok(sh[0], sh[1], F->f32)) return ADSCF_E_ARG;
   for (int d = 0; d < 3; ++d) F->adi[d] = sh[d];
+  F->adi_fuse = fuse;
   F->adi_set = true;
+  ctx->film_launches = 1 + (fuse ? 2 : 3) * ctx->ns;
   return ADSCF_OK;
 }
 

@@ -115,6 +115,22 @@ AdiShape adi_default_shape(int dim, const FilmDev<float>& D) {
   return v.back();
 }
 
+// The fused x + y plane sweep (k_adi_xy_p) exists for square planes whose x
+// and y sweeps share one unstaged shape of these sizes (N G <= 1024 threads).
+bool adi_fused_ok(AdiShape x, AdiShape y, const FilmDev<float>& D) {
+  if (x.g != y.g || x.k != y.k || x.staged || y.staged || D.gx != D.gy || D.gx != x.g * x.k) return false;
+  return (x.g == 16 && (x.k == 4 || x.k == 2)) || (x.g == 8 && (x.k == 4 || x.k == 2));
+}
+
+void adi_fused_sweep(AdiShape sh, const FilmDev<float>& D, int step, int chains, cudaStream_t s) {
+  const dim3 g(D.gz - 1, chains);
+  const int nt = sh.g * sh.g * sh.k;
+  if (sh.g == 16 && sh.k == 4) k_adi_xy_p<16, 4><<<g, nt, 0, s>>>(D, step);
+  else if (sh.g == 16) k_adi_xy_p<16, 2><<<g, nt, 0, s>>>(D, step);
+  else if (sh.k == 4) k_adi_xy_p<8, 4><<<g, nt, 0, s>>>(D, step);
+  else k_adi_xy_p<8, 2><<<g, nt, 0, s>>>(D, step);
+}
+
 void adi_warp_sweep(int dim, AdiShape sh, const FilmDev<float>& D, int step, int chains, cudaStream_t s) {
   const int G = sh.g, K = sh.k;
   if (dim == 0) {

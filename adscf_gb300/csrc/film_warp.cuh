@@ -389,6 +389,93 @@ k_adi_y_w(FilmDev<float> F, int s) {
   }
 }
 
+// x and y sweeps of one interior plane in one block (gx = gy = N = G K, all N
+// lines of a sweep at once: N G threads).  The plane of the previous slice
+// and the x sweep's result stay in shared memory ([y][x]), so the y sweep
+// reads no global memory and the plane leaves once, row by row.  Right-hand
+// sides, matrices and solver are those of k_adi_x_w and k_adi_y_w with the
+// same shape, operation for operation; the neighbouring planes z - 1 and
+// z + 1 (the x sweep's z couplings) are read from global memory as there.
+// grid (gz - 1 planes, chains).
+template <int G, int K>
+__global__ void __launch_bounds__(G * K * G, 1)
+k_adi_xy_p(FilmDev<float> F, int s) {
+  constexpr int N = G * K;                 // points of an x or a y line
+  constexpr int LPW = 32 / G;              // lines per warp
+  static_assert(N * G <= 1024 && N % LPW == 0, "one block holds every line of the plane");
+  __shared__ float P[N * N];               // previous slice, plane z
+  __shared__ float Wp[N * N];              // x sweep's result, then the y sweep's
+  const int L = F.nlines;                  // = N * N
+  const int z = 1 + blockIdx.x, dir = blockIdx.y;
+  const int lane = threadIdx.x & 31, gl = lane & (G - 1);
+  const int line = (threadIdx.x >> 5) * LPW + lane / G;   // y for the x sweep, x for the y sweep
+  const AdiCoef cf = adi_coef(F, dir, s);
+  const int ty = (F.brush || F.single) ? 0 : film_type(dir, s, F.ns, F.na);
+  const float* p0 = (dir == 0 ? F.q : F.qd) + (size_t)(s - 1) * F.npts;
+  float* out = F.w1 + (size_t)dir * F.npts;
+  const float* wf = F.wf + (size_t)ty * F.npts;
+  const size_t pz = (size_t)z * L;
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) P[i] = __ldg(p0 + pz + i);
+  __syncthreads();
+  const int base = lane - gl;
+  {  // x sweep: line y, lane points x0 .. x0 + K - 1
+    const int y = line, x0 = gl * K;
+    const float ax = cf.ax, bx = cf.bx, cx = ax;
+    const float ay = cf.ay, cy = ay;
+    const float az = __fmul_rn(-cf.dsf, F.alf[z]), cz = __fmul_rn(-cf.dsf, F.gaf[z]);
+    const int ym = (y + N - 1) % N, yp = (y + 1) % N;
+    const size_t row = pz + (size_t)y * N, rzm = row - L, rzp = row + L;
+    float c0[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) c0[i] = P[y * N + x0 + i];
+    const float left = __shfl_sync(0xffffffffu, c0[K - 1], base + ((gl - 1) & (G - 1)));
+    const float right = __shfl_sync(0xffffffffu, c0[0], base + ((gl + 1) & (G - 1)));
+    float a[K], d[K], c[K], r[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const int x = x0 + i;
+      const float qxm = i == 0 ? left : c0[i > 0 ? i - 1 : 0];
+      const float qxp = i == K - 1 ? right : c0[i + 1 < K ? i + 1 : i];
+      const float qym = P[ym * N + x], qyp = P[yp * N + x];
+      const float qzm = __ldg(p0 + rzm + x), qzp = __ldg(p0 + rzp + x);
+      const float dsw = cf.dsf * wf[row + x];
+      const float q0 = c0[i];
+      r[i] = -2.f * (ax * (qxm - q0) + cx * (qxp - q0) + ay * (qym - q0) + cy * (qyp - q0) +
+                     az * (qzm - q0) + cz * (qzp - q0)) - dsw * q0;
+      a[i] = ax; c[i] = cx; d[i] = 1.f + bx;
+    }
+    fw::solve<G, K>(a, d, c, r, true, F.err);
+#pragma unroll
+    for (int i = 0; i < K; ++i) Wp[y * N + x0 + i] = c0[i] + r[i];
+  }
+  __syncthreads();
+  {  // y sweep: line x, lane points y0 .. y0 + K - 1; each lane rewrites only its own points
+    const int x = line, y0 = gl * K;
+    const float ay = cf.ay, by = cf.by, cy = ay;
+    float e[K], ws[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      ws[i] = Wp[(y0 + i) * N + x];
+      e[i] = P[(y0 + i) * N + x] - ws[i];
+    }
+    const float left = __shfl_sync(0xffffffffu, e[K - 1], base + ((gl - 1) & (G - 1)));
+    const float right = __shfl_sync(0xffffffffu, e[0], base + ((gl + 1) & (G - 1)));
+    float a[K], d[K], c[K], r[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const float em = i == 0 ? left : e[i > 0 ? i - 1 : 0];
+      const float ep = i == K - 1 ? right : e[i + 1 < K ? i + 1 : i];
+      r[i] = ay * (em - e[i]) + cy * (ep - e[i]);
+      a[i] = ay; c[i] = cy; d[i] = 1.f + by;
+    }
+    fw::solve<G, K>(a, d, c, r, true, F.err);
+#pragma unroll
+    for (int i = 0; i < K; ++i) Wp[(y0 + i) * N + x] = ws[i] + r[i];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) out[pz + i] = Wp[i];
+}
+
 template <int G, int K>
 __global__ void __launch_bounds__(128)
 k_adi_z_w(FilmDev<float> F, int s) {

@@ -257,8 +257,9 @@ class Context:
 
     def set_adi_plan(self, x_lanes, y_lanes, z_lanes, staged=0):
         """Pin the lanes per line of the FP32 ADI sweeps of a Film_3D context
-        (0: one thread per line) and their staging through shared memory
-        (mask: 2 for y, 4 for z)."""
+        (0: one thread per line), their staging through shared memory
+        (mask: 2 for y, 4 for z) and the x and y sweeps as one plane kernel
+        (mask 8: x and y with one shape on a square plane)."""
         self._ck(self.lib.adscf_set_adi_plan(self.h, int(x_lanes), int(y_lanes), int(z_lanes),
                                              int(staged)))
 

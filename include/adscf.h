@@ -274,10 +274,14 @@ ADSCF_API int adscf_set_pass_plan(adscf_ctx *ctx, int y, int z, int x);
  * context's buffers and each sweep keeps its fastest (cached per device and
  * grid; ADSCF_AUTOTUNE=0 keeps the defaults).  Shapes order the FP32
  * line-solve arithmetic differently, so results agree to FP32 rounding, not
- * bit for bit.  adscf_tuning reports the choice and the timings ("GxK", "s"
- * for staged); adscf_set_adi_plan pins lanes per line for each sweep (0: one
- * thread per line) and staging (mask: 2 y, 4 z); ADSCF_E_ARG if no shape
- * matches, ADSCF_E_STATE for other contexts.                               */
+ * bit for bit.  On a square plane whose x and y sweeps chose one unstaged
+ * shape (16 or 8 lanes, 2 or 4 points each), the two sweeps as one kernel
+ * per plane and chain (the plane held in shared memory, the same arithmetic)
+ * are timed too and kept if faster ("xy=fused").  adscf_tuning reports the
+ * choice and the timings ("GxK", "s" for staged); adscf_set_adi_plan pins
+ * lanes per line for each sweep (0: one thread per line), staging (mask: 2 y,
+ * 4 z) and the fused x + y kernel (mask 8); ADSCF_E_ARG if no shape matches,
+ * ADSCF_E_STATE for other contexts.                                        */
 ADSCF_API int adscf_set_adi_plan(adscf_ctx *ctx, int x_lanes, int y_lanes, int z_lanes, int staged);
 
 /* ---- differentiation (bulk, FP64 context, canonical ensemble) ----------

@@ -177,6 +177,34 @@ def test_film3d_every_adi_shape_vs_oracle(rng):
             c.set_adi_plan(8, 16, 8, 1)   # the x sweep has no staged form
 
 
+@pytest.mark.parametrize("n,lanes", [(32, 16), (32, 8), (64, 16)])
+def test_film3d_fused_xy_sweep(n, lanes, rng):
+    """The x and y ADI sweeps as one plane kernel (mask 8) against the two
+    sweeps of the same shape (the same arithmetic) and against the FP64
+    oracle; refused when the x and y shapes differ."""
+    gx = gy = n
+    gz, ds = 12, 0.01
+    dz, zr = of.generate_mesh(0, gz, 3.0)
+    size = (3.2, 3.2, 3.0)
+    field = 0.5 * rng.standard_normal((2, gz + 1, gy, gx))
+    dss = np.r_[0.0, np.full(40, ds)]   # blocks of 10 and 30 steps
+    step = lambda p, w, h: of.adi_step_3d(p, w, dz, size[0] / gx, size[1] / gy, h)
+    ref = of.film_propagate_diblock(field, dz, dss, 10, step, dx=size[0] / gx,
+                                    dy=size[1] / gy, int_scheme=1, span="full", sizes=size)
+    with film_ctx(FILM_3D, (gx, gy, gz), dz, size, ds, f=(0.1, 0.3), prec=SPLIT) as c:
+        c.set_adi_plan(lanes, lanes, 8, 0)
+        d0, r0 = c.propagate_diblock(field)
+        c.set_adi_plan(lanes, lanes, 8, 8)
+        d1, r1 = c.propagate_diblock(field)
+        assert abs(np.log(r1.Qsum) - np.log(r0.Qsum)) < 1e-9
+        assert np.max(np.abs(d1 - d0)) <= 1e-7 * np.max(np.abs(d0))
+        assert abs(np.log(r1.Qsum) - np.log(ref["Qsum"])) < 2e-6
+        assert np.max(np.abs(d1 - ref["density"])) < 2e-6 * np.max(np.abs(ref["density"]))
+        other = 8 if lanes == 16 else 16
+        with pytest.raises(AdscfError):
+            c.set_adi_plan(lanes, other, 8, 8)
+
+
 @pytest.mark.parametrize("geom,grid", [(FILM_3D, (8, 6, 16)), (FILM_1D, (1, 1, 24))])
 def test_film_scf_iteration_host_buffers(geom, grid, rng):
     """adscf_scf_iteration on films (the densities copied to the host beside
