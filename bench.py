@@ -505,7 +505,8 @@ def run_profile_workload(name, adi_plan=None):
     """One SCF iteration of a film or batch workload for a launch list:
     c4 (Film_3D, 64 x 64 x 65, ADI), c2 (4096 films), c5 (256 bulk
     instances), after two untimed iterations.  For c4 the ADI plan in use is
-    printed as "adi plan x,y,z,staged"; ``adi_plan`` pins one (with
+    printed as "adi plan x,y,z,mask" (mask: 2 y staged, 4 z staged, 8 x and
+    y fused); ``adi_plan`` pins one (with
     ADSCF_AUTOTUNE=0 the context skips the tuner's candidate launches, whose
     timings mean nothing under a profiler)."""
     import adscf_gb300 as A
@@ -523,7 +524,7 @@ def run_profile_workload(name, adi_plan=None):
         if adi_plan:
             print("adi plan " + ",".join(str(v) for v in adi_plan))
         elif chosen:
-            mask = (2 if chosen["y"][1] else 0) + (4 if chosen["z"][1] else 0)
+            mask = (2 if chosen["y"][1] else 0) + (4 if chosen["z"][1] else 0) + (8 if "xy=fused" in rep else 0)
             print(f"adi plan {chosen['x'][0]},{chosen['y'][0]},{chosen['z'][0]},{mask}")
     else:
         inst, fields = c2_films(A) if name == "c2" else c5_bulk(A)
