@@ -882,7 +882,9 @@ int enqueue_film(adscf_batch* b) {
     k_film1d_chains_b<double><<<dim3((b->n64 + FILM_THREADS - 1) / FILM_THREADS, 2), FILM_THREADS, 0, s>>>(
         f64, b->d_S, b->d_list64, b->n64);
   }
-  if (b->n32) k_film_contour_b<float><<<b->n32, 256, 0, s>>>(f32, b->d_list32);
+  // one-line films: blocks of 128 points, twice as many resident films as
+  // with 256 (a longer line takes its points in passes)
+  if (b->n32) k_film_contour_b<float><<<b->n32, 128, 0, s>>>(f32, b->d_list32);
   if (b->n64) k_film_contour_b<double><<<b->n64, 256, 0, s>>>(f64, b->d_list64);
   launch_closure_b(b->d_S, b->max_slots, CL_MEANFIELD | CL_MIXDOTS, dim3(1, b->n), s, b->film_cl_threads);
   // each partial is summed by one warp whatever the block size
