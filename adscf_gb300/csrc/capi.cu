@@ -169,6 +169,7 @@ int validate(const adscf_params* p, std::string& why) {
   if (p->ensemble != 1 && p->ensemble != 2) { why = "ensemble"; return ADSCF_E_ARG; }
   if (!(p->sizex > 0 && p->sizey > 0 && p->sizez > 0)) { why = "box size"; return ADSCF_E_ARG; }
   if (p->geometry != ADSCF_BULK && !p->dz) { why = "films need dz"; return ADSCF_E_ARG; }
+  if (p->geometry != ADSCF_BULK && p->gz < 2) { why = "films need an interior plane (gz >= 2)"; return ADSCF_E_ARG; }
   if (!p->dss && !(p->ds > 0)) { why = "ds"; return ADSCF_E_ARG; }
   if (p->nblocks) {
     if (p->geometry != ADSCF_BULK) { why = "block sequences are for bulk contexts"; return ADSCF_E_ARG; }

@@ -58,7 +58,7 @@ enum { ADSCF_MIX_SIMPLE = 1, ADSCF_MIX_LAMBDA = 2, ADSCF_MIX_ANDERSON = 3 };
 
 typedef struct adscf_params {
   int geometry;             /* ADSCF_BULK, ADSCF_FILM_1D, ADSCF_FILM_3D, ADSCF_BRUSH */
-  int gx, gy, gz;           /* bulk: grid points; films/brush: gz intervals, planes 0..gz */
+  int gx, gy, gz;           /* bulk: grid points; films/brush: gz >= 2 intervals, planes 0..gz */
   double sizex, sizey, sizez;
   double ds;                /* uniform contour step (input_general)          */
   const double *dss;        /* optional [ns+1] contour steps, dss[0] = 0

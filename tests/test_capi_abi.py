@@ -176,6 +176,37 @@ def test_status_strings_without_gpu(lib):
     assert lib.adscf_status_string(3).decode() == "zero tridiagonal pivot"
 
 
+def test_invalid_params_rejected_without_gpu(lib):
+    """Parameter checks run before any CUDA call: each invalid set of
+    parameters returns ADSCF_E_ARG and no context."""
+    import ctypes as C
+    from adscf_gb300 import _lib
+
+    dz = (C.c_double * 2)(0.5, 0.5)
+
+    def params(**kw):
+        p = _lib.Params()
+        p.geometry, p.gx, p.gy, p.gz = 0, 8, 8, 8
+        p.sizex = p.sizey = p.sizez = 1.0
+        p.ds, p.ensemble, p.precision, p.mixing_type, p.mixing_dim = 0.01, 1, 0, 1, 2
+        p.block_length[0], p.block_length[1] = 0.5, 0.5
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+    cases = [dict(geometry=7), dict(gz=0), dict(precision=5), dict(mixing_type=3, mixing_dim=17),
+             dict(ensemble=3), dict(ds=0.0), dict(sizex=0.0), dict(geometry=1, gx=1, gy=1),
+             dict(geometry=2, gz=1, dz=C.cast(dz, C.POINTER(C.c_double))),
+             dict(geometry=1, gx=1, gy=1, gz=1, dz=C.cast(dz, C.POINTER(C.c_double)))]
+    for kw in cases:
+        ctx = C.c_void_p()
+        p = params(**kw)
+        assert lib.adscf_ctx_create(C.byref(p), C.byref(ctx)) == 1, kw
+        assert not ctx.value, kw
+    ctx = C.c_void_p()
+    assert lib.adscf_ctx_create(None, C.byref(ctx)) == 1
+
+
 def test_missing_library_fails_loudly(tmp_path):
     from adscf_gb300 import _lib
     with pytest.raises(RuntimeError, match="no CPU fallback"):
