@@ -205,6 +205,16 @@ def test_invalid_params_rejected_without_gpu(lib):
         assert not ctx.value, kw
     ctx = C.c_void_p()
     assert lib.adscf_ctx_create(None, C.byref(ctx)) == 1
+    # bulk batches check every instance before any CUDA call
+    for kw in [dict(precision=5), dict(gz=0), dict(ds=0.0), dict(geometry=2)]:
+        arr = (_lib.Params * 2)(params(), params(**kw))
+        if "precision" in kw:
+            arr = (_lib.Params * 2)(params(**kw), params())
+        b = C.c_void_p()
+        assert lib.adscf_batch_create(arr, 2, C.byref(b)) == 1, kw
+        assert not b.value, kw
+    b = C.c_void_p()
+    assert lib.adscf_batch_create((_lib.Params * 1)(params()), 0, C.byref(b)) == 1
 
 
 def test_missing_library_fails_loudly(tmp_path):
